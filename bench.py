@@ -1,0 +1,459 @@
+"""Throughput benchmark: A-scans/s of the GB300 reconstruction.
+
+Workload (default, `--config 1`): synthetic tiled scan, 2 x 2 lateral tiles x
+3 depth stacks, each tile 270 B-scans x (25 apodisation + 1000) A-scans x 2048
+uint16 spectral samples (~1.1 GB, 13.3 GB in all, 3.24 M A-scans), generated
+on the device with the package's seeded spectrum model.  Focus at z = 400 +
+U[-30, 30] px per depth, focus_sigma 80 px, 10 % lateral overlap, refractive
+index 1.33, output 1 um pixels, no optical-path correction.  One step is the
+whole volume: for each y-tile row, every tile's spectral stage, focus-weighted
+stitching, row finalise (dB + per-plane clim); then the global clim and the
+legacy uint16 quantisation of the volume.
+
+`--config 0`: one tile, 50 B-scans x (25 + 500) A-scans, z-crop 1000 px:
+spectral stage to dB, global clim, quantisation.
+
+`value` is measured with inputs resident in HBM (inputs are larger than L2, so
+no flush is needed); `e2e` repeats the step through the same API with the raw
+spectra in pinned host memory (H2D inside the timed region) and reads the
+uint16 volume back (D2H).  `--impl reference` times the reference algorithm's
+CPU restatement (the oracle: Numba kernel restated in C/OpenMP + pocketfft +
+NumPy stitching) on the host cores over bounded samples.
+
+Run:  python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "A-scans/s on 1 GB300 (fused vs plain FP32; learned vs search β) at ≤1 LSB"
+APOD = 25
+
+
+# ------------------------------------------------------------------------ workload description
+def config1_layout(seed=1):
+    from oct_recon_af_v1_gb300 import stitching as S
+    rng = np.random.default_rng(seed)
+    lay = S.ScanLayout(np.array([-0.45, 0.45]), np.array([-0.1215, 0.1215]), np.array([0.0, 0.15, 0.30]),
+                       1000, 270, 1.0, 0.27)
+    focus = 400.0 + rng.uniform(-30, 30, 3)
+    return lay, focus
+
+
+def config1_desc():
+    return {"workload": "config1: 2x2 tiles x 3 depths, tile 270 B-scans x 1000 A-scans x 2048 uint16, "
+                        "focus 400+-30 px sigma 80, 10% overlap, n 1.33, 1 um output, uint16 legacy codes",
+            "a_scans_per_step": 12 * 270 * 1000, "tiles": 12, "bscans_per_tile": 270, "ascans_per_bscan": 1000,
+            "apod_lines": APOD, "spectral_samples": 2048, "l2_flush": "inputs (13.3 GB) larger than L2"}
+
+
+def config0_desc():
+    return {"workload": "config0: 1 tile, 50 B-scans x 500 A-scans x 2048 uint16, z-crop 1000, uint16 codes",
+            "a_scans_per_step": 50 * 500, "l2_flush": "spectral inputs 107 MB + outputs 100 MB cycled over "
+            "8 resident copies (856 MB) so each step reads inputs not left in L2"}
+
+
+# ------------------------------------------------------------------------ clocks sampler
+class Clocks:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons, pw = [], [], set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+                pw.append(float(f[3]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm), "power_w_max": float(max(pw)) if pw else None}
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# ------------------------------------------------------------------------ GPU arm
+class Volume:
+    """Config-1 scan: geometry, stitch plans and the raw tiles (device and/or pinned host)."""
+
+    def __init__(self, ctx, torch, dev, host_copy: bool, seed: int = 1):
+        from oct_recon_af_v1_gb300 import geometry as G
+        from oct_recon_af_v1_gb300 import stitching as S
+        from oct_recon_af_v1_gb300 import synthetic
+        self.lay, self.focus = config1_layout(seed)
+        lam = synthetic.lambda_nm()
+        self.sg = G.build_spectral_geometry(lam, synthetic.beta_ref_from_px(1e-5), 1.33)
+        ctx.set_geometry(self.sg.sinc_idx, self.sg.sinc_w, self.sg.window)
+        self.tg = S.tiled_geometry(self.lay, self.sg.z_um, self.focus, 1.0)
+        self.nz, self.nx = len(self.tg.out_z_mm), len(self.tg.out_x_mm)
+        self.ny = self.lay.n_y_px
+        self.order = [(xi, zi) for xi in range(2) for zi in range(3)]   # x-major, z-minor
+        self.st = {}
+        for xi, zi in self.order:
+            st = S.TileStitcher.build(self.tg, self.lay.x_centers_mm[xi], self.lay.z_depths_mm[zi],
+                                      self.focus[zi], 80.0)
+            st.upload(ctx)
+            self.st[(xi, zi)] = st
+        self.raw = {}
+        self.host = {}
+        k = 0
+        for yi in range(2):
+            for xi, zi in self.order:
+                t = synthetic.u16_bits(synthetic.generate(self.ny, self.lay.n_x_px, APOD, seed=seed * 1000 + k,
+                                                          device=dev, chunk=30))
+                if host_copy:
+                    h = torch.empty(t.shape, dtype=torch.int16, pin_memory=True)
+                    h.copy_(t)
+                    self.host[(yi, xi, zi)] = h
+                self.raw[(yi, xi, zi)] = t
+                k += 1
+        torch.cuda.synchronize()
+        self.thr = S.min_weight_threshold(np.float32)
+        self.frames = np.arange(self.ny)
+
+    def raw_bytes(self):
+        return sum(int(t.numel()) * 2 for t in self.raw.values())
+
+
+def run_step(ctx, vol, src, db_vol, bits, batch=30):
+    """One whole-volume reconstruction; src maps tile keys to device or host int16 tensors."""
+    clims = []
+    for yi in range(2):
+        ctx.row_begin(vol.ny, vol.nz, vol.nx)
+        for xi, zi in vol.order:
+            t = src[(yi, xi, zi)]
+            st = vol.st[(xi, zi)]
+            for s in range(0, vol.ny, batch):
+                ctx.row_add_batch(st.plan, t[s:s + batch], APOD, vol.frames[s:s + batch], s, raw_dtype=0)
+        out = db_vol[yi * vol.ny:(yi + 1) * vol.ny]
+        _, mm = ctx.row_finalise(vol.thr, (vol.ny, vol.nz, vol.nx), out, plane_minmax=True)
+        clims.append(mm)
+    mm = np.concatenate(clims)
+    clim = (float(np.nanmin(mm[:, 0])), float(np.nanmax(mm[:, 1])))
+    ctx.quantise(db_vol, clim, bits)
+    return clim
+
+
+def time_spectral_kernel(ctx, torch, raw_tile, reps=10):
+    """CUDA-event time of the spectral stage (apod mean + fused kernel) on one tile."""
+    B = raw_tile.shape[0]
+    nxa = raw_tile.shape[1] - APOD
+    out = torch.empty((B, nxa, 1024), dtype=torch.float32, device="cuda")
+    for _ in range(2):
+        ctx.magnitude(raw_tile, APOD, out, raw_dtype=0)
+    st = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(st)
+    for _ in range(reps):
+        ctx.magnitude(raw_tile, APOD, out, raw_dtype=0)
+    e1.record(st)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    bytes_per_launch = B * raw_tile.shape[1] * 2048 * 2 + B * nxa * 1024 * 4
+    return ms, bytes_per_launch, B * nxa
+
+
+def gpu_arm(args, rank, world):
+    import torch
+    from oct_recon_af_v1_gb300 import build
+    from oct_recon_af_v1_gb300._lib import Context
+    build()
+    dev = f"cuda:{int(os.environ.get('LOCAL_RANK', 0))}"
+    torch.cuda.set_device(dev)
+    ctx = Context(torch.cuda.current_device())
+    ctx.set_stream(torch.cuda.current_stream().cuda_stream)
+    if args.config == 0:
+        return gpu_arm_config0(args, rank, world, torch, ctx)
+    vol = Volume(ctx, torch, dev, host_copy=not args.no_e2e)
+    n_out = (2 * vol.ny, vol.nz, vol.nx)
+    db_vol = torch.empty(n_out, dtype=torch.float32, device=dev)
+    bits = torch.empty(n_out, dtype=torch.int16, device=dev)
+    ascans = 12 * vol.ny * vol.lay.n_x_px
+
+    def timed(src, steps, warm, e2e=False):
+        host_bits = torch.empty(n_out, dtype=torch.int16, pin_memory=True) if e2e else None
+        for _ in range(warm):
+            run_step(ctx, vol, src, db_vol, bits)
+            if e2e:
+                host_bits.copy_(bits, non_blocking=True)
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        n0 = ctx.launches
+        st = torch.cuda.current_stream()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(steps):
+            run_step(ctx, vol, src, db_vol, bits)
+            if e2e:
+                host_bits.copy_(bits, non_blocking=True)
+        e1.record(st)
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        ms = e0.elapsed_time(e1) / steps
+        return ms, ctx.launches - n0
+
+    clocks = Clocks(int(os.environ.get("LOCAL_RANK", 0)))
+    clocks.start()
+    ms, launches = timed(vol.raw, args.steps, args.warmup)
+    clk = clocks.stop()
+    e2e_ms = None
+    if not args.no_e2e:
+        e2e_ms, _ = timed(vol.host, max(1, args.steps // 2), 1, e2e=True)
+    # roofline of the dominant kernel, measured live on one tile
+    kms, kbytes, kascans = time_spectral_kernel(ctx, torch, vol.raw[(0, 0, 0)])
+    ms_all = reduce_max(ms, world)
+    hbm, src = peaks()
+    achieved = kbytes / (kms * 1e-3) / 1e9
+    value = ascans * world / (ms_all * 1e-3)
+    line = {
+        "metric": METRIC, "value": value, "unit": "A-scans/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_all, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (uint16 in, uint16 out)", "data": "synthetic (seeded, generated on device)",
+        "config": dict(config1_desc(), parallelism=f"replicas x{world} (independent volumes)"),
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": None, "kernel": "apod mean + k_spectral (magnitude mode), one tile per launch",
+                     "bytes_per_launch": kbytes, "ms_per_launch": kms, "a_scans_per_launch": kascans,
+                     "peak_source": src + " (burst copy)"},
+        "clocks": clk,
+    }
+    if e2e_ms is not None:
+        line["e2e"] = {"value": ascans / (e2e_ms * 1e-3), "unit": "A-scans/s", "ms_per_step": e2e_ms,
+                       "h2d_bytes_per_step": vol.raw_bytes(), "d2h_bytes_per_step": int(bits.numel()) * 2}
+    if rank == 0 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline_config1(vol, torch, budget_s=args.cpu_budget)
+    return line
+
+
+def gpu_arm_config0(args, rank, world, torch, ctx):
+    from oct_recon_af_v1_gb300 import geometry as G
+    from oct_recon_af_v1_gb300 import synthetic
+    sg = G.build_spectral_geometry(synthetic.lambda_nm(), synthetic.beta_ref_from_px(1e-5), 1.33)
+    ctx.set_geometry(sg.sinc_idx, sg.sinc_w, sg.window)
+    copies = [synthetic.u16_bits(synthetic.generate(50, 500, APOD, seed=k, device="cuda", chunk=50)) for k in range(8)]
+    db = torch.empty((50, 500, 1000), dtype=torch.float32, device="cuda")
+    bits = torch.empty((50, 500, 1000), dtype=torch.int16, device="cuda")
+
+    def step(i):
+        _, clim = ctx.db(copies[i % len(copies)], APOD, 0, 1000, db, raw_dtype=0)
+        ctx.quantise(db, clim, bits)
+
+    for i in range(args.warmup):
+        step(i)
+    torch.cuda.synchronize()
+    n0 = ctx.launches
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = Clocks()
+    clocks.start()
+    e0.record()
+    for i in range(args.steps):
+        step(i)
+    e1.record()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    hbm, src = peaks()
+    per = 2048 * 2 * (525 / 500) + 1000 * 4 + 1000 * 4 + 1000 * 2
+    return {"metric": METRIC, "value": 25000 / (ms * 1e-3), "unit": "A-scans/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (uint16 in, uint16 out)",
+            "data": "synthetic (seeded)", "config": config0_desc(), "gpu_launches": ctx.launches - n0,
+            "roofline": {"bound": "hbm", "achieved": 25000 * per / (ms * 1e-3) / 1e9, "peak": hbm, "unit": "GB/s",
+                         "frac": 25000 * per / (ms * 1e-3) / 1e9 / hbm, "traffic": None,
+                         "peak_source": src}, "clocks": clk}
+
+
+def reduce_max(x, world):
+    if world <= 1:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ------------------------------------------------------------------------ CPU (oracle) arm
+def _cpu_sample(raw_tiles, vol, frames, g, sts):
+    """Oracle reconstruction of `frames` of one y-row: returns the number of A-scans done."""
+    from oracle import numerics as O
+    nF = len(frames)
+    num = np.zeros((nF, vol.nz, vol.nx), np.float32)
+    den = np.zeros((nF, vol.nz, vol.nx), np.float32)
+    n = 0
+    for key, raw in raw_tiles.items():
+        s = sts[key]
+        mag = O.magnitude_numba(raw, g, APOD)
+        n_, d_ = s.contribute(mag)
+        num[:, :, s.c0:s.c1] += n_
+        den[:, :, s.c0:s.c1] += d_
+        n += raw.shape[0] * (raw.shape[1] - APOD)
+    db = O.finalise(num, den, np.float32)
+    fin = db[np.isfinite(db)]
+    O.db_to_bits(db, (float(fin.min()), float(fin.max())))
+    return n
+
+
+def _oracle_setup(vol):
+    from oracle import numerics as O
+    from oct_recon_af_v1_gb300 import synthetic
+    g = O.spectral_geometry(synthetic.lambda_nm(), synthetic.beta_ref_from_px(1e-5), 1.33)
+    sd = O.ScanDesc(vol.lay.x_centers_mm, vol.lay.y_centers_mm, vol.lay.z_depths_mm, vol.lay.n_x_px,
+                    vol.lay.n_y_px, vol.lay.tile_range_x_mm, vol.lay.tile_range_y_mm)
+    tg = O.tiled_geometry(sd, g.z_um, vol.focus, 1.0)
+    sts = {(xi, zi): O.Stitcher(tg, vol.lay.x_centers_mm[xi], vol.lay.z_depths_mm[zi], vol.focus[zi], 80.0)
+           for xi, zi in vol.order}
+    return g, sts
+
+
+def cpu_baseline_config1(vol, torch, budget_s=15.0, frames_max=64):
+    """Time the oracle (reference algorithm restated) on a bounded sample of the
+    workload: the first F frames of all 6 tiles of y-row 0, F grown until the
+    run takes ~budget_s."""
+    from oracle import numerics as O
+    O.build()
+    g, sts = _oracle_setup(vol)
+    F = 1
+    while True:
+        tiles = {(xi, zi): vol.raw[(0, xi, zi)][:F].cpu().numpy().view(np.uint16) for xi, zi in vol.order}
+        t0 = time.perf_counter()
+        n = _cpu_sample(tiles, vol, np.arange(F), g, {k: sts[k] for k in vol.order})
+        dt = time.perf_counter() - t0
+        if dt >= budget_s / 3 or F >= frames_max:
+            break
+        F = min(frames_max, max(F + 1, int(F * budget_s / 3 / max(dt, 1e-3))))
+    return {"value": n / dt, "unit": "A-scans/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": f"y-row 0, frames 0..{F - 1} of all 6 tiles ({n} A-scans): oracle Numba-kernel "
+                      f"restatement (C/OpenMP) + pocketfft + NumPy stitch/finalise/quantise, {dt:.1f} s"}
+
+
+def reference_arm(args, rank, world):
+    """The reference algorithm (CPU restatement) timed on the host cores."""
+    if rank != 0:
+        return None
+    import torch
+    from oracle import numerics as O
+    from oct_recon_af_v1_gb300 import geometry as G  # noqa: F401
+    from oct_recon_af_v1_gb300 import stitching as S
+    from oct_recon_af_v1_gb300 import synthetic
+    O.build()
+    lay, focus = config1_layout()
+
+    class V:  # host-only description of the config-1 volume
+        pass
+    vol = V()
+    vol.lay, vol.focus = lay, focus
+    vol.order = [(xi, zi) for xi in range(2) for zi in range(3)]
+    sg = G.build_spectral_geometry(synthetic.lambda_nm(), synthetic.beta_ref_from_px(1e-5), 1.33)
+    tg = S.tiled_geometry(lay, sg.z_um, focus, 1.0)
+    vol.nz, vol.nx = len(tg.out_z_mm), len(tg.out_x_mm)
+    g, sts = _oracle_setup(vol)
+    F = max(1, int(args.ref_frames))
+    tiles = {(xi, zi): synthetic.generate_numpy(F, lay.n_x_px, APOD, seed=1000 + 10 * xi + zi)
+             for xi, zi in vol.order}
+    for _ in range(args.warmup):
+        _cpu_sample(tiles, vol, np.arange(F), g, sts)
+    t0 = time.perf_counter()
+    n = 0
+    for _ in range(args.steps):
+        n += _cpu_sample(tiles, vol, np.arange(F), g, sts)
+    dt = time.perf_counter() - t0
+    v = n / dt
+    return {"impl": "reference", "metric": METRIC, "value": v, "unit": "A-scans/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64 (Numba types)",
+            "data": "synthetic (seeded)", "config": dict(config1_desc(), parallelism="host cores"),
+            "cpu_baseline": {"value": v, "unit": "A-scans/s", "cores": os.cpu_count(), "kind": "port",
+                             "sample": f"each step: frames 0..{F - 1} of the 6 tiles of y-row 0 "
+                                       f"({6 * F * lay.n_x_px} A-scans)"},
+            "e2e": {"value": v, "unit": "A-scans/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--config", type=int, default=1, choices=[0, 1])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--ref-frames", type=int, default=4)
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group("nccl" if args.impl == "gb300" else "gloo")
+    if args.impl == "reference":
+        line = reference_arm(args, rank, world)
+    else:
+        line = gpu_arm(args, rank, world)
+    if rank == 0 and line is not None:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,154 @@
+/*
+ * octgb — GB300-native (sm_103a) per-plane OCT reconstruction, C ABI.
+ *
+ * Drop-in boundary for the reference octrecon (atesfet/oct_recon_AF_v1) hot
+ * path.  Every entry point returns an int status (OCTGB_OK = 0); no exception
+ * crosses the ABI and nothing calls exit().  On failure the context keeps a
+ * message readable through octgb_last_error().  A context owns one CUDA stream
+ * (or uses the caller's, octgb_set_stream) and its device buffers; callers own
+ * every host buffer and every device buffer they pass in.  Pointer arguments
+ * come with a location flag: OCTGB_HOST (pageable or pinned host memory; the
+ * library copies through its own device buffers) or OCTGB_DEVICE (used in
+ * place, e.g. a torch CUDA tensor's data pointer).
+ *
+ * Threading: one context is driven by one host thread at a time (the reference
+ * drives its backend from the main thread or a web Job thread,
+ * octrecon/webapp/server.py:190-191); contexts are independent.  Not
+ * re-entrant on one context.
+ */
+#ifndef OCTGB_H
+#define OCTGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define OCTGB_OK 0
+#define OCTGB_ERR_ARG 1        /* invalid argument (shape, dtype, pointer, range) */
+#define OCTGB_ERR_CUDA 2       /* a CUDA runtime call failed */
+#define OCTGB_ERR_STATE 3      /* call out of order (e.g. no geometry set) */
+#define OCTGB_ERR_CANCELLED 4  /* octgb_cancel() was called; work was skipped */
+#define OCTGB_ERR_TIMEOUT 5    /* a bounded device-side wait expired */
+#define OCTGB_ERR_NOMEM 6      /* device or host allocation failed */
+
+/* raw spectrum element types (the reference's SUPPORTED_RAW_DTYPES,
+ * octrecon/core/gpu_kernels.py:39-41) */
+#define OCTGB_U16 0
+#define OCTGB_I16 1
+#define OCTGB_F32 2
+
+/* pointer locations */
+#define OCTGB_HOST 0
+#define OCTGB_DEVICE 1
+
+typedef struct octgb_ctx octgb_ctx;
+
+/* ---------------------------------------------------------------- context */
+
+/* Create a context on CUDA device `device` (replaces the device selection of
+ * octrecon/backend.py:61-83 get_xp for the "gb300" device). */
+int octgb_create(int device, octgb_ctx **out);
+int octgb_destroy(octgb_ctx *ctx);
+/* Last error message of this context ("" if none).  Valid until the next call
+ * on the context.  Accepts NULL (returns the message of the last failed
+ * octgb_create). */
+const char *octgb_last_error(const octgb_ctx *ctx);
+/* Launch on `cuda_stream` (a cudaStream_t) instead of the context's own stream;
+ * NULL restores the context stream. */
+int octgb_set_stream(octgb_ctx *ctx, void *cuda_stream);
+int octgb_synchronize(octgb_ctx *ctx);
+/* Cancellation (the reference's threading.Event, octrecon/pipeline.py:45-46,
+ * 262-263): every later batch call returns OCTGB_ERR_CANCELLED without work
+ * until octgb_reset_cancel().  Safe to call from another host thread. */
+int octgb_cancel(octgb_ctx *ctx);
+int octgb_reset_cancel(octgb_ctx *ctx);
+/* Number of kernels this context has launched (instrumentation). */
+int64_t octgb_launch_count(const octgb_ctx *ctx);
+
+/* ---------------------------------------------------------------- spectral */
+
+/* Upload the spectral geometry (SpectralProcessor.__init__,
+ * octrecon/core/spectral.py:91-110; built by geometry.py:84-128).
+ *   sinc_idx (n, taps) int64 row-major: source indices of output i, each row a
+ *            contiguous increasing run padded with index 0 / weight 0;
+ *   sinc_w   (n, taps) float64: weights (rounded to float32 on upload, as
+ *            `sg.sinc_w.astype(float32)` does);
+ *   window   (n, 2) float64 re/im: Hann/rms * exp(i*phase) (rounded to
+ *            complex64).
+ * n must be 2048 (the kernels' FFT length); taps <= 32. */
+int octgb_set_geometry(octgb_ctx *ctx, int n, int taps, const int64_t *sinc_idx, const double *sinc_w,
+                       const double *window);
+
+/* Fused pre-FFT stage only: apodisation mean, line mean, sinc
+ * k-linearisation, window — the operator of octrecon/core/gpu_kernels.py:54-68
+ * and core/cpu_kernels.py:12-41.  raw (B, interf, n) -> spec (B, interf-apod,
+ * n) complex64 as interleaved float pairs. */
+int octgb_fused_pre_fft(octgb_ctx *ctx, const void *raw, int raw_dtype, int raw_loc, int B, int interf,
+                        int apod_size, float *spec, int spec_loc);
+
+/* SpectralProcessor.magnitude (octrecon/core/spectral.py:136-153): raw (B,
+ * interf, n) -> |ifft(spec)|[..., :n/2] float32 (B, interf-apod, n/2). */
+int octgb_magnitude(octgb_ctx *ctx, const void *raw, int raw_dtype, int raw_loc, int B, int interf,
+                    int apod_size, float *mag, int mag_loc);
+
+/* Spectral stage to log-magnitude with a depth crop: db[a, z] =
+ * 20*log10(|X[z0 + z]|) for z < nz (float32, (B, interf-apod, nz)), the
+ * per-voxel value the reference writes after magnitude + crop + log.  When
+ * minmax is non-NULL it receives [min, max] of the finite values (host
+ * doubles), the plane clim of octrecon/io/tiff_writer.py:48-50. */
+int octgb_db(octgb_ctx *ctx, const void *raw, int raw_dtype, int raw_loc, int B, int interf, int apod_size,
+             int z0, int nz, float *db, int db_loc, double *minmax);
+
+/* ---------------------------------------------------------------- quantisation */
+
+/* Legacy quantisation db_to_bits (octrecon/io/tiff_writer.py:26-38):
+ * bits = min(round_half_away((db-c1)/(c2-c1)*65534) + 1, 65535) with the
+ * value clipped to [0, 65535] first, NaN -> 0; c1 < c2 (sorted by the caller
+ * or here).  Evaluated in float64 as write_legacy_tiff does (:62). */
+int octgb_quantise(octgb_ctx *ctx, const float *db, int64_t n, int db_loc, double c1, double c2,
+                   uint16_t *bits, int bits_loc);
+/* [min, max] of the finite values of db (plane_clim, tiff_writer.py:48-50);
+ * NaN pair when none is finite. */
+int octgb_minmax(octgb_ctx *ctx, const float *db, int64_t n, int db_loc, double *minmax);
+
+/* ---------------------------------------------------------------- stitching */
+
+/* One tile position (xi, zi) of the output grid: TileStitcher.__init__
+ * (octrecon/core/stitching.py:84-120).  Wz (n_out_z, r1-r0) and WxT
+ * (n_tile_x, c1-c0) are the reference's dense linear-interpolation operators
+ * restricted to the rows/columns that receive data; each row of Wz and each
+ * column of WxT has at most two adjacent non-zeros (MATLAB linear
+ * interpolation), which the library verifies and stores in compact form.
+ * fz (r1-r0): focus weight.  shift/pdz (n_y, n_tile_x): optical-path
+ * correction (OpticalPathCorrection, stitching.py:54-78), or NULL/NULL when it
+ * is off.  n_rows: depth samples per A-scan (n/2).  Returns a plan id. */
+int octgb_stitch_plan(octgb_ctx *ctx, int n_rows, int r0, int r1, int c0, int c1, int n_out_z, int n_tile_x,
+                      const double *Wz, const double *WxT, const double *fz, const int64_t *shift,
+                      const double *pdz, int n_y, int *plan_id);
+
+/* Start a y-tile row (Reconstructor.process_row, octrecon/pipeline.py:230-232):
+ * zero the device accumulators num/den of shape (n_frames, n_out_z, n_out_x). */
+int octgb_row_begin(octgb_ctx *ctx, int n_frames, int n_out_z, int n_out_x);
+
+/* One batch of one tile (pipeline.py:274-285): spectral stage of raw (B,
+ * interf, n) then TileStitcher.contribute (stitching.py:122-139) and
+ * num/den[frame_offset : frame_offset+B, :, c0:c1] += contribution.
+ * frame_idx (B, host int64): tile-local y frame of each B-scan (selects the
+ * optical-path shift row). */
+int octgb_row_add_batch(octgb_ctx *ctx, int plan_id, const void *raw, int raw_dtype, int raw_loc, int B,
+                        int interf, int apod_size, const int64_t *frame_idx, int frame_offset);
+
+/* Finalise the row (pipeline.py:296-300): den < threshold -> NaN, db =
+ * 20*log10(num/den) as float32 (n_frames, n_out_z, n_out_x) into db (host or
+ * device).  plane_minmax (optional, host, n_frames*2 doubles) receives each
+ * plane's clim (tiff_writer.py:48-50). */
+int octgb_row_finalise(octgb_ctx *ctx, float threshold, float *db, int db_loc, double *plane_minmax);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* OCTGB_H */

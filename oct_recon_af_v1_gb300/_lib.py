@@ -1,0 +1,252 @@
+"""ctypes binding of liboctgb.so (the C ABI declared in include/octgb.h).
+
+The library is loaded from the package's in-tree `_lib/` folder.  There is no
+fallback: if the shared library is missing or fails to load, `load()` raises.
+"""
+from __future__ import annotations
+
+import ctypes
+from ctypes import POINTER, c_double, c_float, c_int, c_int64, c_uint16, c_void_p
+from pathlib import Path
+
+import numpy as np
+
+from ._build import LIB
+
+OK, ERR_ARG, ERR_CUDA, ERR_STATE, ERR_CANCELLED, ERR_TIMEOUT, ERR_NOMEM = range(7)
+U16, I16, F32 = 0, 1, 2
+HOST, DEVICE = 0, 1
+
+_DTYPE = {np.dtype(np.uint16): U16, np.dtype(np.int16): I16, np.dtype(np.float32): F32}
+
+# name -> (restype, argtypes); every symbol include/octgb.h declares
+SIGNATURES = {
+    "octgb_create": (c_int, [c_int, POINTER(c_void_p)]),
+    "octgb_destroy": (c_int, [c_void_p]),
+    "octgb_last_error": (ctypes.c_char_p, [c_void_p]),
+    "octgb_set_stream": (c_int, [c_void_p, c_void_p]),
+    "octgb_synchronize": (c_int, [c_void_p]),
+    "octgb_cancel": (c_int, [c_void_p]),
+    "octgb_reset_cancel": (c_int, [c_void_p]),
+    "octgb_launch_count": (c_int64, [c_void_p]),
+    "octgb_set_geometry": (c_int, [c_void_p, c_int, c_int, c_void_p, c_void_p, c_void_p]),
+    "octgb_fused_pre_fft": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_int, c_void_p, c_int]),
+    "octgb_magnitude": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_int, c_void_p, c_int]),
+    "octgb_db": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_int, c_int, c_int, c_void_p, c_int,
+                         c_void_p]),
+    "octgb_quantise": (c_int, [c_void_p, c_void_p, c_int64, c_int, c_double, c_double, c_void_p, c_int]),
+    "octgb_minmax": (c_int, [c_void_p, c_void_p, c_int64, c_int, c_void_p]),
+    "octgb_stitch_plan": (c_int, [c_void_p, c_int, c_int, c_int, c_int, c_int, c_int, c_int, c_void_p, c_void_p,
+                                  c_void_p, c_void_p, c_void_p, c_int, POINTER(c_int)]),
+    "octgb_row_begin": (c_int, [c_void_p, c_int, c_int, c_int]),
+    "octgb_row_add_batch": (c_int, [c_void_p, c_int, c_void_p, c_int, c_int, c_int, c_int, c_int, c_void_p, c_int]),
+    "octgb_row_finalise": (c_int, [c_void_p, c_float, c_void_p, c_int, c_void_p]),
+}
+
+_lib = None
+
+
+class OctgbError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"octgb error {code}: {msg}")
+        self.code = code
+
+
+class Cancelled(OctgbError):
+    pass
+
+
+def load(path: Path | None = None):
+    """Load (once) and return the ctypes library handle; raises if it is absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = Path(path) if path else LIB
+    if not p.exists():
+        raise RuntimeError(f"{p} is missing: build it with oct_recon_af_v1_gb300.build() "
+                           "(the GB300 path has no CPU fallback)")
+    lib = ctypes.CDLL(str(p))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def exported_symbols(path: Path | None = None):
+    """Names of SIGNATURES present in the library (symbol lookup only, no calls)."""
+    lib = ctypes.CDLL(str(Path(path) if path else LIB))
+    return [n for n in SIGNATURES if hasattr(lib, n)]
+
+
+def _ptr(a):
+    """(pointer, location) of a numpy array or a CUDA tensor-like object."""
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data, HOST
+    if hasattr(a, "data_ptr") and getattr(a, "is_cuda", False):
+        return a.data_ptr(), DEVICE
+    if hasattr(a, "data_ptr"):  # torch CPU tensor
+        return a.data_ptr(), HOST
+    raise TypeError(f"unsupported array type {type(a)!r}")
+
+
+def _raw_dtype(a) -> int:
+    if isinstance(a, np.ndarray):
+        dt = a.dtype
+    else:
+        import torch
+        dt = {torch.int16: np.dtype(np.int16), torch.float32: np.dtype(np.float32)}.get(a.dtype)
+        if dt is None and str(a.dtype) == "torch.uint16":
+            dt = np.dtype(np.uint16)
+    if dt not in _DTYPE:
+        raise TypeError(f"raw spectra must be uint16, int16 or float32, got {dt}")
+    return _DTYPE[dt]
+
+
+class Context:
+    """One octgb context (device, stream, geometry, work buffers)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load()
+        h = c_void_p()
+        rc = self.lib.octgb_create(int(device), ctypes.byref(h))
+        if rc != OK:
+            raise OctgbError(rc, self.lib.octgb_last_error(None).decode())
+        self.h = h
+        self.device = int(device)
+        self.n = None
+        self.taps = None
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.octgb_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc: int):
+        if rc != OK:
+            msg = self.lib.octgb_last_error(self.h).decode()
+            raise (Cancelled if rc == ERR_CANCELLED else OctgbError)(rc, msg)
+
+    # -------------------------------------------------------------- control
+    def set_stream(self, stream_handle: int | None):
+        self._check(self.lib.octgb_set_stream(self.h, c_void_p(stream_handle or None)))
+
+    def synchronize(self):
+        self._check(self.lib.octgb_synchronize(self.h))
+
+    def cancel(self):
+        self._check(self.lib.octgb_cancel(self.h))
+
+    def reset_cancel(self):
+        self._check(self.lib.octgb_reset_cancel(self.h))
+
+    @property
+    def launches(self) -> int:
+        return int(self.lib.octgb_launch_count(self.h))
+
+    # -------------------------------------------------------------- spectral
+    def set_geometry(self, sinc_idx: np.ndarray, sinc_w: np.ndarray, window: np.ndarray):
+        idx = np.ascontiguousarray(sinc_idx, dtype=np.int64)
+        w = np.ascontiguousarray(sinc_w, dtype=np.float64)
+        win = np.ascontiguousarray(np.stack([np.real(window), np.imag(window)], -1), dtype=np.float64)
+        n, taps = idx.shape
+        self._check(self.lib.octgb_set_geometry(self.h, n, taps, idx.ctypes.data, w.ctypes.data, win.ctypes.data))
+        self.n, self.taps = n, taps
+
+    def _raw_args(self, raw, apod_size, raw_dtype=None):
+        if raw.ndim != 3:
+            raise ValueError("raw must be (B, interf, N)")
+        if isinstance(raw, np.ndarray):
+            raw = np.ascontiguousarray(raw)
+        elif not raw.is_contiguous():
+            raw = raw.contiguous()
+        B, interf, N = raw.shape
+        if N != self.n:
+            raise ValueError(f"raw has {N} spectral samples, geometry has {self.n}")
+        p, loc = _ptr(raw)
+        return raw, p, loc, (_raw_dtype(raw) if raw_dtype is None else int(raw_dtype)), B, interf
+
+    def fused_pre_fft(self, raw, apod_size: int, out=None, raw_dtype=None):
+        raw, p, loc, dt, B, interf = self._raw_args(raw, apod_size, raw_dtype)
+        if out is None:
+            out = np.empty((B, interf - apod_size, self.n), np.complex64)
+        op, oloc = _ptr(out)
+        self._check(self.lib.octgb_fused_pre_fft(self.h, p, dt, loc, B, interf, apod_size, op, oloc))
+        return out
+
+    def magnitude(self, raw, apod_size: int, out=None, raw_dtype=None):
+        raw, p, loc, dt, B, interf = self._raw_args(raw, apod_size, raw_dtype)
+        if out is None:
+            out = np.empty((B, interf - apod_size, self.n // 2), np.float32)
+        op, oloc = _ptr(out)
+        self._check(self.lib.octgb_magnitude(self.h, p, dt, loc, B, interf, apod_size, op, oloc))
+        return out
+
+    def db(self, raw, apod_size: int, z0: int, nz: int, out=None, minmax: bool = True, raw_dtype=None):
+        raw, p, loc, dt, B, interf = self._raw_args(raw, apod_size, raw_dtype)
+        if out is None:
+            out = np.empty((B, interf - apod_size, nz), np.float32)
+        op, oloc = _ptr(out)
+        mm = np.full(2, np.nan)
+        self._check(self.lib.octgb_db(self.h, p, dt, loc, B, interf, apod_size, int(z0), int(nz), op, oloc,
+                                      mm.ctypes.data if minmax else None))
+        return out, (float(mm[0]), float(mm[1]))
+
+    # -------------------------------------------------------------- quantisation
+    def quantise(self, db, clim, out=None):
+        p, loc = _ptr(db)
+        n = int(np.prod(db.shape))
+        if out is None:
+            out = np.empty(db.shape, np.uint16)
+        op, oloc = _ptr(out)
+        c1, c2 = sorted(float(c) for c in clim)
+        self._check(self.lib.octgb_quantise(self.h, p, n, loc, c1, c2, op, oloc))
+        return out
+
+    def minmax(self, db):
+        p, loc = _ptr(db)
+        mm = np.full(2, np.nan)
+        self._check(self.lib.octgb_minmax(self.h, p, int(np.prod(db.shape)), loc, mm.ctypes.data))
+        return float(mm[0]), float(mm[1])
+
+    # -------------------------------------------------------------- stitching
+    def stitch_plan(self, n_rows, r0, r1, c0, c1, Wz, WxT, fz, shift=None, pdz=None) -> int:
+        Wz = np.ascontiguousarray(Wz, dtype=np.float64)
+        WxT = np.ascontiguousarray(WxT, dtype=np.float64)
+        fz = np.ascontiguousarray(fz, dtype=np.float64)
+        sh = None if shift is None else np.ascontiguousarray(shift, dtype=np.int64)
+        pz = None if pdz is None else np.ascontiguousarray(pdz, dtype=np.float64)
+        n_y = 0 if sh is None else sh.shape[0]
+        pid = c_int(-1)
+        self._check(self.lib.octgb_stitch_plan(
+            self.h, int(n_rows), int(r0), int(r1), int(c0), int(c1), Wz.shape[0], WxT.shape[0],
+            Wz.ctypes.data, WxT.ctypes.data, fz.ctypes.data,
+            None if sh is None else sh.ctypes.data, None if pz is None else pz.ctypes.data, n_y, ctypes.byref(pid)))
+        return pid.value
+
+    def row_begin(self, n_frames: int, n_out_z: int, n_out_x: int):
+        self._check(self.lib.octgb_row_begin(self.h, int(n_frames), int(n_out_z), int(n_out_x)))
+
+    def row_add_batch(self, plan_id: int, raw, apod_size: int, frame_idx, frame_offset: int, raw_dtype=None):
+        raw, p, loc, dt, B, interf = self._raw_args(raw, apod_size, raw_dtype)
+        fi = np.ascontiguousarray(np.asarray(frame_idx).reshape(-1), dtype=np.int64)
+        if len(fi) != B:
+            raise ValueError("frame_idx must have one entry per B-scan")
+        self._check(self.lib.octgb_row_add_batch(self.h, int(plan_id), p, dt, loc, B, interf, int(apod_size),
+                                                 fi.ctypes.data, int(frame_offset)))
+
+    def row_finalise(self, threshold: float, shape, out=None, plane_minmax: bool = False):
+        if out is None:
+            out = np.empty(shape, np.float32)
+        op, oloc = _ptr(out)
+        mm = np.full((shape[0], 2), np.nan) if plane_minmax else None
+        self._check(self.lib.octgb_row_finalise(self.h, c_float(threshold), op, oloc,
+                                                None if mm is None else mm.ctypes.data))
+        return (out, mm) if plane_minmax else out

@@ -1,0 +1,651 @@
+// C ABI of the octgb library (declared in include/octgb.h).
+//
+// The context owns one CUDA stream (or borrows the caller's), the uploaded
+// geometry, grow-only device work buffers and the row accumulators.  Every
+// entry point catches all C++ exceptions and reports failures as status codes
+// plus a message; none of them exits the process.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <atomic>
+#include <cstdio>
+#include <exception>
+#include <string>
+#include <vector>
+
+#include "../../include/octgb.h"
+#include "octgb_internal.h"
+
+using namespace octgb;
+
+namespace {
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t cap = 0;
+    cudaError_t ensure(size_t bytes) {
+        if (bytes <= cap) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        cudaError_t e = cudaMalloc(&p, bytes);
+        if (e == cudaSuccess) cap = bytes;
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+    template <typename T>
+    T* as() const {
+        return static_cast<T*>(p);
+    }
+};
+
+struct Plan {
+    int n_rows, r0, R, c0, C, n_out_z, n_tile_x, n_y;
+    DevBuf zr, wz0, wz1, xr, wx0, wx1, fz, shift, lo, hi;
+    bool opc = false;
+    StitchDev dev() const {
+        StitchDev d;
+        d.zr = zr.as<int>();
+        d.wz0 = wz0.as<float>();
+        d.wz1 = wz1.as<float>();
+        d.xr = xr.as<int>();
+        d.wx0 = wx0.as<float>();
+        d.wx1 = wx1.as<float>();
+        d.fz = fz.as<float>();
+        d.shift = opc ? shift.as<int>() : nullptr;
+        d.lo = opc ? lo.as<int>() : nullptr;
+        d.hi = opc ? hi.as<int>() : nullptr;
+        d.r0 = r0;
+        d.R = R;
+        d.c0 = c0;
+        d.C = C;
+        d.n_out_z = n_out_z;
+        d.n_tile_x = n_tile_x;
+        d.n_rows = n_rows;
+        return d;
+    }
+    void release() {
+        for (DevBuf* b : {&zr, &wz0, &wz1, &xr, &wx0, &wx1, &fz, &shift, &lo, &hi}) b->release();
+    }
+};
+
+struct Error : std::exception {
+    int code;
+    std::string msg;
+    Error(int c, std::string m) : code(c), msg(std::move(m)) {}
+};
+
+std::string g_create_error;
+
+}  // namespace
+
+struct octgb_ctx {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t own = nullptr;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    std::atomic<int> cancel{0};
+    std::atomic<int64_t> launches{0};
+    // geometry
+    bool has_geom = false;
+    int taps = 0;
+    DevBuf w, start, win, tw;
+    // work buffers
+    DevBuf raw, apod, out, mm, frames;
+    int* status_host = nullptr;  // mapped pinned status word
+    int* status_dev = nullptr;
+    // plans and row state
+    std::vector<Plan*> plans;
+    DevBuf num, den;
+    int row_nf = 0, row_nz = 0, row_nx = 0;
+    bool row_open = false;
+};
+
+namespace {
+
+void ck(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) throw Error(OCTGB_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+void require(bool ok, const char* msg) {
+    if (!ok) throw Error(OCTGB_ERR_ARG, msg);
+}
+
+template <typename F>
+int guarded(octgb_ctx* ctx, F&& f) {
+    if (ctx == nullptr) return OCTGB_ERR_ARG;
+    try {
+        ck(cudaSetDevice(ctx->device), "cudaSetDevice");
+        f();
+        ctx->err.clear();
+        return OCTGB_OK;
+    } catch (const Error& e) {
+        ctx->err = e.msg;
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        ctx->err = "host allocation failed";
+        return OCTGB_ERR_NOMEM;
+    } catch (const std::exception& e) {
+        ctx->err = e.what();
+        return OCTGB_ERR_STATE;
+    } catch (...) {
+        ctx->err = "unknown error";
+        return OCTGB_ERR_STATE;
+    }
+}
+
+size_t raw_elem(int dtype) { return dtype == OCTGB_F32 ? 4 : 2; }
+
+// Make the raw batch available on the device; returns the device pointer.
+const void* stage_raw(octgb_ctx* c, const void* raw, int dtype, int loc, size_t bytes) {
+    if (loc == OCTGB_DEVICE) return raw;
+    ck(c->raw.ensure(bytes), "cudaMalloc(raw)");
+    ck(cudaMemcpyAsync(c->raw.p, raw, bytes, cudaMemcpyHostToDevice, c->stream), "H2D raw");
+    return c->raw.p;
+}
+
+void check_status(octgb_ctx* c) {
+    ck(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+    const int s = *reinterpret_cast<volatile int*>(c->status_host);
+    if (s != kStatusOk) {
+        *reinterpret_cast<volatile int*>(c->status_host) = kStatusOk;
+        throw Error(OCTGB_ERR_TIMEOUT, "a bounded device-side wait expired (bulk copy did not complete)");
+    }
+}
+
+void validate_raw(const void* raw, int dtype, int loc, int B, int interf, int apod) {
+    require(raw != nullptr, "raw is NULL");
+    require(dtype == OCTGB_U16 || dtype == OCTGB_I16 || dtype == OCTGB_F32, "raw_dtype must be U16, I16 or F32");
+    require(loc == OCTGB_HOST || loc == OCTGB_DEVICE, "bad location flag");
+    require(B >= 0, "B < 0");
+    require(apod >= 1 && apod < 32768, "apod_size must be in [1, 32767]");
+    require(interf > apod, "interf must exceed apod_size");
+    if (loc == OCTGB_DEVICE) require((reinterpret_cast<uintptr_t>(raw) & 15u) == 0, "device raw must be 16-byte aligned");
+}
+
+// Run the spectral stage of a batch into `out` (device) in the given mode.
+void run_spectral(octgb_ctx* c, const void* raw, int dtype, int loc, int B, int interf, int apod, int mode,
+                  float* out_dev, int z0, int nz, unsigned int* mm_dev) {
+    if (!c->has_geom) throw Error(OCTGB_ERR_STATE, "octgb_set_geometry has not been called");
+    if (c->cancel.load()) throw Error(OCTGB_ERR_CANCELLED, "cancelled");
+    const size_t bytes = static_cast<size_t>(B) * interf * kN * raw_elem(dtype);
+    const void* rd = stage_raw(c, raw, dtype, loc, bytes);
+    ck(c->apod.ensure(static_cast<size_t>(B) * kN * sizeof(float) + 16), "cudaMalloc(apod)");
+    ck(launch_apod_mean(rd, dtype, B, interf, apod, c->apod.as<float>(), c->stream), "apod kernel");
+    c->launches++;
+    SpectralArgs a{};
+    a.raw = rd;
+    a.B = B;
+    a.interf = interf;
+    a.apod = apod;
+    a.nx = interf - apod;
+    a.n_ascans = static_cast<int64_t>(B) * (interf - apod);
+    a.apod_mean = c->apod.as<float>();
+    a.g.w = c->w.as<float>();
+    a.g.start = c->start.as<int>();
+    a.g.taps = c->taps;
+    a.g.win = c->win.as<float2>();
+    a.g.tw = c->tw.as<float2>();
+    a.out = out_dev;
+    a.z0 = z0;
+    a.nz = nz;
+    a.minmax = mm_dev;
+    a.status = c->status_dev;
+    const int64_t pairs = (a.n_ascans + kPerCta - 1) / kPerCta;
+    int64_t grid = static_cast<int64_t>(c->num_sms) * spectral_max_ctas_per_sm(dtype, mode);
+    if (grid > pairs) grid = pairs;
+    if (grid < 1) return;
+    ck(launch_spectral(a, dtype, mode, static_cast<int>(grid), c->stream), "spectral kernel");
+    c->launches++;
+}
+
+void copy_out(octgb_ctx* c, void* dst, int loc, const void* src_dev, size_t bytes) {
+    if (bytes == 0) return;
+    ck(cudaMemcpyAsync(dst, src_dev, bytes, loc == OCTGB_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                       c->stream),
+       "copy out");
+}
+
+void read_minmax(octgb_ctx* c, const unsigned int* mm_dev, double* out2) {
+    unsigned int h[2];
+    ck(cudaMemcpyAsync(h, mm_dev, sizeof(h), cudaMemcpyDeviceToHost, c->stream), "D2H minmax");
+    check_status(c);
+    if (h[0] == 0xffffffffu) {
+        out2[0] = out2[1] = NAN;
+    } else {
+        out2[0] = ord2f(h[0]);
+        out2[1] = ord2f(h[1]);
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int octgb_create(int device, octgb_ctx** out) {
+    if (out == nullptr) return OCTGB_ERR_ARG;
+    *out = nullptr;
+    octgb_ctx* c = nullptr;
+    try {
+        c = new octgb_ctx();
+        c->device = device;
+        ck(cudaSetDevice(device), "cudaSetDevice");
+        cudaDeviceProp prop;
+        ck(cudaGetDeviceProperties(&prop, device), "cudaGetDeviceProperties");
+        if (prop.major * 10 + prop.minor < 100)
+            throw Error(OCTGB_ERR_STATE, std::string("device ") + prop.name + " is not sm_100 or newer");
+        c->num_sms = prop.multiProcessorCount;
+        ck(cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking), "cudaStreamCreate");
+        c->stream = c->own;
+        ck(cudaHostAlloc(reinterpret_cast<void**>(&c->status_host), sizeof(int), cudaHostAllocMapped),
+           "cudaHostAlloc(status)");
+        *c->status_host = kStatusOk;
+        ck(cudaHostGetDevicePointer(reinterpret_cast<void**>(&c->status_dev), c->status_host, 0),
+           "cudaHostGetDevicePointer");
+        ck(c->mm.ensure(4096), "cudaMalloc(minmax)");
+        *out = c;
+        g_create_error.clear();
+        return OCTGB_OK;
+    } catch (const Error& e) {
+        g_create_error = e.msg;
+        if (c) octgb_destroy(c);
+        return e.code;
+    } catch (...) {
+        g_create_error = "octgb_create failed";
+        if (c) octgb_destroy(c);
+        return OCTGB_ERR_STATE;
+    }
+}
+
+int octgb_destroy(octgb_ctx* c) {
+    if (c == nullptr) return OCTGB_OK;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (Plan* p : c->plans) {
+        if (p) {
+            p->release();
+            delete p;
+        }
+    }
+    for (DevBuf* b : {&c->w, &c->start, &c->win, &c->tw, &c->raw, &c->apod, &c->out, &c->mm, &c->frames, &c->num,
+                      &c->den})
+        b->release();
+    if (c->status_host) cudaFreeHost(c->status_host);
+    if (c->own) cudaStreamDestroy(c->own);
+    delete c;
+    return OCTGB_OK;
+}
+
+const char* octgb_last_error(const octgb_ctx* c) { return c ? c->err.c_str() : g_create_error.c_str(); }
+
+int octgb_set_stream(octgb_ctx* c, void* s) {
+    return guarded(c, [&] { c->stream = s ? static_cast<cudaStream_t>(s) : c->own; });
+}
+
+int octgb_synchronize(octgb_ctx* c) {
+    return guarded(c, [&] { check_status(c); });
+}
+
+int octgb_cancel(octgb_ctx* c) {
+    if (!c) return OCTGB_ERR_ARG;
+    c->cancel.store(1);
+    return OCTGB_OK;
+}
+
+int octgb_reset_cancel(octgb_ctx* c) {
+    if (!c) return OCTGB_ERR_ARG;
+    c->cancel.store(0);
+    return OCTGB_OK;
+}
+
+int64_t octgb_launch_count(const octgb_ctx* c) { return c ? c->launches.load() : 0; }
+
+int octgb_set_geometry(octgb_ctx* c, int n, int taps, const int64_t* idx, const double* w, const double* window) {
+    return guarded(c, [&] {
+        require(n == kN, "n must be 2048");
+        require(taps >= 1 && taps <= kMaxTaps, "taps must be in [1, 32]");
+        require(idx && w && window, "NULL geometry array");
+        std::vector<float> wt(static_cast<size_t>(taps) * kN);
+        std::vector<int> st(kN);
+        for (int i = 0; i < kN; ++i) {
+            int s = -1, len = 0;
+            for (int t = 0; t < taps; ++t) {
+                const double wv = w[static_cast<size_t>(i) * taps + t];
+                const int64_t j = idx[static_cast<size_t>(i) * taps + t];
+                require(j >= 0 && j < kN, "sinc index out of range");
+                if (t == 0) s = static_cast<int>(j);
+                const bool pad_entry = (wv == 0.0 && j == 0 && t > 0);
+                if (!pad_entry) {
+                    require(j == s + t, "sinc taps of a row must be contiguous increasing indices");
+                    len = t + 1;
+                }
+                wt[static_cast<size_t>(t) * kN + i] = static_cast<float>(wv);
+            }
+            (void)len;
+            st[i] = s;
+        }
+        std::vector<float2> win(kN), tw(kN);
+        for (int i = 0; i < kN; ++i) {
+            // complex64 window (core/spectral.py:219) times 1/N: exact power-of-two scaling
+            win[i] = make_float2(static_cast<float>(window[2 * i]) * (1.0f / kN),
+                                 static_cast<float>(window[2 * i + 1]) * (1.0f / kN));
+            const double ang = 2.0 * 3.14159265358979323846 * i / kN;
+            tw[i] = make_float2(static_cast<float>(cos(ang)), static_cast<float>(sin(ang)));
+        }
+        ck(c->w.ensure(wt.size() * sizeof(float)), "cudaMalloc(w)");
+        ck(c->start.ensure(kN * sizeof(int)), "cudaMalloc(start)");
+        ck(c->win.ensure(kN * sizeof(float2)), "cudaMalloc(win)");
+        ck(c->tw.ensure(kN * sizeof(float2)), "cudaMalloc(tw)");
+        ck(cudaMemcpyAsync(c->w.p, wt.data(), wt.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream), "H2D w");
+        ck(cudaMemcpyAsync(c->start.p, st.data(), kN * sizeof(int), cudaMemcpyHostToDevice, c->stream), "H2D start");
+        ck(cudaMemcpyAsync(c->win.p, win.data(), kN * sizeof(float2), cudaMemcpyHostToDevice, c->stream), "H2D win");
+        ck(cudaMemcpyAsync(c->tw.p, tw.data(), kN * sizeof(float2), cudaMemcpyHostToDevice, c->stream), "H2D tw");
+        ck(cudaStreamSynchronize(c->stream), "sync geometry");
+        c->taps = taps;
+        c->has_geom = true;
+    });
+}
+
+int octgb_fused_pre_fft(octgb_ctx* c, const void* raw, int dtype, int loc, int B, int interf, int apod, float* spec,
+                        int spec_loc) {
+    return guarded(c, [&] {
+        validate_raw(raw, dtype, loc, B, interf, apod);
+        require(spec != nullptr, "spec is NULL");
+        const size_t ob = static_cast<size_t>(B) * (interf - apod) * kN * 2 * sizeof(float);
+        float* dst = spec;
+        if (spec_loc != OCTGB_DEVICE) {
+            ck(c->out.ensure(ob), "cudaMalloc(out)");
+            dst = c->out.as<float>();
+        }
+        run_spectral(c, raw, dtype, loc, B, interf, apod, kModeSpec, dst, 0, 0, nullptr);
+        if (spec_loc != OCTGB_DEVICE) copy_out(c, spec, OCTGB_HOST, dst, ob);
+        check_status(c);
+    });
+}
+
+int octgb_magnitude(octgb_ctx* c, const void* raw, int dtype, int loc, int B, int interf, int apod, float* mag,
+                    int mag_loc) {
+    return guarded(c, [&] {
+        validate_raw(raw, dtype, loc, B, interf, apod);
+        require(mag != nullptr, "mag is NULL");
+        const size_t ob = static_cast<size_t>(B) * (interf - apod) * kHalf * sizeof(float);
+        float* dst = mag;
+        if (mag_loc != OCTGB_DEVICE) {
+            ck(c->out.ensure(ob), "cudaMalloc(out)");
+            dst = c->out.as<float>();
+        }
+        run_spectral(c, raw, dtype, loc, B, interf, apod, kModeMag, dst, 0, 0, nullptr);
+        if (mag_loc != OCTGB_DEVICE) copy_out(c, mag, OCTGB_HOST, dst, ob);
+        if (mag_loc != OCTGB_DEVICE || loc != OCTGB_DEVICE) check_status(c);
+    });
+}
+
+int octgb_db(octgb_ctx* c, const void* raw, int dtype, int loc, int B, int interf, int apod, int z0, int nz,
+             float* db, int db_loc, double* minmax) {
+    return guarded(c, [&] {
+        validate_raw(raw, dtype, loc, B, interf, apod);
+        require(db != nullptr, "db is NULL");
+        require(z0 >= 0 && nz >= 1 && z0 + nz <= kHalf, "depth crop must lie within [0, N/2)");
+        const size_t ob = static_cast<size_t>(B) * (interf - apod) * nz * sizeof(float);
+        float* dst = db;
+        if (db_loc != OCTGB_DEVICE) {
+            ck(c->out.ensure(ob), "cudaMalloc(out)");
+            dst = c->out.as<float>();
+        }
+        unsigned int* mm = c->mm.as<unsigned int>();
+        if (minmax) {
+            ck(launch_minmax_init(mm, 2, c->stream), "minmax init");
+            c->launches++;
+        }
+        run_spectral(c, raw, dtype, loc, B, interf, apod, kModeDb, dst, z0, nz, minmax ? mm : nullptr);
+        if (db_loc != OCTGB_DEVICE) copy_out(c, db, OCTGB_HOST, dst, ob);
+        if (minmax)
+            read_minmax(c, mm, minmax);
+        else if (db_loc != OCTGB_DEVICE || loc != OCTGB_DEVICE)
+            check_status(c);
+    });
+}
+
+int octgb_quantise(octgb_ctx* c, const float* db, int64_t n, int db_loc, double c1, double c2, uint16_t* bits,
+                   int bits_loc) {
+    return guarded(c, [&] {
+        require(n >= 0, "n < 0");
+        require(db && bits, "NULL array");
+        if (c1 > c2) {
+            const double t = c1;
+            c1 = c2;
+            c2 = t;
+        }
+        require(c2 > c1, "clim must span a non-empty range");
+        const float* src = db;
+        if (db_loc != OCTGB_DEVICE) {
+            ck(c->raw.ensure(static_cast<size_t>(n) * sizeof(float)), "cudaMalloc(db in)");
+            ck(cudaMemcpyAsync(c->raw.p, db, static_cast<size_t>(n) * sizeof(float), cudaMemcpyHostToDevice,
+                               c->stream),
+               "H2D db");
+            src = c->raw.as<float>();
+        }
+        uint16_t* dst = bits;
+        if (bits_loc != OCTGB_DEVICE) {
+            ck(c->out.ensure(static_cast<size_t>(n) * sizeof(uint16_t)), "cudaMalloc(bits)");
+            dst = c->out.as<uint16_t>();
+        }
+        ck(launch_quantise(src, n, c1, c2, dst, c->stream), "quantise kernel");
+        c->launches++;
+        if (bits_loc != OCTGB_DEVICE) {
+            copy_out(c, bits, OCTGB_HOST, dst, static_cast<size_t>(n) * sizeof(uint16_t));
+            check_status(c);
+        }
+    });
+}
+
+int octgb_minmax(octgb_ctx* c, const float* db, int64_t n, int db_loc, double* minmax) {
+    return guarded(c, [&] {
+        require(n >= 0 && db && minmax, "bad argument");
+        const float* src = db;
+        if (db_loc != OCTGB_DEVICE) {
+            ck(c->raw.ensure(static_cast<size_t>(n) * sizeof(float) + 16), "cudaMalloc(db in)");
+            ck(cudaMemcpyAsync(c->raw.p, db, static_cast<size_t>(n) * sizeof(float), cudaMemcpyHostToDevice,
+                               c->stream),
+               "H2D db");
+            src = c->raw.as<float>();
+        }
+        unsigned int* mm = c->mm.as<unsigned int>();
+        ck(launch_minmax_init(mm, 2, c->stream), "minmax init");
+        ck(launch_minmax(src, n, mm, c->stream), "minmax kernel");
+        c->launches += 2;
+        read_minmax(c, mm, minmax);
+    });
+}
+
+int octgb_stitch_plan(octgb_ctx* c, int n_rows, int r0, int r1, int c0, int c1, int n_out_z, int n_tile_x,
+                      const double* Wz, const double* WxT, const double* fz, const int64_t* shift, const double* pdz,
+                      int n_y, int* plan_id) {
+    return guarded(c, [&] {
+        require(plan_id != nullptr, "plan_id is NULL");
+        require(n_rows == kHalf, "n_rows must be N/2 = 1024");
+        require(r0 >= 0 && r1 > r0 && r1 <= n_rows, "bad row window");
+        require(c0 >= 0 && c1 > c0, "bad column window");
+        require(n_out_z >= 1 && n_tile_x >= 2, "bad output / tile size");
+        require(Wz && WxT && fz, "NULL operator");
+        require((shift == nullptr) == (pdz == nullptr), "shift and pdz go together");
+        const int R = r1 - r0, C = c1 - c0;
+        // compact the depth operator: <= 2 adjacent non-zeros per output row
+        std::vector<int> zr(n_out_z, -1), xr(C, -1);
+        std::vector<float> wz0(n_out_z, 0.f), wz1(n_out_z, 0.f), wx0(C, 0.f), wx1(C, 0.f), fzf(R);
+        for (int zo = 0; zo < n_out_z; ++zo) {
+            int first = -1, last = -1;
+            for (int r = 0; r < R; ++r) {
+                if (Wz[static_cast<size_t>(zo) * R + r] != 0.0) {
+                    if (first < 0) first = r;
+                    last = r;
+                }
+            }
+            if (first < 0) continue;
+            require(last - first <= 1, "Wz row has more than two adjacent non-zeros");
+            if (first == R - 1) first = R - 2 >= 0 ? R - 2 : 0;  // keep zr+1 inside the window
+            zr[zo] = first;
+            wz0[zo] = static_cast<float>(Wz[static_cast<size_t>(zo) * R + first]);
+            wz1[zo] = first + 1 < R ? static_cast<float>(Wz[static_cast<size_t>(zo) * R + first + 1]) : 0.f;
+        }
+        for (int cc = 0; cc < C; ++cc) {
+            int first = -1, last = -1;
+            for (int x = 0; x < n_tile_x; ++x) {
+                if (WxT[static_cast<size_t>(x) * C + cc] != 0.0) {
+                    if (first < 0) first = x;
+                    last = x;
+                }
+            }
+            if (first < 0) continue;
+            require(last - first <= 1, "WxT column has more than two adjacent non-zeros");
+            if (first == n_tile_x - 1) first = n_tile_x - 2;
+            xr[cc] = first;
+            wx0[cc] = static_cast<float>(WxT[static_cast<size_t>(first) * C + cc]);
+            wx1[cc] = static_cast<float>(WxT[static_cast<size_t>(first + 1) * C + cc]);
+        }
+        for (int r = 0; r < R; ++r) fzf[r] = static_cast<float>(fz[r]);
+        Plan* p = new Plan();
+        p->n_rows = n_rows;
+        p->r0 = r0;
+        p->R = R;
+        p->c0 = c0;
+        p->C = C;
+        p->n_out_z = n_out_z;
+        p->n_tile_x = n_tile_x;
+        p->n_y = n_y;
+        auto up = [&](DevBuf& b, const void* src, size_t bytes) {
+            ck(b.ensure(bytes > 0 ? bytes : 4), "cudaMalloc(plan)");
+            if (bytes) ck(cudaMemcpyAsync(b.p, src, bytes, cudaMemcpyHostToDevice, c->stream), "H2D plan");
+        };
+        try {
+            up(p->zr, zr.data(), zr.size() * sizeof(int));
+            up(p->wz0, wz0.data(), wz0.size() * sizeof(float));
+            up(p->wz1, wz1.data(), wz1.size() * sizeof(float));
+            up(p->xr, xr.data(), xr.size() * sizeof(int));
+            up(p->wx0, wx0.data(), wx0.size() * sizeof(float));
+            up(p->wx1, wx1.data(), wx1.size() * sizeof(float));
+            up(p->fz, fzf.data(), fzf.size() * sizeof(float));
+            if (shift != nullptr) {
+                require(n_y >= 1, "n_y must be >= 1 with optical-path correction");
+                const size_t m = static_cast<size_t>(n_y) * n_tile_x;
+                std::vector<int> sh(m), lo(m), hi(m);
+                for (size_t i = 0; i < m; ++i) {
+                    sh[i] = static_cast<int>(shift[i]);
+                    // exact integer form of 0 <= r + pdz <= n_rows - 1
+                    lo[i] = static_cast<int>(ceil(-pdz[i]));
+                    hi[i] = static_cast<int>(floor(n_rows - 1 - pdz[i]));
+                }
+                up(p->shift, sh.data(), m * sizeof(int));
+                up(p->lo, lo.data(), m * sizeof(int));
+                up(p->hi, hi.data(), m * sizeof(int));
+                p->opc = true;
+            }
+            ck(cudaStreamSynchronize(c->stream), "sync plan");
+        } catch (...) {
+            p->release();
+            delete p;
+            throw;
+        }
+        c->plans.push_back(p);
+        *plan_id = static_cast<int>(c->plans.size() - 1);
+    });
+}
+
+int octgb_row_begin(octgb_ctx* c, int n_frames, int n_out_z, int n_out_x) {
+    return guarded(c, [&] {
+        require(n_frames >= 0 && n_out_z >= 1 && n_out_x >= 1, "bad row shape");
+        const size_t bytes = static_cast<size_t>(n_frames) * n_out_z * n_out_x * sizeof(float);
+        ck(c->num.ensure(bytes + 16), "cudaMalloc(num)");
+        ck(c->den.ensure(bytes + 16), "cudaMalloc(den)");
+        ck(cudaMemsetAsync(c->num.p, 0, bytes, c->stream), "memset num");
+        ck(cudaMemsetAsync(c->den.p, 0, bytes, c->stream), "memset den");
+        c->row_nf = n_frames;
+        c->row_nz = n_out_z;
+        c->row_nx = n_out_x;
+        c->row_open = true;
+    });
+}
+
+int octgb_row_add_batch(octgb_ctx* c, int plan_id, const void* raw, int dtype, int loc, int B, int interf, int apod,
+                        const int64_t* frame_idx, int frame_offset) {
+    return guarded(c, [&] {
+        if (!c->row_open) throw Error(OCTGB_ERR_STATE, "octgb_row_begin has not been called");
+        require(plan_id >= 0 && plan_id < static_cast<int>(c->plans.size()), "bad plan id");
+        const Plan& p = *c->plans[plan_id];
+        validate_raw(raw, dtype, loc, B, interf, apod);
+        require(interf - apod == p.n_tile_x, "A-scans per B-scan differ from the plan's tile width");
+        require(p.n_out_z == c->row_nz && p.c0 + p.C <= c->row_nx, "plan does not fit the row");
+        require(frame_offset >= 0 && frame_offset + B <= c->row_nf, "frames outside the row");
+        require(frame_idx != nullptr, "frame_idx is NULL");
+        std::vector<int> fy(B > 0 ? B : 1);
+        for (int f = 0; f < B; ++f) {
+            require(!p.opc || (frame_idx[f] >= 0 && frame_idx[f] < p.n_y), "frame index outside the scan");
+            fy[f] = static_cast<int>(frame_idx[f]);
+        }
+        if (B == 0) return;
+        const size_t mb = static_cast<size_t>(B) * p.n_tile_x * kHalf * sizeof(float);
+        ck(c->out.ensure(mb), "cudaMalloc(mag)");
+        ck(c->frames.ensure(fy.size() * sizeof(int)), "cudaMalloc(frames)");
+        ck(cudaMemcpyAsync(c->frames.p, fy.data(), fy.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream),
+           "H2D frames");
+        run_spectral(c, raw, dtype, loc, B, interf, apod, kModeMag, c->out.as<float>(), 0, 0, nullptr);
+        ck(launch_stitch(p.dev(), c->out.as<float>(), c->frames.as<int>(), B, c->num.as<float>(), c->den.as<float>(),
+                         frame_offset, c->row_nx, c->stream),
+           "stitch kernel");
+        c->launches++;
+        // cudaMemcpyAsync from pageable memory returns once the frame list is
+        // staged, so `fy` may go out of scope without a stream sync here
+    });
+}
+
+int octgb_row_finalise(octgb_ctx* c, float thr, float* db, int db_loc, double* plane_minmax) {
+    return guarded(c, [&] {
+        if (!c->row_open) throw Error(OCTGB_ERR_STATE, "octgb_row_begin has not been called");
+        require(db != nullptr, "db is NULL");
+        const int64_t per = static_cast<int64_t>(c->row_nz) * c->row_nx;
+        const size_t bytes = static_cast<size_t>(c->row_nf) * per * sizeof(float);
+        float* dst = db;
+        if (db_loc != OCTGB_DEVICE) {
+            ck(c->out.ensure(bytes + 16), "cudaMalloc(db)");
+            dst = c->out.as<float>();
+        }
+        unsigned int* mm = nullptr;
+        DevBuf tmp;
+        if (plane_minmax) {
+            ck(c->mm.ensure(static_cast<size_t>(2 * c->row_nf) * sizeof(unsigned int) + 16), "cudaMalloc(mm)");
+            mm = c->mm.as<unsigned int>();
+            ck(launch_minmax_init(mm, 2 * c->row_nf, c->stream), "minmax init");
+            c->launches++;
+        }
+        ck(launch_finalise(c->num.as<float>(), c->den.as<float>(), per, c->row_nf, thr, dst, mm, c->stream),
+           "finalise kernel");
+        c->launches++;
+        if (db_loc != OCTGB_DEVICE) copy_out(c, db, OCTGB_HOST, dst, bytes);
+        if (plane_minmax) {
+            std::vector<unsigned int> h(2 * static_cast<size_t>(c->row_nf));
+            ck(cudaMemcpyAsync(h.data(), mm, h.size() * sizeof(unsigned int), cudaMemcpyDeviceToHost, c->stream),
+               "D2H plane minmax");
+            check_status(c);
+            for (int f = 0; f < c->row_nf; ++f) {
+                if (h[2 * f] == 0xffffffffu) {
+                    plane_minmax[2 * f] = plane_minmax[2 * f + 1] = NAN;
+                } else {
+                    plane_minmax[2 * f] = ord2f(h[2 * f]);
+                    plane_minmax[2 * f + 1] = ord2f(h[2 * f + 1]);
+                }
+            }
+        } else {
+            check_status(c);
+        }
+        c->row_open = false;
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,96 @@
+// Internal declarations shared by the octgb CUDA translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace octgb {
+
+constexpr int kN = 2048;          // spectral samples per A-scan (FFT length)
+constexpr int kHalf = kN / 2;     // depth bins kept (core/spectral.py:153, nz = N/2)
+constexpr int kMaxTaps = 32;      // sinc taps supported
+constexpr int kTail = 32;         // zero tail after each line so padded taps stay in bounds
+constexpr int kGroup = 128;       // threads per A-scan in the FFT (16 points each)
+constexpr int kPerCta = 2;        // A-scans per CTA iteration
+constexpr int kThreads = kGroup * kPerCta;
+
+// device-side status word values
+constexpr int kStatusOk = 0;
+constexpr int kStatusTimeout = 1;
+
+enum OutMode : int { kModeSpec = 0, kModeMag = 1, kModeDb = 2 };
+
+struct DevGeometry {
+    const float* w;       // [taps][kN] sinc weights, tap-major, float32
+    const int* start;     // [kN] first source sample of each output sample
+    int taps;
+    const float2* win;    // [kN] complex64 window scaled by 1/kN (ifft normalisation)
+    const float2* tw;     // [kN] exp(+2*pi*i*k/kN), rounded from float64
+};
+
+struct SpectralArgs {
+    const void* raw;          // (B, interf, kN)
+    int B, interf, apod, nx;  // nx = interf - apod
+    int64_t n_ascans;         // B * nx
+    const float* apod_mean;   // (B, kN) float32 apodisation mean
+    DevGeometry g;
+    float* out;               // spec (M, kN, 2) | mag (M, kHalf) | db (M, nz)
+    int z0, nz;               // depth crop (db mode)
+    unsigned int* minmax;     // [2] ordered-uint min / max (db mode), may be null
+    int* status;              // device status word
+};
+
+// spectral.cu
+cudaError_t launch_apod_mean(const void* raw, int dtype, int B, int interf, int apod, float* apod_mean,
+                             cudaStream_t st);
+cudaError_t launch_spectral(const SpectralArgs& a, int dtype, int mode, int grid, cudaStream_t st);
+int spectral_max_ctas_per_sm(int dtype, int mode);
+size_t spectral_smem_bytes(int dtype);
+
+// stitch.cu
+struct StitchDev {
+    // compact 2-tap depth operator: for output row zo, rows zr[zo] and zr[zo]+1 (relative to r0)
+    const int* zr;            // [n_out_z], -1 = no contribution
+    const float* wz0;         // [n_out_z]
+    const float* wz1;         // [n_out_z]
+    // compact 2-tap lateral operator: output column c0+cc takes A-scans xr[cc], xr[cc]+1
+    const int* xr;            // [C], -1 = none
+    const float* wx0;         // [C]
+    const float* wx1;         // [C]
+    const float* fz;          // [R] focus weight of rows r0..r1-1
+    const int* shift;         // [n_y, n_tile_x] optical-path row shift, or null
+    const int* lo;            // [n_y, n_tile_x] smallest valid r (incl.), or null
+    const int* hi;            // [n_y, n_tile_x] largest valid r (incl.), or null
+    int r0, R, c0, C, n_out_z, n_tile_x, n_rows;
+};
+
+cudaError_t launch_stitch(const StitchDev& p, const float* mag, const int* frame_y, int B, float* num, float* den,
+                          int frame_offset, int n_out_x, cudaStream_t st);
+cudaError_t launch_finalise(const float* num, const float* den, int64_t n_per_plane, int n_planes, float thr,
+                            float* db, unsigned int* plane_minmax, cudaStream_t st);
+cudaError_t launch_quantise(const float* db, int64_t n, double c1, double c2, uint16_t* bits, cudaStream_t st);
+cudaError_t launch_minmax(const float* x, int64_t n, unsigned int* minmax, cudaStream_t st);
+cudaError_t launch_minmax_init(unsigned int* minmax, int count, cudaStream_t st);
+
+// ordered-uint encoding of float32 for atomic min/max
+__host__ __device__ inline unsigned int f2ord(float f) {
+#ifdef __CUDA_ARCH__
+    unsigned int u = __float_as_uint(f);
+#else
+    unsigned int u;
+    __builtin_memcpy(&u, &f, 4);
+#endif
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__host__ __device__ inline float ord2f(unsigned int u) {
+    unsigned int v = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u;
+#ifdef __CUDA_ARCH__
+    return __uint_as_float(v);
+#else
+    float f;
+    __builtin_memcpy(&f, &v, 4);
+    return f;
+#endif
+}
+
+}  // namespace octgb

@@ -1,0 +1,486 @@
+// Fused spectral stage for sm_103a: raw camera counts -> |ifft| / dB.
+//
+// One CTA of 256 threads processes two A-scans per iteration of a persistent
+// loop.  Per A-scan (2048 samples):
+//   (a) the raw row (4 KiB of uint16) is staged into shared memory by a bulk
+//       TMA copy (cp.async.bulk, mbarrier completion), double-buffered so the
+//       next pair's rows stream in while the current pair is computed;
+//   (b) d[j] = float(raw[j]) - apod[j] (float32 apodisation mean of the
+//       B-scan, rounded from an exact sum as core/cpu_kernels.py:20-25 does),
+//       line mean m removed (cpu_kernels.py:26-36);
+//   (c) banded sinc k-linearisation, sum_t w[t,i] * d[start_i + t]
+//       (cpu_kernels.py:37-40), float32 accumulation;
+//   (d) (acc + m) * window[i] (Hann/rms * dispersion phase, scaled by 1/N for
+//       the ifft normalisation, cpu_kernels.py:41, spectral.py:160-165);
+//   (e) inverse FFT of length 2048 in shared memory: Stockham radix 16,16,8,
+//       each radix butterfly in registers (128 threads, 16 points each);
+//   (f) |X[k]| for k < N/2 (spectral.py:153), optionally 20*log10 with a
+//       depth crop and a running min/max for the global clim.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "octgb_internal.h"
+
+namespace octgb {
+namespace {
+
+constexpr int kPadShift = 4;                              // one pad slot per 16 complex
+constexpr int kSpecStride = kN + (kN >> kPadShift);       // padded complex line length
+constexpr int kDStride = kN + kTail;
+
+__device__ __forceinline__ int pad(int e) { return e + (e >> kPadShift); }
+
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+    return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+__device__ __forceinline__ float2 muli(float2 a) { return make_float2(-a.y, a.x); }
+
+// inverse DFT-4 (omega = +i), natural order in and out
+__device__ __forceinline__ void dft4(float2& x0, float2& x1, float2& x2, float2& x3) {
+    const float2 a = cadd(x0, x2), b = csub(x0, x2), c = cadd(x1, x3), d = muli(csub(x1, x3));
+    x0 = cadd(a, c);
+    x2 = csub(a, c);
+    x1 = cadd(b, d);
+    x3 = csub(b, d);
+}
+
+// cos/sin of multiples of pi/8 (float64 literals rounded to float32)
+constexpr float kC1 = 0.92387953251128675613f;   // cos(pi/8)
+constexpr float kS1 = 0.38268343236508977173f;   // sin(pi/8)
+constexpr float kC2 = 0.70710678118654752440f;   // cos(pi/4)
+
+// inverse DFT-16 as 4 x 4: X[4*k1 + k2] = sum_n1 w4^(n1 k1) w16^(n1 k2) sum_n2 x[n1 + 4 n2] w4^(n2 k2)
+__device__ __forceinline__ void dft16(float2 (&v)[16]) {
+#pragma unroll
+    for (int n1 = 0; n1 < 4; ++n1) dft4(v[n1], v[n1 + 4], v[n1 + 8], v[n1 + 12]);
+    // twiddles w16^(n1*k2) on element v[n1 + 4*k2]
+    v[1 + 4] = cmul(v[1 + 4], make_float2(kC1, kS1));     // n1=1,k2=1: w^1
+    v[1 + 8] = cmul(v[1 + 8], make_float2(kC2, kC2));     // n1=1,k2=2: w^2
+    v[1 + 12] = cmul(v[1 + 12], make_float2(kS1, kC1));   // n1=1,k2=3: w^3
+    v[2 + 4] = cmul(v[2 + 4], make_float2(kC2, kC2));     // n1=2,k2=1: w^2
+    v[2 + 8] = muli(v[2 + 8]);                            // n1=2,k2=2: w^4 = i
+    v[2 + 12] = cmul(v[2 + 12], make_float2(-kC2, kC2));  // n1=2,k2=3: w^6
+    v[3 + 4] = cmul(v[3 + 4], make_float2(kS1, kC1));     // n1=3,k2=1: w^3
+    v[3 + 8] = cmul(v[3 + 8], make_float2(-kC2, kC2));    // n1=3,k2=2: w^6
+    v[3 + 12] = cmul(v[3 + 12], make_float2(-kC1, -kS1)); // n1=3,k2=3: w^9
+#pragma unroll
+    for (int k2 = 0; k2 < 4; ++k2) dft4(v[4 * k2], v[4 * k2 + 1], v[4 * k2 + 2], v[4 * k2 + 3]);
+    // X[4*k1 + k2] sits in v[k1 + 4*k2]: transpose the 4x4 block
+    float2 t;
+    t = v[1]; v[1] = v[4]; v[4] = t;
+    t = v[2]; v[2] = v[8]; v[8] = t;
+    t = v[3]; v[3] = v[12]; v[12] = t;
+    t = v[6]; v[6] = v[9]; v[9] = t;
+    t = v[7]; v[7] = v[13]; v[13] = t;
+    t = v[11]; v[11] = v[14]; v[14] = t;
+}
+
+// inverse DFT-8 as 2 x 4, returning only X[0..3] (the last stage keeps k < N/2)
+__device__ __forceinline__ void dft8_low(float2 (&v)[8], float2 (&X)[4]) {
+    dft4(v[0], v[2], v[4], v[6]);
+    dft4(v[1], v[3], v[5], v[7]);
+    const float2 y1 = cmul(v[3], make_float2(kC2, kC2));
+    const float2 y2 = muli(v[5]);
+    const float2 y3 = cmul(v[7], make_float2(-kC2, kC2));
+    X[0] = cadd(v[0], v[1]);
+    X[1] = cadd(v[2], y1);
+    X[2] = cadd(v[4], y2);
+    X[3] = cadd(v[6], y3);
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ void tma_bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Bounded wait on an mbarrier phase: gives up after ~2 s of wall time and
+// reports it through the status word (the copy it waits for is 4 KiB and
+// normally lands within microseconds).
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int* status) {
+    if (mbar_test(bar, parity)) return true;
+    const uint64_t t0 = globaltimer_ns();
+    for (uint32_t it = 0; it < (1u << 30); ++it) {
+        if (mbar_test(bar, parity)) return true;
+        __nanosleep(64);
+        if ((it & 255u) == 255u && globaltimer_ns() - t0 > 2000000000ull) break;
+    }
+    atomicExch(status, kStatusTimeout);
+    return false;
+}
+
+template <typename RawT>
+struct RawLoad;
+template <>
+struct RawLoad<uint16_t> {
+    static __device__ __forceinline__ void load4(const uint16_t* p, float (&f)[4]) {
+        const uint2 u = *reinterpret_cast<const uint2*>(p);
+        f[0] = static_cast<float>(u.x & 0xffffu);
+        f[1] = static_cast<float>(u.x >> 16);
+        f[2] = static_cast<float>(u.y & 0xffffu);
+        f[3] = static_cast<float>(u.y >> 16);
+    }
+};
+template <>
+struct RawLoad<int16_t> {
+    static __device__ __forceinline__ void load4(const int16_t* p, float (&f)[4]) {
+        const uint2 u = *reinterpret_cast<const uint2*>(p);
+        f[0] = static_cast<float>(static_cast<int16_t>(u.x & 0xffffu));
+        f[1] = static_cast<float>(static_cast<int16_t>(u.x >> 16));
+        f[2] = static_cast<float>(static_cast<int16_t>(u.y & 0xffffu));
+        f[3] = static_cast<float>(static_cast<int16_t>(u.y >> 16));
+    }
+};
+template <>
+struct RawLoad<float> {
+    static __device__ __forceinline__ void load4(const float* p, float (&f)[4]) {
+        const float4 u = *reinterpret_cast<const float4*>(p);
+        f[0] = u.x;
+        f[1] = u.y;
+        f[2] = u.z;
+        f[3] = u.w;
+    }
+};
+
+template <typename RawT>
+struct Smem {
+    uint64_t bar[2];
+    float red[kPerCta][4];
+    float mval[kPerCta];
+    unsigned int mm[2];
+    alignas(128) RawT stage[2][kPerCta][kN];      // bulk-copy destinations (16-byte aligned)
+    alignas(16) float d[kPerCta][kDStride];
+    alignas(16) float2 spec[kPerCta][kSpecStride];
+};
+
+template <typename RawT, int Mode>
+__global__ void __launch_bounds__(kThreads) k_spectral(const SpectralArgs a) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    Smem<RawT>& S = *reinterpret_cast<Smem<RawT>*>(smem_raw);
+
+    const int tid = threadIdx.x;
+    const int g = tid / kGroup;        // A-scan slot in the pair
+    const int lt = tid % kGroup;       // thread within the A-scan group
+    const int warp = tid / 32, lane = tid % 32;
+    const int64_t M = a.n_ascans;
+    const int64_t npairs = (M + kPerCta - 1) / kPerCta;
+    const int taps = a.g.taps;
+
+    if (tid == 0) {
+        mbar_init(&S.bar[0], 1);
+        mbar_init(&S.bar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        S.mm[0] = 0xffffffffu;
+        S.mm[1] = 0u;
+    }
+    for (int k = tid; k < kPerCta * kTail; k += kThreads) S.d[k / kTail][kN + k % kTail] = 0.f;
+
+    // per-thread sinc band starts of its 8 output samples (i = tid + 256 r)
+    int st[8];
+#pragma unroll
+    for (int r = 0; r < 8; ++r) st[r] = __ldg(a.g.start + tid + kThreads * r);
+
+    float run_min = __int_as_float(0x7f800000), run_max = -__int_as_float(0x7f800000);
+    __syncthreads();
+
+    auto issue = [&](int64_t pair, int buf) {
+        uint32_t bytes = 0;
+        int64_t a0 = pair * kPerCta;
+        int nvalid = static_cast<int>(M - a0 < kPerCta ? M - a0 : kPerCta);
+        bytes = static_cast<uint32_t>(nvalid) * kN * sizeof(RawT);
+        mbar_expect_tx(&S.bar[buf], bytes);
+        for (int s = 0; s < nvalid; ++s) {
+            const int64_t as = a0 + s;
+            const int64_t b = as / a.nx, x = as - b * a.nx;
+            const RawT* src = static_cast<const RawT*>(a.raw) + ((b * a.interf + a.apod + x) * kN);
+            tma_bulk_g2s(&S.stage[buf][s][0], src, kN * sizeof(RawT), &S.bar[buf]);
+        }
+    };
+
+    if (tid == 0 && blockIdx.x < npairs) issue(blockIdx.x, 0);
+
+    int it = 0;
+    for (int64_t pair = blockIdx.x; pair < npairs; pair += gridDim.x, ++it) {
+        const int buf = it & 1;
+        const int64_t next = pair + gridDim.x;
+        if (tid == 0 && next < npairs) issue(next, buf ^ 1);
+
+        const bool ok = mbar_wait_bounded(&S.bar[buf], (it >> 1) & 1, a.status);
+        if (__syncthreads_or(!ok)) return;
+
+        // ---- (b) background: d = raw - apod, line mean ----
+        const int64_t as = pair * kPerCta + g;
+        const bool valid = as < M;
+        const int64_t bsc = valid ? as / a.nx : 0;
+        const float* apod = a.apod_mean + bsc * kN;
+        float dv[16];
+        float sum = 0.f;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int j = 4 * lt + 512 * q;
+            float rv[4];
+            RawLoad<RawT>::load4(&S.stage[buf][g][j], rv);
+            const float4 ap = __ldg(reinterpret_cast<const float4*>(apod + j));
+            dv[4 * q + 0] = rv[0] - ap.x;
+            dv[4 * q + 1] = rv[1] - ap.y;
+            dv[4 * q + 2] = rv[2] - ap.z;
+            dv[4 * q + 3] = rv[3] - ap.w;
+            sum += (dv[4 * q + 0] + dv[4 * q + 1]) + (dv[4 * q + 2] + dv[4 * q + 3]);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+        if (lane == 0) S.red[g][warp & 3] = sum;
+        __syncthreads();
+        const float m = ((S.red[g][0] + S.red[g][1]) + (S.red[g][2] + S.red[g][3])) * (1.0f / kN);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int j = 4 * lt + 512 * q;
+            *reinterpret_cast<float4*>(&S.d[g][j]) =
+                make_float4(dv[4 * q] - m, dv[4 * q + 1] - m, dv[4 * q + 2] - m, dv[4 * q + 3] - m);
+        }
+        if (lt == 0) S.mval[g] = m;
+        __syncthreads();
+
+        // ---- (c)+(d) sinc k-linearisation and window, both A-scans ----
+        {
+            float acc0[8], acc1[8];
+#pragma unroll
+            for (int r = 0; r < 8; ++r) acc0[r] = acc1[r] = 0.f;
+            for (int k = 0; k < taps; ++k) {
+                const float* wk = a.g.w + static_cast<int64_t>(k) * kN + tid;
+#pragma unroll
+                for (int r = 0; r < 8; ++r) {
+                    const float wv = __ldg(wk + kThreads * r);
+                    acc0[r] = fmaf(wv, S.d[0][st[r] + k], acc0[r]);
+                    acc1[r] = fmaf(wv, S.d[1][st[r] + k], acc1[r]);
+                }
+            }
+            const float m0 = S.mval[0], m1 = S.mval[1];
+            const int64_t a0 = pair * kPerCta;
+#pragma unroll
+            for (int r = 0; r < 8; ++r) {
+                const int i = tid + kThreads * r;
+                const float2 w = __ldg(a.g.win + i);
+                const float v0 = acc0[r] + m0, v1 = acc1[r] + m1;
+                const float2 s0 = make_float2(v0 * w.x, v0 * w.y);
+                const float2 s1 = make_float2(v1 * w.x, v1 * w.y);
+                if (Mode == kModeSpec) {
+                    // spec output undoes the 1/N ifft scaling folded into the window
+                    float2* o = reinterpret_cast<float2*>(a.out);
+                    if (a0 < M) o[a0 * kN + i] = make_float2(s0.x * kN, s0.y * kN);
+                    if (a0 + 1 < M) o[(a0 + 1) * kN + i] = make_float2(s1.x * kN, s1.y * kN);
+                } else {
+                    S.spec[0][pad(i)] = s0;
+                    S.spec[1][pad(i)] = s1;
+                }
+            }
+        }
+        if (Mode == kModeSpec) {
+            __syncthreads();
+            continue;
+        }
+        __syncthreads();
+
+        // ---- (e) inverse FFT, group g on its own line ----
+        float2* X = S.spec[g];
+        {
+            float2 v[16];
+#pragma unroll
+            for (int r = 0; r < 16; ++r) v[r] = X[pad(lt + 128 * r)];
+            dft16(v);
+            __syncthreads();
+#pragma unroll
+            for (int r = 0; r < 16; ++r) X[pad(16 * lt + r)] = v[r];
+            __syncthreads();
+        }
+        {
+            float2 v[16];
+            const int jm = lt & 15;
+#pragma unroll
+            for (int r = 0; r < 16; ++r) v[r] = X[pad(lt + 128 * r)];
+#pragma unroll
+            for (int r = 1; r < 16; ++r) v[r] = cmul(v[r], __ldg(a.g.tw + r * jm * (kN / 256)));
+            dft16(v);
+            __syncthreads();
+            const int idxD = (lt >> 4) * 256 + jm;
+#pragma unroll
+            for (int r = 0; r < 16; ++r) X[pad(idxD + 16 * r)] = v[r];
+            __syncthreads();
+        }
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int j = lt + 128 * h;
+            float2 v[8];
+#pragma unroll
+            for (int r = 0; r < 8; ++r) v[r] = X[pad(j + 256 * r)];
+#pragma unroll
+            for (int r = 1; r < 8; ++r) v[r] = cmul(v[r], __ldg(a.g.tw + r * j));
+            float2 Xk[4];
+            dft8_low(v, Xk);
+            if (valid) {
+#pragma unroll
+                for (int r = 0; r < 4; ++r) {
+                    const int k = j + 256 * r;
+                    const float mag = __fsqrt_rn(fmaf(Xk[r].x, Xk[r].x, Xk[r].y * Xk[r].y));
+                    if (Mode == kModeMag) {
+                        a.out[as * kHalf + k] = mag;
+                    } else {
+                        const int z = k - a.z0;
+                        if (z >= 0 && z < a.nz) {
+                            const float db = 20.0f * log10f(mag);
+                            a.out[as * a.nz + z] = db;
+                            if (isfinite(db)) {
+                                run_min = fminf(run_min, db);
+                                run_max = fmaxf(run_max, db);
+                            }
+                        }
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+
+    if (Mode == kModeDb && a.minmax != nullptr) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            run_min = fminf(run_min, __shfl_xor_sync(0xffffffffu, run_min, o));
+            run_max = fmaxf(run_max, __shfl_xor_sync(0xffffffffu, run_max, o));
+        }
+        if (lane == 0 && run_min <= run_max) {
+            atomicMin(&S.mm[0], f2ord(run_min));
+            atomicMax(&S.mm[1], f2ord(run_max));
+        }
+        __syncthreads();
+        if (tid == 0 && S.mm[0] != 0xffffffffu) {
+            atomicMin(&a.minmax[0], S.mm[0]);
+            atomicMax(&a.minmax[1], S.mm[1]);
+        }
+    }
+}
+
+// apodisation mean (cpu_kernels.py:20-25): exact sum, divided in float64, stored float32
+template <typename RawT>
+__global__ void k_apod_mean(const RawT* __restrict__ raw, int B, int interf, int apod, float* __restrict__ out) {
+    const int b = blockIdx.y;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= B || j >= kN) return;
+    const RawT* p = raw + static_cast<int64_t>(b) * interf * kN + j;
+    double s;
+    if (sizeof(RawT) == 2) {
+        int acc = 0;
+        for (int k = 0; k < apod; ++k) acc += static_cast<int>(p[static_cast<int64_t>(k) * kN]);
+        s = static_cast<double>(acc);
+    } else {
+        s = 0.0;
+        for (int k = 0; k < apod; ++k) s += static_cast<double>(p[static_cast<int64_t>(k) * kN]);
+    }
+    out[static_cast<int64_t>(b) * kN + j] = static_cast<float>(s / apod);
+}
+
+template <typename RawT, int Mode>
+cudaError_t launch_t(const SpectralArgs& a, int grid, cudaStream_t st) {
+    const size_t smem = sizeof(Smem<RawT>);
+    cudaError_t e = cudaFuncSetAttribute(k_spectral<RawT, Mode>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(smem));
+    if (e != cudaSuccess) return e;
+    k_spectral<RawT, Mode><<<grid, kThreads, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+template <typename RawT>
+cudaError_t launch_mode(const SpectralArgs& a, int mode, int grid, cudaStream_t st) {
+    switch (mode) {
+        case kModeSpec: return launch_t<RawT, kModeSpec>(a, grid, st);
+        case kModeMag: return launch_t<RawT, kModeMag>(a, grid, st);
+        default: return launch_t<RawT, kModeDb>(a, grid, st);
+    }
+}
+
+template <typename RawT, int Mode>
+int occupancy_t() {
+    const size_t smem = sizeof(Smem<RawT>);
+    if (cudaFuncSetAttribute(k_spectral<RawT, Mode>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(smem)) != cudaSuccess)
+        return 1;
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_spectral<RawT, Mode>, kThreads, smem) != cudaSuccess)
+        return 1;
+    return n > 0 ? n : 1;
+}
+
+template <typename RawT>
+int occupancy_mode(int mode) {
+    switch (mode) {
+        case kModeSpec: return occupancy_t<RawT, kModeSpec>();
+        case kModeMag: return occupancy_t<RawT, kModeMag>();
+        default: return occupancy_t<RawT, kModeDb>();
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_apod_mean(const void* raw, int dtype, int B, int interf, int apod, float* apod_mean,
+                             cudaStream_t st) {
+    const dim3 grid(kN / 256, B);
+    if (dtype == 0)
+        k_apod_mean<uint16_t><<<grid, 256, 0, st>>>(static_cast<const uint16_t*>(raw), B, interf, apod, apod_mean);
+    else if (dtype == 1)
+        k_apod_mean<int16_t><<<grid, 256, 0, st>>>(static_cast<const int16_t*>(raw), B, interf, apod, apod_mean);
+    else
+        k_apod_mean<float><<<grid, 256, 0, st>>>(static_cast<const float*>(raw), B, interf, apod, apod_mean);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_spectral(const SpectralArgs& a, int dtype, int mode, int grid, cudaStream_t st) {
+    if (dtype == 0) return launch_mode<uint16_t>(a, mode, grid, st);
+    if (dtype == 1) return launch_mode<int16_t>(a, mode, grid, st);
+    return launch_mode<float>(a, mode, grid, st);
+}
+
+int spectral_max_ctas_per_sm(int dtype, int mode) {
+    if (dtype == 0) return occupancy_mode<uint16_t>(mode);
+    if (dtype == 1) return occupancy_mode<int16_t>(mode);
+    return occupancy_mode<float>(mode);
+}
+
+size_t spectral_smem_bytes(int dtype) {
+    return dtype == 2 ? sizeof(Smem<float>) : sizeof(Smem<uint16_t>);
+}
+
+}  // namespace octgb
