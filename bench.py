@@ -43,19 +43,23 @@ APOD = 25
 
 
 # ------------------------------------------------------------------------ workload description
-def config1_layout(seed=1):
+def config1_layout(seed=1, bscans=270):
+    """Config-1 scan layout; `bscans` < 270 gives a small case of the same
+    geometry (used for profiling captures)."""
     from oct_recon_af_v1_gb300 import stitching as S
     rng = np.random.default_rng(seed)
-    lay = S.ScanLayout(np.array([-0.45, 0.45]), np.array([-0.1215, 0.1215]), np.array([0.0, 0.15, 0.30]),
-                       1000, 270, 1.0, 0.27)
+    ty = int(bscans) * 1e-3                       # 1 um y pixels
+    lay = S.ScanLayout(np.array([-0.45, 0.45]), np.array([-0.45 * ty, 0.45 * ty]), np.array([0.0, 0.15, 0.30]),
+                       1000, int(bscans), 1.0, ty)
     focus = 400.0 + rng.uniform(-30, 30, 3)
     return lay, focus
 
 
-def config1_desc():
-    return {"workload": "config1: 2x2 tiles x 3 depths, tile 270 B-scans x 1000 A-scans x 2048 uint16, "
+def config1_desc(bscans=270):
+    return {"workload": f"config1: 2x2 tiles x 3 depths, tile {bscans} B-scans x 1000 A-scans x 2048 uint16, "
                         "focus 400+-30 px sigma 80, 10% overlap, n 1.33, 1 um output, uint16 legacy codes",
-            "a_scans_per_step": 12 * 270 * 1000, "tiles": 12, "bscans_per_tile": 270, "ascans_per_bscan": 1000,
+            "a_scans_per_step": 12 * bscans * 1000, "tiles": 12, "bscans_per_tile": bscans,
+            "ascans_per_bscan": 1000,
             "apod_lines": APOD, "spectral_samples": 2048, "l2_flush": "inputs (13.3 GB) larger than L2"}
 
 
@@ -132,11 +136,11 @@ def peaks():
 class Volume:
     """Config-1 scan: geometry, stitch plans and the raw tiles (device and/or pinned host)."""
 
-    def __init__(self, ctx, torch, dev, host_copy: bool, seed: int = 1):
+    def __init__(self, ctx, torch, dev, host_copy: bool, seed: int = 1, bscans: int = 270):
         from oct_recon_af_v1_gb300 import geometry as G
         from oct_recon_af_v1_gb300 import stitching as S
         from oct_recon_af_v1_gb300 import synthetic
-        self.lay, self.focus = config1_layout(seed)
+        self.lay, self.focus = config1_layout(seed, bscans)
         lam = synthetic.lambda_nm()
         self.sg = G.build_spectral_geometry(lam, synthetic.beta_ref_from_px(1e-5), 1.33)
         ctx.set_geometry(self.sg.sinc_idx, self.sg.sinc_w, self.sg.window)
@@ -171,39 +175,37 @@ class Volume:
         return sum(int(t.numel()) * 2 for t in self.raw.values())
 
 
-def run_step(ctx, vol, src, db_vol, bits, batch=30):
-    """One whole-volume reconstruction; src maps tile keys to device or host int16 tensors."""
-    clims = []
+def run_step(ctx, vol, src, db_vol, bits, batch=2):
+    """One whole-volume reconstruction through the frame-batch API: for each
+    y-row and each batch of `batch` frames, every tile's spectral stage and
+    the stitched, finalised planes (num/den never leave the chip; the
+    magnitudes of a batch stay in L2); then the legacy quantisation with the
+    running (global) clim read on the device.  src maps tile keys to device or
+    pinned-host int16 tensors holding uint16 spectra."""
+    ids = [vol.st[k].plan for k in vol.order]
+    ctx.clim_reset()
     for yi in range(2):
-        ctx.row_begin(vol.ny, vol.nz, vol.nx)
-        for xi, zi in vol.order:
-            t = src[(yi, xi, zi)]
-            st = vol.st[(xi, zi)]
-            for s in range(0, vol.ny, batch):
-                ctx.row_add_batch(st.plan, t[s:s + batch], APOD, vol.frames[s:s + batch], s, raw_dtype=0)
-        out = db_vol[yi * vol.ny:(yi + 1) * vol.ny]
-        _, mm = ctx.row_finalise(vol.thr, (vol.ny, vol.nz, vol.nx), out, plane_minmax=True)
-        clims.append(mm)
-    mm = np.concatenate(clims)
-    clim = (float(np.nanmin(mm[:, 0])), float(np.nanmax(mm[:, 1])))
-    ctx.quantise(db_vol, clim, bits)
-    return clim
+        for s in range(0, vol.ny, batch):
+            raws = [src[(yi, xi, zi)][s:s + batch] for xi, zi in vol.order]
+            o = yi * vol.ny + s
+            ctx.frames_process(ids, raws, APOD, s, vol.nz, vol.nx, vol.thr, out=db_vol[o:o + len(raws[0])],
+                               raw_dtype=0)
+    ctx.quantise_running(db_vol, bits)
 
 
-def time_spectral_kernel(ctx, torch, raw_tile, reps=10):
-    """CUDA-event time of the spectral stage (apod mean + fused kernel) on one tile."""
+def time_spectral_kernel(ctx, torch, raw_tile, stream, reps=10):
+    """CUDA-event time of the spectral stage (apod mean + fused kernel) on a slab of one tile."""
     B = raw_tile.shape[0]
     nxa = raw_tile.shape[1] - APOD
     out = torch.empty((B, nxa, 1024), dtype=torch.float32, device="cuda")
     for _ in range(2):
         ctx.magnitude(raw_tile, APOD, out, raw_dtype=0)
-    st = torch.cuda.current_stream()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
-    e0.record(st)
+    e0.record(stream)
     for _ in range(reps):
         ctx.magnitude(raw_tile, APOD, out, raw_dtype=0)
-    e1.record(st)
+    e1.record(stream)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / reps
     bytes_per_launch = B * raw_tile.shape[1] * 2048 * 2 + B * nxa * 1024 * 4
@@ -217,39 +219,51 @@ def gpu_arm(args, rank, world):
     build()
     dev = f"cuda:{int(os.environ.get('LOCAL_RANK', 0))}"
     torch.cuda.set_device(dev)
+    stream = torch.cuda.Stream()            # a real stream handle: the library launches on it
+    torch.cuda.set_stream(stream)
     ctx = Context(torch.cuda.current_device())
-    ctx.set_stream(torch.cuda.current_stream().cuda_stream)
+    ctx.set_stream(stream.cuda_stream)
     if args.config == 0:
         return gpu_arm_config0(args, rank, world, torch, ctx)
-    vol = Volume(ctx, torch, dev, host_copy=not args.no_e2e)
+    vol = Volume(ctx, torch, dev, host_copy=not args.no_e2e, bscans=args.bscans)
     n_out = (2 * vol.ny, vol.nz, vol.nx)
     db_vol = torch.empty(n_out, dtype=torch.float32, device=dev)
     bits = torch.empty(n_out, dtype=torch.int16, device=dev)
     ascans = 12 * vol.ny * vol.lay.n_x_px
 
+    graph = None
+    if not args.no_graph:
+        run_step(ctx, vol, vol.raw, db_vol, bits, args.batch)      # sizes every buffer
+        ctx.synchronize()
+        ctx.graph_begin()
+        run_step(ctx, vol, vol.raw, db_vol, bits, args.batch)
+        graph = ctx.graph_end()
+
+    def step(src, e2e=False, host_bits=None):
+        if graph is not None and not e2e:
+            ctx.graph_launch(graph)
+        else:
+            run_step(ctx, vol, src, db_vol, bits, args.batch)
+        if e2e:
+            host_bits.copy_(bits, non_blocking=True)
+
     def timed(src, steps, warm, e2e=False):
         host_bits = torch.empty(n_out, dtype=torch.int16, pin_memory=True) if e2e else None
         for _ in range(warm):
-            run_step(ctx, vol, src, db_vol, bits)
-            if e2e:
-                host_bits.copy_(bits, non_blocking=True)
+            step(src, e2e, host_bits)
         torch.cuda.synchronize()
         if world > 1:
             torch.distributed.barrier()
         n0 = ctx.launches
-        st = torch.cuda.current_stream()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(st)
+        e0.record(stream)
         for _ in range(steps):
-            run_step(ctx, vol, src, db_vol, bits)
-            if e2e:
-                host_bits.copy_(bits, non_blocking=True)
-        e1.record(st)
+            step(src, e2e, host_bits)
+        e1.record(stream)
         torch.cuda.synchronize()
         if world > 1:
             torch.distributed.barrier()
-        ms = e0.elapsed_time(e1) / steps
-        return ms, ctx.launches - n0
+        return e0.elapsed_time(e1) / steps, ctx.launches - n0
 
     clocks = Clocks(int(os.environ.get("LOCAL_RANK", 0)))
     clocks.start()
@@ -258,8 +272,8 @@ def gpu_arm(args, rank, world):
     e2e_ms = None
     if not args.no_e2e:
         e2e_ms, _ = timed(vol.host, max(1, args.steps // 2), 1, e2e=True)
-    # roofline of the dominant kernel, measured live on one tile
-    kms, kbytes, kascans = time_spectral_kernel(ctx, torch, vol.raw[(0, 0, 0)])
+    # roofline of the dominant kernel, measured live on a 30-B-scan slab of one tile
+    kms, kbytes, kascans = time_spectral_kernel(ctx, torch, vol.raw[(0, 0, 0)][:30], stream)
     ms_all = reduce_max(ms, world)
     hbm, src = peaks()
     achieved = kbytes / (kms * 1e-3) / 1e9
@@ -268,10 +282,11 @@ def gpu_arm(args, rank, world):
         "metric": METRIC, "value": value, "unit": "A-scans/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_all, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 (uint16 in, uint16 out)", "data": "synthetic (seeded, generated on device)",
-        "config": dict(config1_desc(), parallelism=f"replicas x{world} (independent volumes)"),
+        "config": dict(config1_desc(vol.ny), parallelism=f"replicas x{world} (independent volumes)",
+                       frame_batch=args.batch, cuda_graph=graph is not None),
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": None, "kernel": "apod mean + k_spectral (magnitude mode), one tile per launch",
+                     "traffic": None, "kernel": "spectral stage (apod mean + k_spectral, magnitude out)",
                      "bytes_per_launch": kbytes, "ms_per_launch": kms, "a_scans_per_launch": kascans,
                      "peak_source": src + " (burst copy)"},
         "clocks": clk,
@@ -438,6 +453,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--ref-frames", type=int, default=4)
+    ap.add_argument("--batch", type=int, default=2, help="frames per frame batch")
+    ap.add_argument("--bscans", type=int, default=270, help="B-scans per tile (270 = the full workload)")
+    ap.add_argument("--no-graph", action="store_true")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))

@@ -148,6 +148,45 @@ int octgb_row_add_batch(octgb_ctx *ctx, int plan_id, const void *raw, int raw_dt
  * plane's clim (tiff_writer.py:48-50). */
 int octgb_row_finalise(octgb_ctx *ctx, float threshold, float *db, int db_loc, double *plane_minmax);
 
+
+/* ---------------------------------------------------------------- frame batches */
+
+/* One batch of frames across all tiles of a y-tile row (the body of
+ * Reconstructor.process_row, octrecon/pipeline.py:261-300, with the loop
+ * order frames-outer / tiles-inner, which gives every voxel the same tile
+ * summation order as the reference's tiles-outer loop):
+ *   spectral stage of raws[t] (B, interf, n) for t < n_tiles (one launch);
+ *   stitching of every tile in array order (plan_ids[t], TileStitcher.contribute,
+ *   stitching.py:122-139), with num/den kept on chip;
+ *   finalise (pipeline.py:296-300) into db (B, n_out_z, n_out_x) float32.
+ * f0: tile-local y frame of the batch's first B-scan (frames are consecutive).
+ * The finite [min, max] of db folds into the context's running clim (see
+ * octgb_clim_reset); plane_minmax (optional, host, B*2 doubles) receives each
+ * plane's clim and forces a host sync.  With device raws, device db and no
+ * plane_minmax the call does not synchronise and can be graph-captured.
+ * n_tiles <= 32. */
+int octgb_frames_process(octgb_ctx *ctx, int n_tiles, const int *plan_ids, const void *const *raws, int raw_dtype,
+                         int raw_loc, int B, int interf, int apod_size, int f0, int n_out_z, int n_out_x,
+                         float threshold, float *db, int db_loc, double *plane_minmax);
+
+/* Running clim over everything octgb_frames_process wrote since the last reset
+ * (the global clim of octrecon/pipeline.py:388). */
+int octgb_clim_reset(octgb_ctx *ctx);
+int octgb_clim_get(octgb_ctx *ctx, double *clim);
+/* db_to_bits with the running clim read on the device (no host round trip;
+ * device arrays only). */
+int octgb_quantise_running(octgb_ctx *ctx, const float *db, int64_t n, int db_loc, uint16_t *bits, int bits_loc);
+
+/* ---------------------------------------------------------------- CUDA graphs */
+
+/* Capture the calls made between begin and end on the context's stream into a
+ * CUDA graph, replayed by octgb_graph_launch.  Calls that read results on the
+ * host or take host buffers are refused while capturing; run the sequence once
+ * before capturing so every device buffer already has its size. */
+int octgb_graph_begin(octgb_ctx *ctx);
+int octgb_graph_end(octgb_ctx *ctx, int *graph_id);
+int octgb_graph_launch(octgb_ctx *ctx, int graph_id);
+
 #ifdef __cplusplus
 }
 #endif

@@ -41,6 +41,14 @@ SIGNATURES = {
     "octgb_row_begin": (c_int, [c_void_p, c_int, c_int, c_int]),
     "octgb_row_add_batch": (c_int, [c_void_p, c_int, c_void_p, c_int, c_int, c_int, c_int, c_int, c_void_p, c_int]),
     "octgb_row_finalise": (c_int, [c_void_p, c_float, c_void_p, c_int, c_void_p]),
+    "octgb_frames_process": (c_int, [c_void_p, c_int, c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_int, c_int,
+                                     c_int, c_int, c_float, c_void_p, c_int, c_void_p]),
+    "octgb_clim_reset": (c_int, [c_void_p]),
+    "octgb_clim_get": (c_int, [c_void_p, c_void_p]),
+    "octgb_quantise_running": (c_int, [c_void_p, c_void_p, c_int64, c_int, c_void_p, c_int]),
+    "octgb_graph_begin": (c_int, [c_void_p]),
+    "octgb_graph_end": (c_int, [c_void_p, POINTER(c_int)]),
+    "octgb_graph_launch": (c_int, [c_void_p, c_int]),
 }
 
 _lib = None
@@ -250,3 +258,60 @@ class Context:
         self._check(self.lib.octgb_row_finalise(self.h, c_float(threshold), op, oloc,
                                                 None if mm is None else mm.ctypes.data))
         return (out, mm) if plane_minmax else out
+
+    # -------------------------------------------------------------- frame batches
+    def frames_process(self, plan_ids, raws, apod_size: int, f0: int, n_out_z: int, n_out_x: int,
+                       threshold: float, out=None, plane_minmax: bool = False, raw_dtype=None):
+        """Spectral + stitch + finalise of one frame batch over several tiles
+        (raws[t] of shape (B, interf, N), all on the host or all on the device)."""
+        n = len(raws)
+        if n != len(plan_ids) or n == 0:
+            raise ValueError("one raw batch per plan id")
+        ptrs, locs, keep = [], set(), []
+        dt = None
+        for r in raws:
+            r2, p, loc, d, B, interf = self._raw_args(r, apod_size, raw_dtype)
+            keep.append(r2)
+            ptrs.append(p)
+            locs.add(loc)
+            dt = d if dt is None else dt
+            if d != dt:
+                raise ValueError("all raw batches must share one dtype")
+        if len(locs) != 1:
+            raise ValueError("raw batches must all be host or all device arrays")
+        if out is None:
+            out = np.empty((B, n_out_z, n_out_x), np.float32)
+        op, oloc = _ptr(out)
+        ids = (c_int * n)(*[int(i) for i in plan_ids])
+        arr = (c_void_p * n)(*ptrs)
+        mm = np.full((B, 2), np.nan) if plane_minmax else None
+        self._check(self.lib.octgb_frames_process(
+            self.h, n, ids, arr, dt, locs.pop(), B, interf, int(apod_size), int(f0), int(n_out_z), int(n_out_x),
+            c_float(threshold), op, oloc, None if mm is None else mm.ctypes.data))
+        return (out, mm) if plane_minmax else out
+
+    def clim_reset(self):
+        self._check(self.lib.octgb_clim_reset(self.h))
+
+    def clim_get(self):
+        c = np.full(2, np.nan)
+        self._check(self.lib.octgb_clim_get(self.h, c.ctypes.data))
+        return float(c[0]), float(c[1])
+
+    def quantise_running(self, db, out):
+        p, loc = _ptr(db)
+        op, oloc = _ptr(out)
+        self._check(self.lib.octgb_quantise_running(self.h, p, int(np.prod(db.shape)), loc, op, oloc))
+        return out
+
+    # -------------------------------------------------------------- graphs
+    def graph_begin(self):
+        self._check(self.lib.octgb_graph_begin(self.h))
+
+    def graph_end(self) -> int:
+        gid = c_int(-1)
+        self._check(self.lib.octgb_graph_end(self.h, ctypes.byref(gid)))
+        return gid.value
+
+    def graph_launch(self, gid: int):
+        self._check(self.lib.octgb_graph_launch(self.h, int(gid)))

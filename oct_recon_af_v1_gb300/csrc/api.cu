@@ -47,7 +47,8 @@ struct DevBuf {
 
 struct Plan {
     int n_rows, r0, R, c0, C, n_out_z, n_tile_x, n_y;
-    DevBuf zr, wz0, wz1, xr, wx0, wx1, fz, shift, lo, hi;
+    int cblk_first = 0, n_cblk = 0, xs_max = 1, rs_max = 1;
+    DevBuf zr, wz0, wz1, xr, wx0, wx1, fz, shift, lo, hi, zblk, cblk;
     bool opc = false;
     StitchDev dev() const {
         StitchDev d;
@@ -61,6 +62,10 @@ struct Plan {
         d.shift = opc ? shift.as<int>() : nullptr;
         d.lo = opc ? lo.as<int>() : nullptr;
         d.hi = opc ? hi.as<int>() : nullptr;
+        d.zblk = zblk.as<int2>();
+        d.cblk = cblk.as<int2>();
+        d.cblk_first = cblk_first;
+        d.n_cblk = n_cblk;
         d.r0 = r0;
         d.R = R;
         d.c0 = c0;
@@ -71,7 +76,7 @@ struct Plan {
         return d;
     }
     void release() {
-        for (DevBuf* b : {&zr, &wz0, &wz1, &xr, &wx0, &wx1, &fz, &shift, &lo, &hi}) b->release();
+        for (DevBuf* b : {&zr, &wz0, &wz1, &xr, &wx0, &wx1, &fz, &shift, &lo, &hi, &zblk, &cblk}) b->release();
     }
 };
 
@@ -96,13 +101,22 @@ struct octgb_ctx {
     // geometry
     bool has_geom = false;
     int taps = 0;
-    DevBuf w, start, win, tw;
+    int U = 0;
+    DevBuf w, start, win, tw, wsh, s0;
     // work buffers
     DevBuf raw, apod, out, mm, frames;
     int* status_host = nullptr;  // mapped pinned status word
     int* status_dev = nullptr;
     // plans and row state
     std::vector<Plan*> plans;
+    DevBuf plan_table;           // device array of StitchDev, one per plan
+    int xs_max = 1, rs_max = 1;  // largest stitch patch over all plans
+    DevBuf run_mm;               // running [min, max] (ordered uint) of finite dB
+    std::vector<cudaGraphExec_t> graphs;
+    std::vector<int64_t> graph_kernels;
+    bool capturing = false;
+    int64_t capture_launch0 = 0;
+    DevBuf magbuf, dbbuf, planemm, segs, qtable;
     DevBuf num, den;
     int row_nf = 0, row_nz = 0, row_nx = 0;
     bool row_open = false;
@@ -152,6 +166,7 @@ const void* stage_raw(octgb_ctx* c, const void* raw, int dtype, int loc, size_t 
 }
 
 void check_status(octgb_ctx* c) {
+    if (c->capturing) throw Error(OCTGB_ERR_STATE, "a host-synchronising call was made during graph capture");
     ck(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
     const int s = *reinterpret_cast<volatile int*>(c->status_host);
     if (s != kStatusOk) {
@@ -170,40 +185,53 @@ void validate_raw(const void* raw, int dtype, int loc, int B, int interf, int ap
     if (loc == OCTGB_DEVICE) require((reinterpret_cast<uintptr_t>(raw) & 15u) == 0, "device raw must be 16-byte aligned");
 }
 
-// Run the spectral stage of a batch into `out` (device) in the given mode.
-void run_spectral(octgb_ctx* c, const void* raw, int dtype, int loc, int B, int interf, int apod, int mode,
-                  float* out_dev, int z0, int nz, unsigned int* mm_dev) {
-    if (!c->has_geom) throw Error(OCTGB_ERR_STATE, "octgb_set_geometry has not been called");
-    if (c->cancel.load()) throw Error(OCTGB_ERR_CANCELLED, "cancelled");
-    const size_t bytes = static_cast<size_t>(B) * interf * kN * raw_elem(dtype);
-    const void* rd = stage_raw(c, raw, dtype, loc, bytes);
-    ck(c->apod.ensure(static_cast<size_t>(B) * kN * sizeof(float) + 16), "cudaMalloc(apod)");
-    ck(launch_apod_mean(rd, dtype, B, interf, apod, c->apod.as<float>(), c->stream), "apod kernel");
-    c->launches++;
+// Launch apod mean + fused spectral kernel over n_seg device batches (same B, interf, apod).
+void launch_spectral_segs(octgb_ctx* c, const void* const* segs, int n_seg, int dtype, int B, int interf, int apod,
+                          int mode, float* out_dev, int z0, int nz, unsigned int* mm_dev) {
+    if (B == 0 || n_seg == 0) return;
+    ck(c->apod.ensure(static_cast<size_t>(n_seg) * B * kN * sizeof(float) + 16), "cudaMalloc(apod)");
     SpectralArgs a{};
-    a.raw = rd;
+    a.raw = segs[0];
+    for (int i = 0; i < n_seg; ++i) a.seg[i] = segs[i];
+    a.n_seg = n_seg;
     a.B = B;
     a.interf = interf;
     a.apod = apod;
     a.nx = interf - apod;
-    a.n_ascans = static_cast<int64_t>(B) * (interf - apod);
+    a.n_ascans = static_cast<int64_t>(n_seg) * B * (interf - apod);
     a.apod_mean = c->apod.as<float>();
     a.g.w = c->w.as<float>();
     a.g.start = c->start.as<int>();
     a.g.taps = c->taps;
     a.g.win = c->win.as<float2>();
     a.g.tw = c->tw.as<float2>();
+    a.g.wsh = c->wsh.as<float>();
+    a.g.s0 = c->s0.as<int>();
+    a.g.U = c->U;
     a.out = out_dev;
     a.z0 = z0;
     a.nz = nz;
     a.minmax = mm_dev;
     a.status = c->status_dev;
+    ck(launch_apod_mean(a, dtype, c->stream), "apod kernel");
+    c->launches++;
     const int64_t pairs = (a.n_ascans + kPerCta - 1) / kPerCta;
     int64_t grid = static_cast<int64_t>(c->num_sms) * spectral_max_ctas_per_sm(dtype, mode);
     if (grid > pairs) grid = pairs;
     if (grid < 1) return;
     ck(launch_spectral(a, dtype, mode, static_cast<int>(grid), c->stream), "spectral kernel");
     c->launches++;
+}
+
+// Run the spectral stage of a batch into `out` (device) in the given mode.
+void run_spectral(octgb_ctx* c, const void* raw, int dtype, int loc, int B, int interf, int apod, int mode,
+                  float* out_dev, int z0, int nz, unsigned int* mm_dev) {
+    if (!c->has_geom) throw Error(OCTGB_ERR_STATE, "octgb_set_geometry has not been called");
+    if (c->cancel.load()) throw Error(OCTGB_ERR_CANCELLED, "cancelled");
+    if (B == 0) return;  // empty batch: nothing to launch
+    const size_t bytes = static_cast<size_t>(B) * interf * kN * raw_elem(dtype);
+    const void* rd = stage_raw(c, raw, dtype, loc, bytes);
+    launch_spectral_segs(c, &rd, 1, dtype, B, interf, apod, mode, out_dev, z0, nz, mm_dev);
 }
 
 void copy_out(octgb_ctx* c, void* dst, int loc, const void* src_dev, size_t bytes) {
@@ -274,9 +302,11 @@ int octgb_destroy(octgb_ctx* c) {
             delete p;
         }
     }
-    for (DevBuf* b : {&c->w, &c->start, &c->win, &c->tw, &c->raw, &c->apod, &c->out, &c->mm, &c->frames, &c->num,
-                      &c->den})
+    for (DevBuf* b : {&c->w, &c->start, &c->win, &c->tw, &c->wsh, &c->s0, &c->raw, &c->apod, &c->out, &c->mm, &c->frames, &c->num,
+                      &c->den, &c->plan_table, &c->run_mm, &c->magbuf, &c->dbbuf, &c->planemm, &c->segs, &c->qtable})
         b->release();
+    for (cudaGraphExec_t g : c->graphs)
+        if (g) cudaGraphExecDestroy(g);
     if (c->status_host) cudaFreeHost(c->status_host);
     if (c->own) cudaStreamDestroy(c->own);
     delete c;
@@ -331,6 +361,40 @@ int octgb_set_geometry(octgb_ctx* c, int n, int taps, const int64_t* idx, const 
             (void)len;
             st[i] = s;
         }
+        // shifted dense weights of the spectral kernel: thread t owns outputs
+        // 4t..4t+3; wsh[t][r][u] = weight of source s0_t + u for output 4t + r
+        int len_max = 0;
+        std::vector<int> len(kN, 0);
+        for (int i = 0; i < kN; ++i) {
+            for (int t = 0; t < taps; ++t)
+                if (!(t > 0 && idx[static_cast<size_t>(i) * taps + t] == 0)) len[i] = t + 1;
+        }
+        int U_need = 0;
+        for (int t = 0; t < kThreads; ++t) {
+            const int base = st[4 * t];
+            for (int r = 0; r < 4; ++r) {
+                const int i = 4 * t + r;
+                require(st[i] >= base, "sinc band starts must not decrease");
+                const int reach = st[i] - base + len[i];
+                U_need = U_need > reach ? U_need : reach;
+            }
+        }
+        (void)len_max;
+        int U = U_need <= 16 ? 16 : (U_need <= 20 ? 20 : (U_need <= 24 ? 24 : 0));
+        require(U > 0, "sinc band too wide for the spectral kernel (4 outputs need > 24 source samples)");
+        std::vector<float> wsh(static_cast<size_t>(kThreads) * 4 * U, 0.f);
+        std::vector<int> s0v(kThreads);
+        for (int t = 0; t < kThreads; ++t) {
+            const int base = st[4 * t];
+            s0v[t] = base;
+            for (int r = 0; r < 4; ++r) {
+                const int i = 4 * t + r;
+                for (int k = 0; k < len[i]; ++k) {
+                    const int u = st[i] - base + k;
+                    wsh[(static_cast<size_t>(t) * 4 + r) * U + u] = wt[static_cast<size_t>(k) * kN + i];
+                }
+            }
+        }
         std::vector<float2> win(kN), tw(kN);
         for (int i = 0; i < kN; ++i) {
             // complex64 window (core/spectral.py:219) times 1/N: exact power-of-two scaling
@@ -347,7 +411,14 @@ int octgb_set_geometry(octgb_ctx* c, int n, int taps, const int64_t* idx, const 
         ck(cudaMemcpyAsync(c->start.p, st.data(), kN * sizeof(int), cudaMemcpyHostToDevice, c->stream), "H2D start");
         ck(cudaMemcpyAsync(c->win.p, win.data(), kN * sizeof(float2), cudaMemcpyHostToDevice, c->stream), "H2D win");
         ck(cudaMemcpyAsync(c->tw.p, tw.data(), kN * sizeof(float2), cudaMemcpyHostToDevice, c->stream), "H2D tw");
+        ck(c->wsh.ensure(wsh.size() * sizeof(float)), "cudaMalloc(wsh)");
+        ck(c->s0.ensure(s0v.size() * sizeof(int)), "cudaMalloc(s0)");
+        ck(cudaMemcpyAsync(c->wsh.p, wsh.data(), wsh.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream),
+           "H2D wsh");
+        ck(cudaMemcpyAsync(c->s0.p, s0v.data(), s0v.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream),
+           "H2D s0");
         ck(cudaStreamSynchronize(c->stream), "sync geometry");
+        c->U = U;
         c->taps = taps;
         c->has_geom = true;
     });
@@ -437,8 +508,9 @@ int octgb_quantise(octgb_ctx* c, const float* db, int64_t n, int db_loc, double 
             ck(c->out.ensure(static_cast<size_t>(n) * sizeof(uint16_t)), "cudaMalloc(bits)");
             dst = c->out.as<uint16_t>();
         }
-        ck(launch_quantise(src, n, c1, c2, dst, c->stream), "quantise kernel");
-        c->launches++;
+        ck(c->qtable.ensure(kQuantTable * sizeof(float)), "cudaMalloc(quant table)");
+        ck(launch_quantise(src, n, c1, c2, c->qtable.as<float>(), dst, c->stream), "quantise kernel");
+        c->launches += 2;
         if (bits_loc != OCTGB_DEVICE) {
             copy_out(c, bits, OCTGB_HOST, dst, static_cast<size_t>(n) * sizeof(uint16_t));
             check_status(c);
@@ -511,7 +583,45 @@ int octgb_stitch_plan(octgb_ctx* c, int n_rows, int r0, int r1, int c0, int c1, 
             wx1[cc] = static_cast<float>(WxT[static_cast<size_t>(first + 1) * C + cc]);
         }
         for (int r = 0; r < R; ++r) fzf[r] = static_cast<float>(fz[r]);
+        // per 32 x 32 output block: the input rows / A-scans it reads (patch extents)
+        const int nzb = (n_out_z + kBlk - 1) / kBlk;
+        std::vector<int2> zb(nzb, make_int2(-1, -1));
+        int rs_max = 1, xs_max = 1;
+        for (int b = 0; b < nzb; ++b) {
+            int lo = 1 << 30, hi = -1;
+            for (int zo = b * kBlk; zo < n_out_z && zo < (b + 1) * kBlk; ++zo) {
+                if (zr[zo] < 0) continue;
+                lo = lo < zr[zo] ? lo : zr[zo];
+                const int h = zr[zo] + 1 < R ? zr[zo] + 1 : R - 1;
+                hi = hi > h ? hi : h;
+            }
+            if (hi >= 0) {
+                zb[b] = make_int2(lo, hi);
+                rs_max = rs_max > hi - lo + 1 ? rs_max : hi - lo + 1;
+            }
+        }
+        const int cbf = c0 / kBlk, cbl = (c0 + C - 1) / kBlk;
+        std::vector<int2> cbt(cbl - cbf + 1, make_int2(-1, -1));
+        for (int b = cbf; b <= cbl; ++b) {
+            int lo = 1 << 30, hi = -1;
+            for (int cabs = b * kBlk; cabs < (b + 1) * kBlk; ++cabs) {
+                const int cc = cabs - c0;
+                if (cc < 0 || cc >= C || xr[cc] < 0) continue;
+                lo = lo < xr[cc] ? lo : xr[cc];
+                hi = hi > xr[cc] + 1 ? hi : xr[cc] + 1;
+            }
+            if (hi >= 0) {
+                cbt[b - cbf] = make_int2(lo, hi);
+                xs_max = xs_max > hi - lo + 1 ? xs_max : hi - lo + 1;
+            }
+        }
+        require(static_cast<size_t>(2 * xs_max * rs_max + 2 * xs_max * kBlk) * sizeof(float) <= 160 * 1024,
+                "stitch patch too large (output pixel much coarser than the tile sampling)");
         Plan* p = new Plan();
+        p->cblk_first = cbf;
+        p->n_cblk = cbl - cbf + 1;
+        p->xs_max = xs_max;
+        p->rs_max = rs_max;
         p->n_rows = n_rows;
         p->r0 = r0;
         p->R = R;
@@ -532,6 +642,8 @@ int octgb_stitch_plan(octgb_ctx* c, int n_rows, int r0, int r1, int c0, int c1, 
             up(p->wx0, wx0.data(), wx0.size() * sizeof(float));
             up(p->wx1, wx1.data(), wx1.size() * sizeof(float));
             up(p->fz, fzf.data(), fzf.size() * sizeof(float));
+            up(p->zblk, zb.data(), zb.size() * sizeof(int2));
+            up(p->cblk, cbt.data(), cbt.size() * sizeof(int2));
             if (shift != nullptr) {
                 require(n_y >= 1, "n_y must be >= 1 with optical-path correction");
                 const size_t m = static_cast<size_t>(n_y) * n_tile_x;
@@ -555,6 +667,16 @@ int octgb_stitch_plan(octgb_ctx* c, int n_rows, int r0, int r1, int c0, int c1, 
         }
         c->plans.push_back(p);
         *plan_id = static_cast<int>(c->plans.size() - 1);
+        // refresh the device plan table and the context-wide patch bound
+        std::vector<StitchDev> table;
+        for (Plan* q : c->plans) table.push_back(q->dev());
+        ck(c->plan_table.ensure(table.size() * sizeof(StitchDev)), "cudaMalloc(plan table)");
+        ck(cudaMemcpyAsync(c->plan_table.p, table.data(), table.size() * sizeof(StitchDev), cudaMemcpyHostToDevice,
+                           c->stream),
+           "H2D plan table");
+        ck(cudaStreamSynchronize(c->stream), "sync plan table");
+        c->xs_max = c->xs_max > xs_max ? c->xs_max : xs_max;
+        c->rs_max = c->rs_max > rs_max ? c->rs_max : rs_max;
     });
 }
 
@@ -585,23 +707,28 @@ int octgb_row_add_batch(octgb_ctx* c, int plan_id, const void* raw, int dtype, i
         require(frame_offset >= 0 && frame_offset + B <= c->row_nf, "frames outside the row");
         require(frame_idx != nullptr, "frame_idx is NULL");
         std::vector<int> fy(B > 0 ? B : 1);
+        bool contiguous = true;
         for (int f = 0; f < B; ++f) {
             require(!p.opc || (frame_idx[f] >= 0 && frame_idx[f] < p.n_y), "frame index outside the scan");
             fy[f] = static_cast<int>(frame_idx[f]);
+            contiguous = contiguous && frame_idx[f] == frame_idx[0] + f;
         }
         if (B == 0) return;
         const size_t mb = static_cast<size_t>(B) * p.n_tile_x * kHalf * sizeof(float);
-        ck(c->out.ensure(mb), "cudaMalloc(mag)");
-        ck(c->frames.ensure(fy.size() * sizeof(int)), "cudaMalloc(frames)");
-        ck(cudaMemcpyAsync(c->frames.p, fy.data(), fy.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream),
-           "H2D frames");
-        run_spectral(c, raw, dtype, loc, B, interf, apod, kModeMag, c->out.as<float>(), 0, 0, nullptr);
-        ck(launch_stitch(p.dev(), c->out.as<float>(), c->frames.as<int>(), B, c->num.as<float>(), c->den.as<float>(),
-                         frame_offset, c->row_nx, c->stream),
+        ck(c->magbuf.ensure(mb), "cudaMalloc(mag)");
+        const int* fdev = nullptr;
+        if (!contiguous) {
+            // pageable copy: returns once staged, so `fy` may go out of scope
+            ck(c->frames.ensure(fy.size() * sizeof(int)), "cudaMalloc(frames)");
+            ck(cudaMemcpyAsync(c->frames.p, fy.data(), fy.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream),
+               "H2D frames");
+            fdev = c->frames.as<int>();
+        }
+        run_spectral(c, raw, dtype, loc, B, interf, apod, kModeMag, c->magbuf.as<float>(), 0, 0, nullptr);
+        ck(launch_stitch(p.dev(), c->magbuf.as<float>(), fdev, fy[0], B, c->num.as<float>(), c->den.as<float>(),
+                         frame_offset, c->row_nx, p.xs_max, p.rs_max, c->stream),
            "stitch kernel");
         c->launches++;
-        // cudaMemcpyAsync from pageable memory returns once the frame list is
-        // staged, so `fy` may go out of scope without a stream sync here
     });
 }
 
@@ -645,6 +772,150 @@ int octgb_row_finalise(octgb_ctx* c, float thr, float* db, int db_loc, double* p
             check_status(c);
         }
         c->row_open = false;
+    });
+}
+
+
+int octgb_frames_process(octgb_ctx* c, int n_tiles, const int* plan_ids, const void* const* raws, int dtype, int loc,
+                         int B, int interf, int apod, int f0, int n_out_z, int n_out_x, float thr, float* db,
+                         int db_loc, double* plane_minmax) {
+    return guarded(c, [&] {
+        if (!c->has_geom) throw Error(OCTGB_ERR_STATE, "octgb_set_geometry has not been called");
+        if (c->cancel.load()) throw Error(OCTGB_ERR_CANCELLED, "cancelled");
+        require(n_tiles >= 1 && n_tiles <= kMaxSeg, "n_tiles must be in [1, 32]");
+        require(plan_ids && raws && db, "NULL argument");
+        require(n_out_z >= 1 && n_out_x >= 1, "bad output shape");
+        require(!(db_loc == OCTGB_HOST && c->capturing), "host output during graph capture");
+        TileList tl{};
+        tl.n = n_tiles;
+        bool any_opc = false;
+        for (int t = 0; t < n_tiles; ++t) {
+            require(plan_ids[t] >= 0 && plan_ids[t] < static_cast<int>(c->plans.size()), "bad plan id");
+            const Plan& p = *c->plans[plan_ids[t]];
+            any_opc = any_opc || p.opc;
+            require(p.n_tile_x == interf - apod, "A-scans per B-scan differ from a plan's tile width");
+            require(p.n_out_z == n_out_z && p.c0 + p.C <= n_out_x, "a plan does not fit the output grid");
+            require(!p.opc || (f0 >= 0 && f0 + B <= p.n_y), "frames outside the scan");
+            validate_raw(raws[t], dtype, loc, B, interf, apod);
+            tl.id[t] = plan_ids[t];
+        }
+        if (B == 0) return;
+        const size_t tile_bytes = static_cast<size_t>(B) * interf * kN * raw_elem(dtype);
+        const void* segs[kMaxSeg];
+        if (loc == OCTGB_HOST) {
+            require(!c->capturing, "host input during graph capture");
+            ck(c->raw.ensure(tile_bytes * n_tiles), "cudaMalloc(raw)");
+            for (int t = 0; t < n_tiles; ++t) {
+                void* dst = static_cast<char*>(c->raw.p) + t * tile_bytes;
+                ck(cudaMemcpyAsync(dst, raws[t], tile_bytes, cudaMemcpyHostToDevice, c->stream), "H2D raw");
+                segs[t] = dst;
+            }
+        } else {
+            for (int t = 0; t < n_tiles; ++t) segs[t] = raws[t];
+        }
+        const int nx = interf - apod;
+        const int64_t tile_stride = static_cast<int64_t>(B) * nx * kHalf;
+        ck(c->magbuf.ensure(static_cast<size_t>(tile_stride) * n_tiles * sizeof(float)), "cudaMalloc(mag)");
+        launch_spectral_segs(c, segs, n_tiles, dtype, B, interf, apod, kModeMag, c->magbuf.as<float>(), 0, 0, nullptr);
+        const size_t db_bytes = static_cast<size_t>(B) * n_out_z * n_out_x * sizeof(float);
+        float* dst = db;
+        if (db_loc != OCTGB_DEVICE) {
+            ck(c->dbbuf.ensure(db_bytes), "cudaMalloc(db)");
+            dst = c->dbbuf.as<float>();
+        }
+        unsigned int* pmm = nullptr;
+        if (plane_minmax) {
+            require(!c->capturing, "per-plane clims are read on the host: not during graph capture");
+            ck(c->planemm.ensure(static_cast<size_t>(2 * B) * sizeof(unsigned int)), "cudaMalloc(plane mm)");
+            pmm = c->planemm.as<unsigned int>();
+            ck(launch_minmax_init(pmm, 2 * B, c->stream), "minmax init");
+            c->launches++;
+        }
+        ck(c->run_mm.ensure(2 * sizeof(unsigned int)), "cudaMalloc(run mm)");
+        ck(launch_stitch_frames(c->plan_table.as<StitchDev>(), tl, c->magbuf.as<float>(), tile_stride, B, nx, f0,
+                                n_out_z, n_out_x, thr, dst, pmm, c->run_mm.as<unsigned int>(), c->xs_max, c->rs_max,
+                                any_opc, c->stream),
+           "stitch frames kernel");
+        c->launches++;
+        if (db_loc != OCTGB_DEVICE) copy_out(c, db, OCTGB_HOST, dst, db_bytes);
+        if (plane_minmax) {
+            std::vector<unsigned int> h(2 * static_cast<size_t>(B));
+            ck(cudaMemcpyAsync(h.data(), pmm, h.size() * sizeof(unsigned int), cudaMemcpyDeviceToHost, c->stream),
+               "D2H plane minmax");
+            check_status(c);
+            for (int f = 0; f < B; ++f) {
+                const bool none = h[2 * f] == 0xffffffffu;
+                plane_minmax[2 * f] = none ? NAN : ord2f(h[2 * f]);
+                plane_minmax[2 * f + 1] = none ? NAN : ord2f(h[2 * f + 1]);
+            }
+        } else if (db_loc != OCTGB_DEVICE || loc != OCTGB_DEVICE) {
+            check_status(c);
+        }
+    });
+}
+
+int octgb_clim_reset(octgb_ctx* c) {
+    return guarded(c, [&] {
+        ck(c->run_mm.ensure(2 * sizeof(unsigned int)), "cudaMalloc(run mm)");
+        ck(launch_minmax_init(c->run_mm.as<unsigned int>(), 2, c->stream), "minmax init");
+        c->launches++;
+    });
+}
+
+int octgb_clim_get(octgb_ctx* c, double* clim) {
+    return guarded(c, [&] {
+        require(clim != nullptr, "clim is NULL");
+        ck(c->run_mm.ensure(2 * sizeof(unsigned int)), "cudaMalloc(run mm)");
+        read_minmax(c, c->run_mm.as<unsigned int>(), clim);
+    });
+}
+
+int octgb_quantise_running(octgb_ctx* c, const float* db, int64_t n, int db_loc, uint16_t* bits, int bits_loc) {
+    return guarded(c, [&] {
+        require(n >= 0 && db && bits, "bad argument");
+        require(db_loc == OCTGB_DEVICE && bits_loc == OCTGB_DEVICE, "octgb_quantise_running takes device arrays");
+        ck(c->run_mm.ensure(2 * sizeof(unsigned int)), "cudaMalloc(run mm)");
+        ck(c->qtable.ensure(kQuantTable * sizeof(float)), "cudaMalloc(quant table)");
+        ck(launch_quantise_dev(db, n, c->run_mm.as<unsigned int>(), c->qtable.as<float>(), bits, c->stream),
+           "quantise kernel");
+        c->launches += 2;
+    });
+}
+
+int octgb_graph_begin(octgb_ctx* c) {
+    return guarded(c, [&] {
+        if (c->capturing) throw Error(OCTGB_ERR_STATE, "already capturing");
+        ck(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed), "cudaStreamBeginCapture");
+        c->capturing = true;
+        c->capture_launch0 = c->launches.load();
+    });
+}
+
+int octgb_graph_end(octgb_ctx* c, int* graph_id) {
+    return guarded(c, [&] {
+        if (!c->capturing) throw Error(OCTGB_ERR_STATE, "not capturing");
+        require(graph_id != nullptr, "graph_id is NULL");
+        c->capturing = false;
+        cudaGraph_t g = nullptr;
+        ck(cudaStreamEndCapture(c->stream, &g), "cudaStreamEndCapture");
+        cudaGraphExec_t ge = nullptr;
+        const cudaError_t e = cudaGraphInstantiate(&ge, g, 0);
+        cudaGraphDestroy(g);
+        ck(e, "cudaGraphInstantiate");
+        c->graphs.push_back(ge);
+        c->graph_kernels.push_back(c->launches.load() - c->capture_launch0);
+        c->launches.store(c->capture_launch0);
+        *graph_id = static_cast<int>(c->graphs.size() - 1);
+    });
+}
+
+int octgb_graph_launch(octgb_ctx* c, int graph_id) {
+    return guarded(c, [&] {
+        require(graph_id >= 0 && graph_id < static_cast<int>(c->graphs.size()) && c->graphs[graph_id],
+                "bad graph id");
+        if (c->cancel.load()) throw Error(OCTGB_ERR_CANCELLED, "cancelled");
+        ck(cudaGraphLaunch(c->graphs[graph_id], c->stream), "cudaGraphLaunch");
+        c->launches += c->graph_kernels[graph_id];
     });
 }
 

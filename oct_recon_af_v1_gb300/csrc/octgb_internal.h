@@ -11,7 +11,7 @@ constexpr int kHalf = kN / 2;     // depth bins kept (core/spectral.py:153, nz =
 constexpr int kMaxTaps = 32;      // sinc taps supported
 constexpr int kTail = 32;         // zero tail after each line so padded taps stay in bounds
 constexpr int kGroup = 128;       // threads per A-scan in the FFT (16 points each)
-constexpr int kPerCta = 2;        // A-scans per CTA iteration
+constexpr int kPerCta = 4;        // A-scans per CTA iteration
 constexpr int kThreads = kGroup * kPerCta;
 
 // device-side status word values
@@ -20,19 +20,27 @@ constexpr int kStatusTimeout = 1;
 
 enum OutMode : int { kModeSpec = 0, kModeMag = 1, kModeDb = 2 };
 
+constexpr int kBlk = 32;          // output rows / columns per stitch block
+constexpr int kMaxSeg = 32;       // tiles per multi-tile launch
+
 struct DevGeometry {
     const float* w;       // [taps][kN] sinc weights, tap-major, float32
     const int* start;     // [kN] first source sample of each output sample
     int taps;
+    const float* wsh;     // [kThreads][4][U] shifted weights of outputs 4t..4t+3
+    const int* s0;        // [kThreads] source window base of thread t
+    int U;                // window width (16, 20 or 24)
     const float2* win;    // [kN] complex64 window scaled by 1/kN (ifft normalisation)
     const float2* tw;     // [kN] exp(+2*pi*i*k/kN), rounded from float64
 };
 
 struct SpectralArgs {
-    const void* raw;          // (B, interf, kN)
+    const void* raw;          // (B, interf, kN), segment 0
+    const void* seg[kMaxSeg]; // raw batches of n_seg tiles, each (B, interf, kN); seg[0] == raw
+    int n_seg;
     int B, interf, apod, nx;  // nx = interf - apod
-    int64_t n_ascans;         // B * nx
-    const float* apod_mean;   // (B, kN) float32 apodisation mean
+    int64_t n_ascans;         // n_seg * B * nx
+    const float* apod_mean;   // (n_seg * B, kN) float32 apodisation mean
     DevGeometry g;
     float* out;               // spec (M, kN, 2) | mag (M, kHalf) | db (M, nz)
     int z0, nz;               // depth crop (db mode)
@@ -41,8 +49,7 @@ struct SpectralArgs {
 };
 
 // spectral.cu
-cudaError_t launch_apod_mean(const void* raw, int dtype, int B, int interf, int apod, float* apod_mean,
-                             cudaStream_t st);
+cudaError_t launch_apod_mean(const SpectralArgs& a, int dtype, cudaStream_t st);
 cudaError_t launch_spectral(const SpectralArgs& a, int dtype, int mode, int grid, cudaStream_t st);
 int spectral_max_ctas_per_sm(int dtype, int mode);
 size_t spectral_smem_bytes(int dtype);
@@ -61,14 +68,35 @@ struct StitchDev {
     const int* shift;         // [n_y, n_tile_x] optical-path row shift, or null
     const int* lo;            // [n_y, n_tile_x] smallest valid r (incl.), or null
     const int* hi;            // [n_y, n_tile_x] largest valid r (incl.), or null
+    // per 32-row output block zb: input rows [x, y] (relative to r0) it reads; x = -1: none
+    const int2* zblk;
+    // per absolute 32-column output block cblk_first + i: A-scans [x, y] it reads; x = -1: none
+    const int2* cblk;
+    int cblk_first, n_cblk;
     int r0, R, c0, C, n_out_z, n_tile_x, n_rows;
 };
 
-cudaError_t launch_stitch(const StitchDev& p, const float* mag, const int* frame_y, int B, float* num, float* den,
-                          int frame_offset, int n_out_x, cudaStream_t st);
+struct TileList {
+    int n;
+    int id[kMaxSeg];
+};
+
+// row API: one tile, accumulate into num/den (n_frames, n_out_z, n_out_x)
+cudaError_t launch_stitch(const StitchDev& p, const float* mag, const int* frame_y, int f0, int B, float* num,
+                          float* den, int frame_offset, int n_out_x, int xs_max, int rs_max, cudaStream_t st);
+// frames API: all tiles of a frame batch, num/den kept on chip, dB + clim written
+cudaError_t launch_stitch_frames(const StitchDev* plans_dev, const TileList& tiles, const float* mag,
+                                 int64_t mag_tile_stride, int B, int n_tile_x, int f0, int n_out_z, int n_out_x,
+                                 float thr, float* db, unsigned int* plane_mm, unsigned int* run_mm, int xs_max,
+                                 int rs_max, bool any_opc, cudaStream_t st);
 cudaError_t launch_finalise(const float* num, const float* den, int64_t n_per_plane, int n_planes, float thr,
                             float* db, unsigned int* plane_minmax, cudaStream_t st);
-cudaError_t launch_quantise(const float* db, int64_t n, double c1, double c2, uint16_t* bits, cudaStream_t st);
+// quantisation: `table` is scratch of kQuantTable floats (the code thresholds of the clim)
+constexpr int kQuantTable = 65537;
+cudaError_t launch_quantise(const float* db, int64_t n, double c1, double c2, float* table, uint16_t* bits,
+                            cudaStream_t st);
+cudaError_t launch_quantise_dev(const float* db, int64_t n, const unsigned int* clim_mm, float* table,
+                                uint16_t* bits, cudaStream_t st);
 cudaError_t launch_minmax(const float* x, int64_t n, unsigned int* minmax, cudaStream_t st);
 cudaError_t launch_minmax_init(unsigned int* minmax, int count, cudaStream_t st);
 

@@ -177,29 +177,63 @@ struct RawLoad<float> {
     }
 };
 
+constexpr int kDLine = kN + kTail;                        // d line incl. zero tail
+constexpr int kDSkew = kDLine + kDLine / 32 + 4;           // skewed length (+1 word per 32)
+__device__ __forceinline__ int skew(int w) { return w + (w >> 5); }
+
 template <typename RawT>
 struct Smem {
     uint64_t bar[2];
     float red[kPerCta][4];
     float mval[kPerCta];
     unsigned int mm[2];
-    alignas(128) RawT stage[2][kPerCta][kN];      // bulk-copy destinations (16-byte aligned)
-    alignas(16) float d[kPerCta][kDStride];
-    alignas(16) float2 spec[kPerCta][kSpecStride];
+    alignas(128) RawT stage[2][kPerCta][kN];        // bulk-copy destinations (16-byte aligned)
+    alignas(16) float d[kPerCta][kDSkew];           // background-free line, skewed
+    alignas(16) float2 spec[kPerCta][kSpecStride];  // windowed spectrum / FFT work line
+    alignas(16) float2 tw2[16][16];                 // stage-2 twiddles [r][j mod 16]
+    alignas(16) float2 tw3[8][256];                 // stage-3 twiddles [r][j]
 };
 
-template <typename RawT, int Mode>
-__global__ void __launch_bounds__(kThreads) k_spectral(const SpectralArgs a) {
+__device__ __forceinline__ void group_sync(int g) {
+    asm volatile("bar.sync %0, %1;" ::"r"(1 + g), "r"(kGroup) : "memory");
+}
+
+// One CTA (512 threads) = 4 A-scans per iteration of a persistent loop.
+// Sinc: thread t owns output samples 4t..4t+3 of all four A-scans; its band
+// weights live in registers for the whole kernel in a shifted dense form
+// wr[r][u] (the weight of source sample s0_t + u for output 4t + r, zero
+// outside the band), so each A-scan costs U conflict-free shared loads of the
+// source window (d is stored skewed by one word per 32) and 4*U FMAs, summed
+// in the reference's tap order.  FFT: 128 threads per A-scan, radix 16,16,8
+// Stockham through the padded spec line, per-group named barriers.
+template <typename RawT, int Mode, int U>
+__global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     Smem<RawT>& S = *reinterpret_cast<Smem<RawT>*>(smem_raw);
 
     const int tid = threadIdx.x;
-    const int g = tid / kGroup;        // A-scan slot in the pair
+    const int g = tid / kGroup;        // A-scan slot of the iteration
     const int lt = tid % kGroup;       // thread within the A-scan group
     const int warp = tid / 32, lane = tid % 32;
     const int64_t M = a.n_ascans;
-    const int64_t npairs = (M + kPerCta - 1) / kPerCta;
-    const int taps = a.g.taps;
+    const int64_t nquads = (M + kPerCta - 1) / kPerCta;
+
+    // this thread's shifted sinc weights and source window base
+    float wr[4][U];
+    {
+        const float4* wp = reinterpret_cast<const float4*>(a.g.wsh + static_cast<int64_t>(tid) * 4 * U);
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+#pragma unroll
+            for (int q = 0; q < U / 4; ++q) {
+                const float4 v = __ldg(wp + r * (U / 4) + q);
+                wr[r][4 * q] = v.x;
+                wr[r][4 * q + 1] = v.y;
+                wr[r][4 * q + 2] = v.z;
+                wr[r][4 * q + 3] = v.w;
+            }
+    }
+    const int s0 = __ldg(a.g.s0 + tid);
 
     if (tid == 0) {
         mbar_init(&S.bar[0], 1);
@@ -208,47 +242,51 @@ __global__ void __launch_bounds__(kThreads) k_spectral(const SpectralArgs a) {
         S.mm[0] = 0xffffffffu;
         S.mm[1] = 0u;
     }
-    for (int k = tid; k < kPerCta * kTail; k += kThreads) S.d[k / kTail][kN + k % kTail] = 0.f;
-
-    // per-thread sinc band starts of its 8 output samples (i = tid + 256 r)
-    int st[8];
-#pragma unroll
-    for (int r = 0; r < 8; ++r) st[r] = __ldg(a.g.start + tid + kThreads * r);
-
+    for (int k = tid; k < kPerCta * kTail; k += kThreads) S.d[k / kTail][skew(kN + k % kTail)] = 0.f;
+    for (int k = tid; k < 16 * 16; k += kThreads) {
+        const int r = k / 16, j = k % 16;
+        S.tw2[r][j] = __ldg(a.g.tw + (r * j * (kN / 256)) % kN);
+    }
+    for (int k = tid; k < 8 * 256; k += kThreads) {
+        const int r = k / 256, j = k % 256;
+        S.tw3[r][j] = __ldg(a.g.tw + (r * j) % kN);
+    }
     float run_min = __int_as_float(0x7f800000), run_max = -__int_as_float(0x7f800000);
     __syncthreads();
 
-    auto issue = [&](int64_t pair, int buf) {
-        uint32_t bytes = 0;
-        int64_t a0 = pair * kPerCta;
-        int nvalid = static_cast<int>(M - a0 < kPerCta ? M - a0 : kPerCta);
-        bytes = static_cast<uint32_t>(nvalid) * kN * sizeof(RawT);
-        mbar_expect_tx(&S.bar[buf], bytes);
+    auto issue = [&](int64_t quad, int buf) {
+        const int64_t a0 = quad * kPerCta;
+        const int nvalid = static_cast<int>(M - a0 < kPerCta ? M - a0 : kPerCta);
+        mbar_expect_tx(&S.bar[buf], static_cast<uint32_t>(nvalid) * kN * sizeof(RawT));
         for (int s = 0; s < nvalid; ++s) {
             const int64_t as = a0 + s;
-            const int64_t b = as / a.nx, x = as - b * a.nx;
-            const RawT* src = static_cast<const RawT*>(a.raw) + ((b * a.interf + a.apod + x) * kN);
+            const int64_t bt = as / a.nx, x = as - bt * a.nx;   // bt = segment * B + b
+            const int sg = static_cast<int>(bt / a.B);
+            const int64_t b = bt - static_cast<int64_t>(sg) * a.B;
+            const RawT* src = static_cast<const RawT*>(a.seg[sg]) + ((b * a.interf + a.apod + x) * kN);
             tma_bulk_g2s(&S.stage[buf][s][0], src, kN * sizeof(RawT), &S.bar[buf]);
         }
     };
 
-    if (tid == 0 && blockIdx.x < npairs) issue(blockIdx.x, 0);
+    if (tid == 0 && blockIdx.x < nquads) issue(blockIdx.x, 0);
 
     int it = 0;
-    for (int64_t pair = blockIdx.x; pair < npairs; pair += gridDim.x, ++it) {
+    for (int64_t quad = blockIdx.x; quad < nquads; quad += gridDim.x, ++it) {
         const int buf = it & 1;
-        const int64_t next = pair + gridDim.x;
-        if (tid == 0 && next < npairs) issue(next, buf ^ 1);
+        const int64_t next = quad + gridDim.x;
+        if (tid == 0 && next < nquads) issue(next, buf ^ 1);
 
         const bool ok = mbar_wait_bounded(&S.bar[buf], (it >> 1) & 1, a.status);
         if (__syncthreads_or(!ok)) return;
 
-        // ---- (b) background: d = raw - apod, line mean ----
-        const int64_t as = pair * kPerCta + g;
+        // ---- (b) background: d = raw - apod, line mean (group g, A-scan g) ----
+        const int64_t as = quad * kPerCta + g;
         const bool valid = as < M;
         const int64_t bsc = valid ? as / a.nx : 0;
         const float* apod = a.apod_mean + bsc * kN;
-        float dv[16];
+        // d = raw - apod goes to shared memory now; the line mean m is
+        // subtracted when the sinc loads its window (the same float32 value
+        // d - m the reference stores, cpu_kernels.py:35-36)
         float sum = 0.f;
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
@@ -256,65 +294,53 @@ __global__ void __launch_bounds__(kThreads) k_spectral(const SpectralArgs a) {
             float rv[4];
             RawLoad<RawT>::load4(&S.stage[buf][g][j], rv);
             const float4 ap = __ldg(reinterpret_cast<const float4*>(apod + j));
-            dv[4 * q + 0] = rv[0] - ap.x;
-            dv[4 * q + 1] = rv[1] - ap.y;
-            dv[4 * q + 2] = rv[2] - ap.z;
-            dv[4 * q + 3] = rv[3] - ap.w;
-            sum += (dv[4 * q + 0] + dv[4 * q + 1]) + (dv[4 * q + 2] + dv[4 * q + 3]);
+            const float d0 = rv[0] - ap.x, d1 = rv[1] - ap.y, d2 = rv[2] - ap.z, d3 = rv[3] - ap.w;
+            S.d[g][skew(j)] = d0;
+            S.d[g][skew(j + 1)] = d1;
+            S.d[g][skew(j + 2)] = d2;
+            S.d[g][skew(j + 3)] = d3;
+            sum += (d0 + d1) + (d2 + d3);
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
         if (lane == 0) S.red[g][warp & 3] = sum;
-        __syncthreads();
-        const float m = ((S.red[g][0] + S.red[g][1]) + (S.red[g][2] + S.red[g][3])) * (1.0f / kN);
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const int j = 4 * lt + 512 * q;
-            *reinterpret_cast<float4*>(&S.d[g][j]) =
-                make_float4(dv[4 * q] - m, dv[4 * q + 1] - m, dv[4 * q + 2] - m, dv[4 * q + 3] - m);
-        }
-        if (lt == 0) S.mval[g] = m;
+        group_sync(g);
+        if (lt == 0) S.mval[g] = ((S.red[g][0] + S.red[g][1]) + (S.red[g][2] + S.red[g][3])) * (1.0f / kN);
         __syncthreads();
 
-        // ---- (c)+(d) sinc k-linearisation and window, both A-scans ----
+        // ---- (c)+(d) sinc k-linearisation and window, four A-scans ----
         {
-            float acc0[8], acc1[8];
+            const int i0 = 4 * tid;
+            const float4 wa = __ldg(reinterpret_cast<const float4*>(a.g.win + i0));
+            const float4 wb = __ldg(reinterpret_cast<const float4*>(a.g.win + i0 + 2));
+            const float wre[4] = {wa.x, wa.z, wb.x, wb.z}, wim[4] = {wa.y, wa.w, wb.y, wb.w};
+            const int64_t a0 = quad * kPerCta;
+#pragma unroll 1
+            for (int k = 0; k < kPerCta; ++k) {
+                const float mk = S.mval[k];
+                float win[U];
 #pragma unroll
-            for (int r = 0; r < 8; ++r) acc0[r] = acc1[r] = 0.f;
-            for (int k = 0; k < taps; ++k) {
-                const float* wk = a.g.w + static_cast<int64_t>(k) * kN + tid;
+                for (int u = 0; u < U; ++u) win[u] = S.d[k][skew(s0 + u)] - mk;
 #pragma unroll
-                for (int r = 0; r < 8; ++r) {
-                    const float wv = __ldg(wk + kThreads * r);
-                    acc0[r] = fmaf(wv, S.d[0][st[r] + k], acc0[r]);
-                    acc1[r] = fmaf(wv, S.d[1][st[r] + k], acc1[r]);
+                for (int r = 0; r < 4; ++r) {
+                    float acc = 0.f;
+#pragma unroll
+                    for (int u = 0; u < U; ++u) acc = fmaf(wr[r][u], win[u], acc);
+                    const float v = acc + mk;
+                    const float2 sp = make_float2(v * wre[r], v * wim[r]);
+                    if (Mode == kModeSpec) {
+                        // spec output undoes the 1/N ifft scaling folded into the window
+                        if (a0 + k < M)
+                            reinterpret_cast<float2*>(a.out)[(a0 + k) * kN + i0 + r] =
+                                make_float2(sp.x * kN, sp.y * kN);
+                    } else {
+                        S.spec[k][pad(i0 + r)] = sp;
+                    }
                 }
             }
-            const float m0 = S.mval[0], m1 = S.mval[1];
-            const int64_t a0 = pair * kPerCta;
-#pragma unroll
-            for (int r = 0; r < 8; ++r) {
-                const int i = tid + kThreads * r;
-                const float2 w = __ldg(a.g.win + i);
-                const float v0 = acc0[r] + m0, v1 = acc1[r] + m1;
-                const float2 s0 = make_float2(v0 * w.x, v0 * w.y);
-                const float2 s1 = make_float2(v1 * w.x, v1 * w.y);
-                if (Mode == kModeSpec) {
-                    // spec output undoes the 1/N ifft scaling folded into the window
-                    float2* o = reinterpret_cast<float2*>(a.out);
-                    if (a0 < M) o[a0 * kN + i] = make_float2(s0.x * kN, s0.y * kN);
-                    if (a0 + 1 < M) o[(a0 + 1) * kN + i] = make_float2(s1.x * kN, s1.y * kN);
-                } else {
-                    S.spec[0][pad(i)] = s0;
-                    S.spec[1][pad(i)] = s1;
-                }
-            }
-        }
-        if (Mode == kModeSpec) {
-            __syncthreads();
-            continue;
         }
         __syncthreads();
+        if (Mode == kModeSpec) continue;
 
         // ---- (e) inverse FFT, group g on its own line ----
         float2* X = S.spec[g];
@@ -323,10 +349,10 @@ __global__ void __launch_bounds__(kThreads) k_spectral(const SpectralArgs a) {
 #pragma unroll
             for (int r = 0; r < 16; ++r) v[r] = X[pad(lt + 128 * r)];
             dft16(v);
-            __syncthreads();
+            group_sync(g);
 #pragma unroll
             for (int r = 0; r < 16; ++r) X[pad(16 * lt + r)] = v[r];
-            __syncthreads();
+            group_sync(g);
         }
         {
             float2 v[16];
@@ -334,13 +360,13 @@ __global__ void __launch_bounds__(kThreads) k_spectral(const SpectralArgs a) {
 #pragma unroll
             for (int r = 0; r < 16; ++r) v[r] = X[pad(lt + 128 * r)];
 #pragma unroll
-            for (int r = 1; r < 16; ++r) v[r] = cmul(v[r], __ldg(a.g.tw + r * jm * (kN / 256)));
+            for (int r = 1; r < 16; ++r) v[r] = cmul(v[r], S.tw2[r][jm]);
             dft16(v);
-            __syncthreads();
+            group_sync(g);
             const int idxD = (lt >> 4) * 256 + jm;
 #pragma unroll
             for (int r = 0; r < 16; ++r) X[pad(idxD + 16 * r)] = v[r];
-            __syncthreads();
+            group_sync(g);
         }
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
@@ -349,7 +375,7 @@ __global__ void __launch_bounds__(kThreads) k_spectral(const SpectralArgs a) {
 #pragma unroll
             for (int r = 0; r < 8; ++r) v[r] = X[pad(j + 256 * r)];
 #pragma unroll
-            for (int r = 1; r < 8; ++r) v[r] = cmul(v[r], __ldg(a.g.tw + r * j));
+            for (int r = 1; r < 8; ++r) v[r] = cmul(v[r], S.tw3[r][j]);
             float2 Xk[4];
             dft8_low(v, Xk);
             if (valid) {
@@ -373,7 +399,6 @@ __global__ void __launch_bounds__(kThreads) k_spectral(const SpectralArgs a) {
                 }
             }
         }
-        __syncthreads();
     }
 
     if (Mode == kModeDb && a.minmax != nullptr) {
@@ -382,6 +407,7 @@ __global__ void __launch_bounds__(kThreads) k_spectral(const SpectralArgs a) {
             run_min = fminf(run_min, __shfl_xor_sync(0xffffffffu, run_min, o));
             run_max = fmaxf(run_max, __shfl_xor_sync(0xffffffffu, run_max, o));
         }
+        __syncthreads();
         if (lane == 0 && run_min <= run_max) {
             atomicMin(&S.mm[0], f2ord(run_min));
             atomicMax(&S.mm[1], f2ord(run_max));
@@ -396,11 +422,13 @@ __global__ void __launch_bounds__(kThreads) k_spectral(const SpectralArgs a) {
 
 // apodisation mean (cpu_kernels.py:20-25): exact sum, divided in float64, stored float32
 template <typename RawT>
-__global__ void k_apod_mean(const RawT* __restrict__ raw, int B, int interf, int apod, float* __restrict__ out) {
-    const int b = blockIdx.y;
+__global__ void k_apod_mean(const SpectralArgs a, float* __restrict__ out) {
+    const int bt = blockIdx.y;                  // segment * B + b
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= B || j >= kN) return;
-    const RawT* p = raw + static_cast<int64_t>(b) * interf * kN + j;
+    const int sg = bt / a.B, b = bt - sg * a.B;
+    const int interf = a.interf, apod = a.apod;
+    if (sg >= a.n_seg || j >= kN) return;
+    const RawT* p = static_cast<const RawT*>(a.seg[sg]) + static_cast<int64_t>(b) * interf * kN + j;
     double s;
     if (sizeof(RawT) == 2) {
         int acc = 0;
@@ -410,60 +438,49 @@ __global__ void k_apod_mean(const RawT* __restrict__ raw, int B, int interf, int
         s = 0.0;
         for (int k = 0; k < apod; ++k) s += static_cast<double>(p[static_cast<int64_t>(k) * kN]);
     }
-    out[static_cast<int64_t>(b) * kN + j] = static_cast<float>(s / apod);
+    out[static_cast<int64_t>(bt) * kN + j] = static_cast<float>(s / apod);
+}
+
+template <typename RawT, int Mode, int U>
+cudaError_t launch_t(const SpectralArgs& a, int grid, cudaStream_t st) {
+    const size_t smem = sizeof(Smem<RawT>);
+    cudaError_t e = cudaFuncSetAttribute(k_spectral<RawT, Mode, U>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(smem));
+    if (e != cudaSuccess) return e;
+    k_spectral<RawT, Mode, U><<<grid, kThreads, smem, st>>>(a);
+    return cudaGetLastError();
 }
 
 template <typename RawT, int Mode>
-cudaError_t launch_t(const SpectralArgs& a, int grid, cudaStream_t st) {
-    const size_t smem = sizeof(Smem<RawT>);
-    cudaError_t e = cudaFuncSetAttribute(k_spectral<RawT, Mode>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         static_cast<int>(smem));
-    if (e != cudaSuccess) return e;
-    k_spectral<RawT, Mode><<<grid, kThreads, smem, st>>>(a);
-    return cudaGetLastError();
+cudaError_t launch_u(const SpectralArgs& a, int grid, cudaStream_t st) {
+    switch (a.g.U) {
+        case 16: return launch_t<RawT, Mode, 16>(a, grid, st);
+        case 20: return launch_t<RawT, Mode, 20>(a, grid, st);
+        case 24: return launch_t<RawT, Mode, 24>(a, grid, st);
+        default: return cudaErrorInvalidValue;
+    }
 }
 
 template <typename RawT>
 cudaError_t launch_mode(const SpectralArgs& a, int mode, int grid, cudaStream_t st) {
     switch (mode) {
-        case kModeSpec: return launch_t<RawT, kModeSpec>(a, grid, st);
-        case kModeMag: return launch_t<RawT, kModeMag>(a, grid, st);
-        default: return launch_t<RawT, kModeDb>(a, grid, st);
-    }
-}
-
-template <typename RawT, int Mode>
-int occupancy_t() {
-    const size_t smem = sizeof(Smem<RawT>);
-    if (cudaFuncSetAttribute(k_spectral<RawT, Mode>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             static_cast<int>(smem)) != cudaSuccess)
-        return 1;
-    int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_spectral<RawT, Mode>, kThreads, smem) != cudaSuccess)
-        return 1;
-    return n > 0 ? n : 1;
-}
-
-template <typename RawT>
-int occupancy_mode(int mode) {
-    switch (mode) {
-        case kModeSpec: return occupancy_t<RawT, kModeSpec>();
-        case kModeMag: return occupancy_t<RawT, kModeMag>();
-        default: return occupancy_t<RawT, kModeDb>();
+        case kModeSpec: return launch_u<RawT, kModeSpec>(a, grid, st);
+        case kModeMag: return launch_u<RawT, kModeMag>(a, grid, st);
+        default: return launch_u<RawT, kModeDb>(a, grid, st);
     }
 }
 
 }  // namespace
 
-cudaError_t launch_apod_mean(const void* raw, int dtype, int B, int interf, int apod, float* apod_mean,
-                             cudaStream_t st) {
-    const dim3 grid(kN / 256, B);
+cudaError_t launch_apod_mean(const SpectralArgs& a, int dtype, cudaStream_t st) {
+    const dim3 grid(kN / 256, a.n_seg * a.B);
+    float* out = const_cast<float*>(a.apod_mean);
     if (dtype == 0)
-        k_apod_mean<uint16_t><<<grid, 256, 0, st>>>(static_cast<const uint16_t*>(raw), B, interf, apod, apod_mean);
+        k_apod_mean<uint16_t><<<grid, 256, 0, st>>>(a, out);
     else if (dtype == 1)
-        k_apod_mean<int16_t><<<grid, 256, 0, st>>>(static_cast<const int16_t*>(raw), B, interf, apod, apod_mean);
+        k_apod_mean<int16_t><<<grid, 256, 0, st>>>(a, out);
     else
-        k_apod_mean<float><<<grid, 256, 0, st>>>(static_cast<const float*>(raw), B, interf, apod, apod_mean);
+        k_apod_mean<float><<<grid, 256, 0, st>>>(a, out);
     return cudaGetLastError();
 }
 
@@ -474,9 +491,9 @@ cudaError_t launch_spectral(const SpectralArgs& a, int dtype, int mode, int grid
 }
 
 int spectral_max_ctas_per_sm(int dtype, int mode) {
-    if (dtype == 0) return occupancy_mode<uint16_t>(mode);
-    if (dtype == 1) return occupancy_mode<int16_t>(mode);
-    return occupancy_mode<float>(mode);
+    (void)dtype;
+    (void)mode;
+    return 1;   // 512 threads, ~155 KB shared memory, 128 registers: one CTA per SM
 }
 
 size_t spectral_smem_bytes(int dtype) {

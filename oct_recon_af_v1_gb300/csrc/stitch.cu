@@ -5,12 +5,26 @@
 // one tile and one batch of B-scans,
 //   a[f,x,r]  = mag[f, x, clip(r0 + r + shift)]   (optical-path gather)
 //   F[f,x,r]  = valid * fz[r]
-//   num[f0+f, zo, c0+c] += sum_x WxT[x,c] sum_r Wz[zo,r] a F
-//   den[f0+f, zo, c0+c] += sum_x WxT[x,c] sum_r Wz[zo,r] F
+//   num[f, zo, c0+c] += sum_x WxT[x,c] sum_r Wz[zo,r] a F
+//   den[f, zo, c0+c] += sum_x WxT[x,c] sum_r Wz[zo,r] F
 // Wz / WxT are linear-interpolation operators with at most two adjacent
-// non-zeros per output row / column, stored compactly.  One thread per output
-// voxel; tiles are added one launch after the other on one stream, so each
-// voxel sums its tile contributions in the same order as the reference loop.
+// non-zeros per output row / column, stored compactly.
+//
+// The work unit is a 32 x 32 block of output voxels (rows zo, columns c) of
+// one frame.  The block reads a small patch of the tile's magnitudes (the
+// A-scans feeding its columns x the depth rows feeding its rows) into shared
+// memory with reads along depth (the magnitude layout), applies the depth
+// interpolation per A-scan, then the lateral interpolation, and writes along
+// x (the output layout): a transpose through shared memory, so both global
+// sides are coalesced.
+//
+// Two kernels use it:
+//   k_stitch_tile    one tile, num/den += contribution (per-tile row API);
+//   k_stitch_frames  every tile of a frame batch in tile order, num/den kept in
+//                    registers, then finalise (threshold -> NaN, 20 log10) and
+//                    the plane / running clim: num/den never reach memory.
+// In both the per-voxel floating-point operations and their order are those of
+// the reference loop (tile contributions added one after the other).
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
@@ -20,58 +34,314 @@
 namespace octgb {
 namespace {
 
-__device__ __forceinline__ float gather(const float* __restrict__ mag_ax, const StitchDev& p, int fy, int x, int r,
-                                        float& F) {
-    // r: row relative to r0
-    int src = p.r0 + r;
-    bool ok = true;
-    if (p.shift != nullptr) {
-        const int64_t o = static_cast<int64_t>(fy) * p.n_tile_x + x;
-        const int rr = p.r0 + r;
-        ok = rr >= p.lo[o] && rr <= p.hi[o];
-        src = rr + p.shift[o];
-        src = src < 0 ? 0 : (src > p.n_rows - 1 ? p.n_rows - 1 : src);
-    }
-    F = ok ? p.fz[r] : 0.f;
-    return mag_ax[static_cast<int64_t>(x) * kHalf + src] * F;
+constexpr int kStThreads = 256;          // 32 columns x 8 row groups
+constexpr int kRowsPerThread = kBlk / 8; // 4 output rows per thread
+
+struct PatchSmem {
+    float* pa;   // [xs_max][rs_max] a * F
+    float* pf;   // [xs_max][rs_max] F
+    float* un;   // [xs_max][kBlk]   depth-interpolated a F
+    float* ud;   // [xs_max][kBlk]   depth-interpolated F
+};
+
+__device__ __forceinline__ PatchSmem carve(float* sm, int xs_max, int rs_max) {
+    PatchSmem s;
+    s.pa = sm;
+    s.pf = s.pa + xs_max * rs_max;
+    s.un = s.pf + xs_max * rs_max;
+    s.ud = s.un + xs_max * kBlk;
+    return s;
 }
 
-__global__ void k_stitch(const StitchDev p, const float* __restrict__ mag, const int* __restrict__ frame_y, int B,
-                         float* __restrict__ num, float* __restrict__ den, int frame_offset, int n_out_x) {
-    const int64_t n = static_cast<int64_t>(B) * p.n_out_z * p.C;
-    for (int64_t t = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; t < n;
-         t += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-        const int c = static_cast<int>(t % p.C);
-        const int64_t t2 = t / p.C;
-        const int zo = static_cast<int>(t2 % p.n_out_z);
-        const int f = static_cast<int>(t2 / p.n_out_z);
-        const int zr = p.zr[zo];
-        const int xr = p.xr[c];
-        if (zr < 0 || xr < 0) continue;
-        const float wz0 = p.wz0[zo], wz1 = p.wz1[zo];
-        const float wx0 = p.wx0[c], wx1 = p.wx1[c];
-        const float* mf = mag + static_cast<int64_t>(f) * p.n_tile_x * kHalf;
-        const int fy = frame_y[f];
-        // depth interpolation (Wz) per contributing A-scan, then lateral (WxT)
-        float un[2], ud[2];
-#pragma unroll
-        for (int q = 0; q < 2; ++q) {
-            const int x = xr + q;
-            un[q] = 0.f;
-            ud[q] = 0.f;
-            if (x >= p.n_tile_x || (q == 1 && wx1 == 0.f)) continue;
-            float F0, F1 = 0.f;
-            const float a0 = gather(mf, p, fy, x, zr, F0);
-            float a1 = 0.f;
-            if (wz1 != 0.f) a1 = gather(mf, p, fy, x, zr + 1, F1);
-            un[q] = fmaf(a1, wz1, a0 * wz0);
-            ud[q] = fmaf(F1, wz1, F0 * wz0);
+// Contribution of one tile to the block (zb, cb) of frame f; adds it to
+// an/ad (4 voxels per thread: rows zb + ty + 8q, column cb + tx).  Uniform
+// control flow across the CTA; returns false when the tile misses the block.
+__device__ bool block_contrib(const StitchDev& p, const float* __restrict__ mag_f, int fy, int zb, int cb,
+                              const PatchSmem& s, int rs_max, float (&an)[kRowsPerThread],
+                              float (&ad)[kRowsPerThread]) {
+    const int cbi = cb / kBlk - p.cblk_first;
+    if (cbi < 0 || cbi >= p.n_cblk) return false;
+    const int2 xb = p.cblk[cbi];
+    const int2 zr_b = p.zblk[zb / kBlk];
+    if (xb.x < 0 || zr_b.x < 0) return false;
+    const int x_lo = xb.x, xs = xb.y - xb.x + 1;
+    const int r_lo = zr_b.x, rs = zr_b.y - zr_b.x + 1;
+    const int tid = threadIdx.x;
+
+    // 1. gather the patch: rows fastest (contiguous in the magnitude layout)
+    for (int i = tid; i < xs * rs; i += kStThreads) {
+        const int xx = i / rs, rr = i - xx * rs;
+        const int x = x_lo + xx;
+        const int r = r_lo + rr;
+        const int ra = p.r0 + r;
+        int src = ra;
+        float F = p.fz[r];
+        if (p.shift != nullptr) {
+            const int64_t o = static_cast<int64_t>(fy) * p.n_tile_x + x;
+            if (ra < p.lo[o] || ra > p.hi[o]) F = 0.f;
+            src = ra + p.shift[o];
+            src = src < 0 ? 0 : (src > p.n_rows - 1 ? p.n_rows - 1 : src);
         }
-        const float cn = fmaf(un[1], wx1, un[0] * wx0);
-        const float cd = fmaf(ud[1], wx1, ud[0] * wx0);
-        const int64_t o = (static_cast<int64_t>(frame_offset + f) * p.n_out_z + zo) * n_out_x + p.c0 + c;
-        num[o] += cn;
-        den[o] += cd;
+        s.pa[xx * rs_max + rr] = mag_f[static_cast<int64_t>(x) * kHalf + src] * F;
+        s.pf[xx * rs_max + rr] = F;
+    }
+    __syncthreads();
+
+    // 2. depth interpolation (Wz) for every A-scan of the patch and row of the block
+    for (int i = tid; i < xs * kBlk; i += kStThreads) {
+        const int xx = i / kBlk, z = i - xx * kBlk;
+        const int zo = zb + z;
+        float un = 0.f, ud = 0.f;
+        if (zo < p.n_out_z) {
+            const int zr = p.zr[zo];
+            if (zr >= 0) {
+                const int rr = zr - r_lo;
+                const float w0 = p.wz0[zo], w1 = p.wz1[zo];
+                const float a0 = s.pa[xx * rs_max + rr], f0 = s.pf[xx * rs_max + rr];
+                float a1 = 0.f, f1 = 0.f;
+                if (rr + 1 < rs) {
+                    a1 = s.pa[xx * rs_max + rr + 1];
+                    f1 = s.pf[xx * rs_max + rr + 1];
+                }
+                un = fmaf(a1, w1, a0 * w0);
+                ud = fmaf(f1, w1, f0 * w0);
+            }
+        }
+        s.un[xx * kBlk + z] = un;
+        s.ud[xx * kBlk + z] = ud;
+    }
+    __syncthreads();
+
+    // 3. lateral interpolation (WxT) and accumulation
+    const int tx = tid & (kBlk - 1), ty = tid / kBlk;
+    const int cc = cb + tx - p.c0;
+    if (cc >= 0 && cc < p.C) {
+        const int xr = p.xr[cc];
+        if (xr >= 0) {
+            const int xx = xr - x_lo;
+            const float w0 = p.wx0[cc], w1 = p.wx1[cc];
+#pragma unroll
+            for (int q = 0; q < kRowsPerThread; ++q) {
+                const int z = ty + 8 * q;
+                const int zo = zb + z;
+                if (zo < p.n_out_z && p.zr[zo] >= 0) {
+                    const float u0 = s.un[xx * kBlk + z], d0 = s.ud[xx * kBlk + z];
+                    const float u1 = xx + 1 < xs ? s.un[(xx + 1) * kBlk + z] : 0.f;
+                    const float d1 = xx + 1 < xs ? s.ud[(xx + 1) * kBlk + z] : 0.f;
+                    an[q] += fmaf(u1, w1, u0 * w0);
+                    ad[q] += fmaf(d1, w1, d0 * w0);
+                }
+            }
+        }
+    }
+    __syncthreads();
+    return true;
+}
+
+__global__ void __launch_bounds__(kStThreads) k_stitch_tile(const StitchDev p, const float* __restrict__ mag,
+                                                            const int* __restrict__ frame_y, int f0,
+                                                            float* __restrict__ num, float* __restrict__ den,
+                                                            int frame_offset, int n_out_x, int xs_max, int rs_max) {
+    extern __shared__ __align__(16) float sm[];
+    const PatchSmem s = carve(sm, xs_max, rs_max);
+    const int f = blockIdx.z;
+    const int zb = blockIdx.y * kBlk;
+    const int cb = (p.cblk_first + blockIdx.x) * kBlk;
+    const int fy = frame_y ? frame_y[f] : f0 + f;
+    float an[kRowsPerThread] = {0.f, 0.f, 0.f, 0.f}, ad[kRowsPerThread] = {0.f, 0.f, 0.f, 0.f};
+    const float* mag_f = mag + static_cast<int64_t>(f) * p.n_tile_x * kHalf;
+    if (!block_contrib(p, mag_f, fy, zb, cb, s, rs_max, an, ad)) return;
+    const int tx = threadIdx.x & (kBlk - 1), ty = threadIdx.x / kBlk;
+    const int c = cb + tx;
+    const int cc = c - p.c0;
+    if (cc < 0 || cc >= p.C || p.xr[cc] < 0) return;
+#pragma unroll
+    for (int q = 0; q < kRowsPerThread; ++q) {
+        const int zo = zb + ty + 8 * q;
+        if (zo >= p.n_out_z || p.zr[zo] < 0) continue;
+        const int64_t o = (static_cast<int64_t>(frame_offset + f) * p.n_out_z + zo) * n_out_x + c;
+        num[o] += an[q];
+        den[o] += ad[q];
+    }
+}
+
+__device__ __forceinline__ void warp_minmax(float& mn, float& mx) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+        mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    }
+}
+
+// Frame-batch kernel: one CTA = one frame x 64 output rows x 32 output
+// columns.  All contributing tiles' patches are gathered first (one barrier,
+// many loads in flight), then every voxel sums the tiles in order.
+constexpr int kFZ = 64;                      // output rows per CTA
+constexpr int kFRows = kFZ / 8;              // rows per thread
+
+struct TileSlot {
+    int plan, x_lo, xs, r_lo, rs, off;       // off: float offset of the slot's patch in smem
+};
+
+__global__ void __launch_bounds__(kStThreads) k_stitch_frames(const StitchDev* __restrict__ plans, const TileList tl,
+                                                              const float* __restrict__ mag, int64_t mag_tile_stride,
+                                                              int n_tile_x, int f0, int n_out_z, int n_out_x,
+                                                              float thr, float* __restrict__ db,
+                                                              unsigned int* __restrict__ plane_mm,
+                                                              unsigned int* __restrict__ run_mm) {
+    extern __shared__ __align__(16) float sm[];
+    __shared__ TileSlot slot[kMaxSeg];
+    __shared__ int n_slot;
+    const int f = blockIdx.z;
+    const int zb = blockIdx.y * kFZ;
+    const int cb = blockIdx.x * kBlk;
+    const int tid = threadIdx.x;
+
+    // 0. which tiles touch this block, and their patch extents (serial, tiny)
+    if (tid == 0) {
+        int n = 0, off = 0;
+        for (int t = 0; t < tl.n; ++t) {
+            const StitchDev& p = plans[tl.id[t]];
+            const int cbi = cb / kBlk - p.cblk_first;
+            if (cbi < 0 || cbi >= p.n_cblk) continue;
+            const int2 xb = p.cblk[cbi];
+            if (xb.x < 0) continue;
+            const int zb0 = zb / kBlk;
+            const int nzb = (p.n_out_z + kBlk - 1) / kBlk;
+            int lo = 1 << 30, hi = -1;
+            for (int k = zb0; k < zb0 + kFZ / kBlk && k < nzb; ++k) {
+                const int2 r = p.zblk[k];
+                if (r.x < 0) continue;
+                lo = min(lo, r.x);
+                hi = max(hi, r.y);
+            }
+            if (hi < 0) continue;
+            TileSlot s;
+            s.plan = t;
+            s.x_lo = xb.x;
+            s.xs = xb.y - xb.x + 1;
+            s.r_lo = lo;
+            s.rs = hi - lo + 1;
+            s.off = off;
+            off += s.xs * s.rs * (p.shift != nullptr ? 2 : 1);
+            slot[n++] = s;
+        }
+        n_slot = n;
+    }
+    __syncthreads();
+    const int ns = n_slot;
+
+    // 1. gather every contributing patch: a * F (and F when the optical-path
+    //    correction makes it depend on the A-scan), depth fastest
+    for (int k = 0; k < ns; ++k) {
+        const TileSlot s = slot[k];
+        const StitchDev& p = plans[tl.id[s.plan]];
+        const float* mag_f = mag + s.plan * mag_tile_stride + static_cast<int64_t>(f) * n_tile_x * kHalf;
+        float* pa = sm + s.off;
+        float* pf = pa + s.xs * s.rs;
+        const int fy = f0 + f;
+        // 64 consecutive threads read 64 consecutive rows of one A-scan, four A-scans per pass
+        for (int rr = tid & 63; rr < s.rs; rr += 64)
+#pragma unroll 4
+        for (int xx = tid >> 6; xx < s.xs; xx += kStThreads / 64) {
+            const int i = xx * s.rs + rr;
+            const int x = s.x_lo + xx;
+            const int r = s.r_lo + rr;
+            const int ra = p.r0 + r;
+            int src = ra;
+            float F = p.fz[r];
+            if (p.shift != nullptr) {
+                const int64_t o = static_cast<int64_t>(fy) * p.n_tile_x + x;
+                if (ra < p.lo[o] || ra > p.hi[o]) F = 0.f;
+                src = ra + p.shift[o];
+                src = src < 0 ? 0 : (src > p.n_rows - 1 ? p.n_rows - 1 : src);
+                pf[i] = F;
+            }
+            pa[i] = mag_f[static_cast<int64_t>(x) * kHalf + src] * F;
+        }
+    }
+    __syncthreads();
+
+    // 2. per voxel: tiles in order, depth (Wz) then lateral (WxT) interpolation
+    const int tx = tid & (kBlk - 1), ty = tid / kBlk;
+    const int c = cb + tx;
+    float an[kFRows], ad[kFRows];
+#pragma unroll
+    for (int q = 0; q < kFRows; ++q) an[q] = ad[q] = 0.f;
+    for (int k = 0; k < ns; ++k) {
+        const TileSlot s = slot[k];
+        const StitchDev& p = plans[tl.id[s.plan]];
+        const int cc = c - p.c0;
+        if (cc < 0 || cc >= p.C) continue;
+        const int xr = p.xr[cc];
+        if (xr < 0) continue;
+        const float* pa = sm + s.off;
+        const float* pf = pa + s.xs * s.rs;
+        const bool opc = p.shift != nullptr;
+        const int x0 = xr - s.x_lo;
+        const bool has_x1 = x0 + 1 < s.xs;
+        const float wx0 = p.wx0[cc], wx1 = p.wx1[cc];
+#pragma unroll
+        for (int q = 0; q < kFRows; ++q) {
+            const int zo = zb + ty + 8 * q;
+            if (zo >= p.n_out_z) continue;
+            const int zr = p.zr[zo];
+            if (zr < 0) continue;
+            const int rr = zr - s.r_lo;
+            const bool has_r1 = rr + 1 < s.rs;
+            const float w0 = p.wz0[zo], w1 = p.wz1[zo];
+            const float* a0p = pa + x0 * s.rs + rr;
+            const float a00 = a0p[0], a01 = has_r1 ? a0p[1] : 0.f;
+            const float a10 = has_x1 ? a0p[s.rs] : 0.f;
+            const float a11 = has_x1 && has_r1 ? a0p[s.rs + 1] : 0.f;
+            float f00, f01, f10, f11;
+            if (opc) {
+                const float* f0p = pf + x0 * s.rs + rr;
+                f00 = f0p[0];
+                f01 = has_r1 ? f0p[1] : 0.f;
+                f10 = has_x1 ? f0p[s.rs] : 0.f;
+                f11 = has_x1 && has_r1 ? f0p[s.rs + 1] : 0.f;
+            } else {
+                f00 = p.fz[zr];
+                f01 = has_r1 ? p.fz[zr + 1] : 0.f;
+                f10 = has_x1 ? f00 : 0.f;
+                f11 = has_x1 ? f01 : 0.f;
+            }
+            const float u0 = fmaf(a01, w1, a00 * w0), u1 = fmaf(a11, w1, a10 * w0);
+            const float d0 = fmaf(f01, w1, f00 * w0), d1 = fmaf(f11, w1, f10 * w0);
+            an[q] += fmaf(u1, wx1, u0 * wx0);
+            ad[q] += fmaf(d1, wx1, d0 * wx0);
+        }
+    }
+
+    // 3. finalise (pipeline.py:296-300) and clim (io/tiff_writer.py:48-50)
+    float mn = __int_as_float(0x7f800000), mx = -__int_as_float(0x7f800000);
+#pragma unroll
+    for (int q = 0; q < kFRows; ++q) {
+        const int zo = zb + ty + 8 * q;
+        if (zo >= n_out_z || c >= n_out_x) continue;
+        float v;
+        if (ad[q] < thr || isnan(ad[q])) {
+            v = __int_as_float(0x7fc00000);
+        } else {
+            v = 20.0f * log10f(__fdiv_rn(an[q], ad[q]));
+        }
+        db[(static_cast<int64_t>(f) * n_out_z + zo) * n_out_x + c] = v;
+        if (isfinite(v)) {
+            mn = fminf(mn, v);
+            mx = fmaxf(mx, v);
+        }
+    }
+    warp_minmax(mn, mx);
+    if ((tid & 31) == 0 && mn <= mx) {
+        if (plane_mm) {
+            atomicMin(&plane_mm[2 * f], f2ord(mn));
+            atomicMax(&plane_mm[2 * f + 1], f2ord(mx));
+        }
+        if (run_mm) {
+            atomicMin(&run_mm[0], f2ord(mn));
+            atomicMax(&run_mm[1], f2ord(mx));
+        }
     }
 }
 
@@ -97,39 +367,121 @@ __global__ void k_finalise(const float* __restrict__ num, const float* __restric
         }
     }
     if (plane_mm == nullptr) return;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
-        mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-    }
+    warp_minmax(mn, mx);
     if ((threadIdx.x & 31) == 0 && mn <= mx) {
         atomicMin(&plane_mm[2 * plane], f2ord(mn));
         atomicMax(&plane_mm[2 * plane + 1], f2ord(mx));
     }
 }
 
-// db_to_bits (io/tiff_writer.py:26-38) in float64
-__global__ void k_quantise(const float* __restrict__ db, int64_t n, double c1, double c2,
-                           uint16_t* __restrict__ bits) {
-    const double span = c2 - c1;
-    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
-         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-        const float x = db[i];
-        uint16_t b;
-        if (isnan(x)) {
-            b = 0;
-        } else {
-            const double v = (static_cast<double>(x) - c1) / span * 65534.0;
-            // MATLAB uint16(): round half away from zero, saturate to [0, 65535]
-            double r = floor(fabs(v) + 0.5);
-            if (v < 0) r = -r;
-            if (!(r > 0.0)) r = 0.0;
-            if (r > 65535.0) r = 65535.0;
-            unsigned int u = static_cast<unsigned int>(r) + 1u;
-            b = static_cast<uint16_t>(u > 65535u ? 65535u : u);
-        }
-        bits[i] = b;
+// MATLAB uint16() of (db - c1)/(c2 - c1) * 65534, then + 1 saturating, NaN -> 0
+__device__ __forceinline__ uint16_t quantise_exact(float x, double c1, double span) {
+    if (isnan(x)) return 0;
+    const double v = (static_cast<double>(x) - c1) / span * 65534.0;
+    double r = floor(fabs(v) + 0.5);
+    if (v < 0) r = -r;
+    if (!(r > 0.0)) r = 0.0;
+    if (r > 65535.0) r = 65535.0;
+    const unsigned int u = static_cast<unsigned int>(r) + 1u;
+    return static_cast<uint16_t>(u > 65535u ? 65535u : u);
+}
+
+// The legacy code is a non-decreasing function of the float32 dB value
+// (every float64 step is monotonic), so it is fully described by 65534
+// thresholds T[k] = the smallest float32 x with code(x) >= k (k = 2..65535;
+// T[1] = -inf, T[65536] = +inf).  k_quant_table finds each T[k] in float64:
+// a float32 guess next to c1 + (k - 1.5) * span / 65534, then moved ulp by ulp
+// until code(T[k]) >= k > code(prev(T[k])).  Per voxel a float32 estimate
+// v32 = (x - c1f) * sf (error < 0.02 code) gives the code directly when v32
+// is more than kGuard from a rounding boundary; otherwise two table
+// comparisons decide.  Bit-exact, and no float64 work per voxel.
+constexpr float kGuard = 0.05f;
+constexpr int kTable = 65537;
+
+__global__ void k_quant_table(const unsigned int* __restrict__ clim_mm, double c1_in, double c2_in,
+                              float* __restrict__ T) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= kTable) return;
+    double c1 = c1_in, c2 = c2_in;
+    if (clim_mm != nullptr) {
+        c1 = static_cast<double>(ord2f(clim_mm[0]));
+        c2 = static_cast<double>(ord2f(clim_mm[1]));
     }
+    const double span = c2 - c1;
+    if (k <= 1) {
+        T[k] = -__int_as_float(0x7f800000);
+        return;
+    }
+    if (k == kTable - 1) {
+        T[k] = __int_as_float(0x7f800000);
+        return;
+    }
+    float y = static_cast<float>(c1 + (k - 1.5) * span / 65534.0);
+    const float lo = -__int_as_float(0x7f800000), hi = __int_as_float(0x7f800000);
+    for (int i = 0; i < 256 && quantise_exact(y, c1, span) >= k; ++i) y = nextafterf(y, lo);
+    for (int i = 0; i < 256 && quantise_exact(y, c1, span) < k; ++i) y = nextafterf(y, hi);
+    T[k] = y;
+}
+
+struct QuantParams {
+    float c1f, sf;
+    bool fast;
+};
+
+__host__ __device__ inline QuantParams quant_params(double c1, double c2) {
+    QuantParams q;
+    const double span = c2 - c1;
+    q.c1f = static_cast<float>(c1);
+    q.sf = static_cast<float>(65534.0 / span);
+    // three float32 roundings of values <= ~65535 plus the offset error of c1f
+    const double off = fabs(c1 - static_cast<double>(q.c1f)) * (65534.0 / span);
+    q.fast = (4.0 * 65536.0 * 5.96e-8 + off) < 0.5 * kGuard && span > 0.0;
+    return q;
+}
+
+__device__ __forceinline__ uint16_t quantise_one(float x, const QuantParams& q, const float* __restrict__ T) {
+    if (isnan(x)) return 0;
+    int n;       // estimated code
+    if (q.fast) {
+        const float v = (x - q.c1f) * q.sf;
+        if (v < 0.5f - kGuard) return 1;              // rounds to <= 0: clipped to 0, + 1
+        if (v > 65534.5f + kGuard) return 65535;      // rounds to >= 65535: + 1 saturates
+        const float f = v + 0.5f;
+        const float fl = floorf(f);
+        const float fr = f - fl;
+        n = static_cast<int>(fl) + 1;
+        if (fr > kGuard && fr < 1.0f - kGuard) return static_cast<uint16_t>(n);
+        n = n < 1 ? 1 : (n > 65535 ? 65535 : n);
+        // within one code of the truth: settle with the thresholds
+        if (n < 65535 && x >= T[n + 1]) return static_cast<uint16_t>(n + 1);
+        if (x >= T[n]) return static_cast<uint16_t>(n);
+        return static_cast<uint16_t>(n - 1);
+    }
+    // no usable estimate: binary search of the thresholds
+    int a = 1, b = 65535;        // code in [a, b]
+    while (a < b) {
+        const int m = (a + b + 1) >> 1;
+        if (x >= T[m]) a = m; else b = m - 1;
+    }
+    return static_cast<uint16_t>(a);
+}
+
+// db_to_bits (io/tiff_writer.py:26-38), float64 semantics
+__global__ void k_quantise(const float* __restrict__ db, int64_t n, double c1, double c2,
+                           const float* __restrict__ T, uint16_t* __restrict__ bits) {
+    const QuantParams q = quant_params(c1, c2);
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        bits[i] = quantise_one(db[i], q, T);
+}
+
+// same with the clim read from device memory (ordered-uint [min, max] of float32 dB)
+__global__ void k_quantise_dev(const float* __restrict__ db, int64_t n, const unsigned int* __restrict__ clim_mm,
+                               const float* __restrict__ T, uint16_t* __restrict__ bits) {
+    const QuantParams q = quant_params(static_cast<double>(ord2f(clim_mm[0])), static_cast<double>(ord2f(clim_mm[1])));
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        bits[i] = quantise_one(db[i], q, T);
 }
 
 __global__ void k_minmax(const float* __restrict__ x, int64_t n, unsigned int* __restrict__ mm) {
@@ -142,11 +494,7 @@ __global__ void k_minmax(const float* __restrict__ x, int64_t n, unsigned int* _
             mx = fmaxf(mx, v);
         }
     }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
-        mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-    }
+    warp_minmax(mn, mx);
     if ((threadIdx.x & 31) == 0 && mn <= mx) {
         atomicMin(&mm[0], f2ord(mn));
         atomicMax(&mm[1], f2ord(mx));
@@ -164,13 +512,39 @@ int grid_for(int64_t n, int threads) {
     return static_cast<int>(b < 1 ? 1 : b);
 }
 
+size_t patch_smem(int xs_max, int rs_max) {
+    return sizeof(float) * (2 * static_cast<size_t>(xs_max) * rs_max + 2 * static_cast<size_t>(xs_max) * kBlk);
+}
+
 }  // namespace
 
-cudaError_t launch_stitch(const StitchDev& p, const float* mag, const int* frame_y, int B, float* num, float* den,
-                          int frame_offset, int n_out_x, cudaStream_t st) {
-    const int64_t n = static_cast<int64_t>(B) * p.n_out_z * p.C;
-    if (n == 0) return cudaSuccess;
-    k_stitch<<<grid_for(n, 256), 256, 0, st>>>(p, mag, frame_y, B, num, den, frame_offset, n_out_x);
+cudaError_t launch_stitch(const StitchDev& p, const float* mag, const int* frame_y, int f0, int B, float* num,
+                          float* den, int frame_offset, int n_out_x, int xs_max, int rs_max, cudaStream_t st) {
+    if (B == 0 || p.n_cblk == 0) return cudaSuccess;
+    const size_t smem = patch_smem(xs_max, rs_max);
+    cudaError_t e = cudaFuncSetAttribute(k_stitch_tile, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(smem));
+    if (e != cudaSuccess) return e;
+    const dim3 grid(p.n_cblk, (p.n_out_z + kBlk - 1) / kBlk, B);
+    k_stitch_tile<<<grid, kStThreads, smem, st>>>(p, mag, frame_y, f0, num, den, frame_offset, n_out_x, xs_max,
+                                                   rs_max);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_stitch_frames(const StitchDev* plans_dev, const TileList& tiles, const float* mag,
+                                 int64_t mag_tile_stride, int B, int n_tile_x, int f0, int n_out_z, int n_out_x,
+                                 float thr, float* db, unsigned int* plane_mm, unsigned int* run_mm, int xs_max,
+                                 int rs_max, bool any_opc, cudaStream_t st) {
+    if (B == 0) return cudaSuccess;
+    // every tile slot: xs_max A-scans x (two 32-row blocks of rows) x a*F (and F with optical-path correction)
+    const size_t smem = sizeof(float) * static_cast<size_t>(tiles.n) * xs_max * (2 * rs_max) * (any_opc ? 2 : 1);
+    if (smem > 200 * 1024) return cudaErrorInvalidValue;
+    cudaError_t e = cudaFuncSetAttribute(k_stitch_frames, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(smem));
+    if (e != cudaSuccess) return e;
+    const dim3 grid((n_out_x + kBlk - 1) / kBlk, (n_out_z + kFZ - 1) / kFZ, B);
+    k_stitch_frames<<<grid, kStThreads, smem, st>>>(plans_dev, tiles, mag, mag_tile_stride, n_tile_x, f0, n_out_z,
+                                                     n_out_x, thr, db, plane_mm, run_mm);
     return cudaGetLastError();
 }
 
@@ -183,9 +557,19 @@ cudaError_t launch_finalise(const float* num, const float* den, int64_t n_per_pl
     return cudaGetLastError();
 }
 
-cudaError_t launch_quantise(const float* db, int64_t n, double c1, double c2, uint16_t* bits, cudaStream_t st) {
+cudaError_t launch_quantise(const float* db, int64_t n, double c1, double c2, float* table, uint16_t* bits,
+                            cudaStream_t st) {
     if (n == 0) return cudaSuccess;
-    k_quantise<<<grid_for(n, 256), 256, 0, st>>>(db, n, c1, c2, bits);
+    k_quant_table<<<(kTable + 255) / 256, 256, 0, st>>>(nullptr, c1, c2, table);
+    k_quantise<<<grid_for(n, 256), 256, 0, st>>>(db, n, c1, c2, table, bits);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_quantise_dev(const float* db, int64_t n, const unsigned int* clim_mm, float* table,
+                                uint16_t* bits, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    k_quant_table<<<(kTable + 255) / 256, 256, 0, st>>>(clim_mm, 0.0, 0.0, table);
+    k_quantise_dev<<<grid_for(n, 256), 256, 0, st>>>(db, n, clim_mm, table, bits);
     return cudaGetLastError();
 }
 

@@ -68,3 +68,58 @@ def test_batching_does_not_change_result(gpu_ctx, telesto):
     np.testing.assert_array_equal(a, b)
     c = rr.process_row(tiles, [1])
     np.testing.assert_array_equal(c[0], a[1])
+
+
+def test_frames_api_equals_row_api(gpu_ctx, telesto):
+    """All tiles of a frame batch in one call (num/den on chip) give the same
+    planes, NaN masks and clims as the per-tile accumulation."""
+    t = telesto
+    rr, tiles = _build(t, gpu_ctx)
+    ref, ref_mm = rr.process_row(tiles, [0, 1], plane_clims=True)
+    ids = [tile.stitcher.plan for tile in tiles]
+    raws = [t["raw"][k][0:2] for k in range(len(tiles))]
+    gpu_ctx.clim_reset()
+    db, mm = gpu_ctx.frames_process(ids, raws, int(t["apod_size"]), 0, rr.n_out_z, rr.n_out_x, rr.threshold,
+                                    plane_minmax=True)
+    np.testing.assert_array_equal(db, ref)
+    np.testing.assert_array_equal(mm, ref_mm)
+    assert gpu_ctx.clim_get() == (float(np.nanmin(ref)), float(np.nanmax(ref)))
+    # one frame at a time from frame 1 (optical-path rows follow f0)
+    one = gpu_ctx.frames_process(ids, [t["raw"][k][1:2] for k in range(len(tiles))], int(t["apod_size"]), 1,
+                                 rr.n_out_z, rr.n_out_x, rr.threshold)
+    np.testing.assert_array_equal(one[0], ref[1])
+
+
+def test_graph_capture_replays_frame_batch(gpu_ctx, telesto):
+    torch = pytest.importorskip("torch")
+    t = telesto
+    rr, tiles = _build(t, gpu_ctx)
+    ref = rr.process_row(tiles, [0, 1])
+    ids = [tile.stitcher.plan for tile in tiles]
+    raws = [torch.from_numpy(np.ascontiguousarray(t["raw"][k][0:2])).cuda() for k in range(len(tiles))]
+    db = torch.empty((2, rr.n_out_z, rr.n_out_x), dtype=torch.float32, device="cuda")
+    bits = torch.empty(db.shape, dtype=torch.int16, device="cuda")
+    stream = torch.cuda.Stream()
+    gpu_ctx.set_stream(stream.cuda_stream)
+    try:
+        def seq():
+            gpu_ctx.clim_reset()
+            gpu_ctx.frames_process(ids, raws, int(t["apod_size"]), 0, rr.n_out_z, rr.n_out_x, rr.threshold, out=db)
+            gpu_ctx.quantise_running(db, bits)
+        seq()                                   # sizes every buffer
+        gpu_ctx.synchronize()
+        db.fill_(0)
+        torch.cuda.synchronize()
+        gpu_ctx.graph_begin()
+        seq()
+        gid = gpu_ctx.graph_end()
+        n0 = gpu_ctx.launches
+        gpu_ctx.graph_launch(gid)
+        gpu_ctx.synchronize()
+        assert gpu_ctx.launches - n0 == 6       # clim init, apod, spectral, stitch, quant table, quantise
+        np.testing.assert_array_equal(db.cpu().numpy(), ref)
+        from oracle import numerics as O
+        clim = (float(np.nanmin(ref)), float(np.nanmax(ref)))
+        np.testing.assert_array_equal(bits.cpu().numpy().view(np.uint16), O.db_to_bits(ref, clim))
+    finally:
+        gpu_ctx.set_stream(None)
