@@ -187,6 +187,25 @@ int octgb_graph_begin(octgb_ctx *ctx);
 int octgb_graph_end(octgb_ctx *ctx, int *graph_id);
 int octgb_graph_launch(octgb_ctx *ctx, int graph_id);
 
+/* ---------------------------------------------------------------- allocation-free */
+
+/* The magnitude of octgb_magnitude for callers that cannot allocate GPU
+ * memory while they run (e.g. a frame-grabber callback, where cudaMalloc may
+ * synchronise the device and stall acquisition, or a process whose GPU
+ * memory belongs to another framework's pool).  This entry point has no
+ * counterpart in the reference.  raw (B, interf, n) and mag (B, interf-apod,
+ * n/2) must be device pointers owned by the caller; the only scratch (the
+ * apodisation mean) lives in a fixed array of 64 B-scans x n floats
+ * (512 KiB) in the library image, held by every GPU that loads the library
+ * until the process exits; B > 64 is rejected with OCTGB_ERR_ARG.  The call
+ * makes no cudaMalloc/cudaFree.  The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress); make that first call before
+ * any stream capture.  All calls on a device share the array, so calls that
+ * overlap on the GPU (other streams or contexts) race; serialise them.  The
+ * call is asynchronous: octgb_synchronize reports device-side errors. */
+int octgb_magnitude_noalloc(octgb_ctx *ctx, const void *raw, int raw_dtype, int B, int interf, int apod_size,
+                            float *mag);
+
 #ifdef __cplusplus
 }
 #endif

@@ -49,6 +49,7 @@ SIGNATURES = {
     "octgb_graph_begin": (c_int, [c_void_p]),
     "octgb_graph_end": (c_int, [c_void_p, POINTER(c_int)]),
     "octgb_graph_launch": (c_int, [c_void_p, c_int]),
+    "octgb_magnitude_noalloc": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_void_p]),
 }
 
 _lib = None

@@ -920,3 +920,88 @@ int octgb_graph_launch(octgb_ctx* c, int graph_id) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free magnitude entry point.
+//
+// Some callers cannot call cudaMalloc at the point where they reconstruct:
+// an acquisition loop that runs inside a frame-grabber callback (cudaMalloc
+// can synchronise the device and stall the camera stream), or a host process
+// whose GPU memory is owned by another framework's pooling allocator under a
+// fixed budget.  For them octgb_magnitude_noalloc does the work of
+// octgb_magnitude on device buffers the caller already owns, and keeps its one
+// piece of scratch (the per-B-scan apodisation mean) in the fixed array below
+// instead of a context buffer.  The array is part of the loaded library image:
+// every GPU that loads the library holds it until the process exits.
+namespace {
+
+constexpr int kNoAllocMaxBscans = 64;   // B-scans per call: 64 x 2048 floats = 512 KiB
+
+static __device__ __align__(256) float g_noalloc_apod[kNoAllocMaxBscans * kN];
+
+// Device address of g_noalloc_apod per device: the name is a host-side
+// stand-in in host code, so the address is looked up once per device, with
+// that device current, and passed to the kernels.
+constexpr int kMaxDevices = 64;
+std::atomic<float*> g_noalloc_ptr[kMaxDevices];
+
+float* noalloc_scratch(int device) {
+    require(device >= 0 && device < kMaxDevices, "device ordinal out of range for the allocation-free path");
+    float* p = g_noalloc_ptr[device].load();
+    if (p == nullptr) {
+        void* addr = nullptr;
+        ck(cudaGetSymbolAddress(&addr, g_noalloc_apod), "cudaGetSymbolAddress(allocation-free scratch)");
+        p = static_cast<float*>(addr);
+        g_noalloc_ptr[device].store(p);
+    }
+    return p;
+}
+
+}  // namespace
+
+extern "C" int octgb_magnitude_noalloc(octgb_ctx* c, const void* raw, int dtype, int B, int interf, int apod,
+                                       float* mag) {
+    return guarded(c, [&] {
+        if (!c->has_geom) throw Error(OCTGB_ERR_STATE, "octgb_set_geometry has not been called");
+        if (c->capturing) throw Error(OCTGB_ERR_STATE, "not available during graph capture through this context");
+        if (c->cancel.load()) throw Error(OCTGB_ERR_CANCELLED, "cancelled");
+        validate_raw(raw, dtype, OCTGB_DEVICE, B, interf, apod);
+        require(mag != nullptr, "mag is NULL");
+        if (B > kNoAllocMaxBscans)
+            throw Error(OCTGB_ERR_ARG, "octgb_magnitude_noalloc: B = " + std::to_string(B) +
+                                           " exceeds the allocation-free limit of " +
+                                           std::to_string(kNoAllocMaxBscans) + " B-scans per call");
+        if (B == 0) return;
+        float* scratch = noalloc_scratch(c->device);
+        // the same launches as octgb_magnitude, with the apodisation mean in
+        // the fixed array; k_apod_mean writes every element the spectral
+        // kernel then reads, so nothing in the array needs clearing
+        SpectralArgs a{};
+        a.raw = raw;
+        a.seg[0] = raw;
+        a.n_seg = 1;
+        a.B = B;
+        a.interf = interf;
+        a.apod = apod;
+        a.nx = interf - apod;
+        a.n_ascans = static_cast<int64_t>(B) * (interf - apod);
+        a.apod_mean = scratch;
+        a.g.w = c->w.as<float>();
+        a.g.start = c->start.as<int>();
+        a.g.taps = c->taps;
+        a.g.win = c->win.as<float2>();
+        a.g.tw = c->tw.as<float2>();
+        a.g.wsh = c->wsh.as<float>();
+        a.g.s0 = c->s0.as<int>();
+        a.g.U = c->U;
+        a.out = mag;
+        a.status = c->status_dev;
+        ck(launch_apod_mean(a, dtype, c->stream), "apod kernel");
+        c->launches++;
+        const int64_t quads = (a.n_ascans + kPerCta - 1) / kPerCta;
+        int64_t grid = static_cast<int64_t>(c->num_sms) * spectral_max_ctas_per_sm(dtype, kModeMag);
+        if (grid > quads) grid = quads;
+        ck(launch_spectral(a, dtype, kModeMag, static_cast<int>(grid), c->stream), "spectral kernel");
+        c->launches++;
+    });
+}
