@@ -1,0 +1,215 @@
+"""Device "gb300" for the reference's octrecon package.
+
+`register()` adds the device to an imported octrecon without editing its
+files, so `Reconstructor`, the CLI (`--set device=gb300`) and the web app
+(config `device`) drive the GB300 kernels unchanged:
+
+* octrecon/backend.py:61-83 `get_xp` accepts "gb300" and returns a TorchXP-
+  like namespace on the CUDA device (`is_torch` true, :86), so the pipeline
+  builds its host-side operators exactly as for its torch backend
+  (octrecon/pipeline.py:172-189) and never imports CuPy.  The name is bound by
+  value in pipeline.py:33 and estimation/_common.py:14, so those module
+  globals are patched too.
+* `Reconstructor.__init__` (pipeline.py:96-192) is wrapped: when the device is
+  "gb300" it uploads the geometry the reference built (self.sg: sinc band and
+  window, geometry.py:84-128; self.stitchers: TileStitcher operators,
+  stitching.py:84-120; self.oc: optical-path correction, :54-78) into an
+  octgb context and binds `process_row` to the GB300 row engine below.
+* The bound `process_row` keeps the reference's contract (pipeline.py:223-302):
+  same arguments, threaded read-ahead of raw batches through the reference's
+  own readers, cancellation checked per batch (raises octrecon's Cancelled),
+  `on_batch(done, total)` callbacks, the `timers` keys, and returns float32 dB
+  (nFrames, nOutZ, nOutX) on the host.  Tiles are processed x-major/z-minor
+  and every batch is added in that order, as in the reference.
+* The web app's GPU card only lights up when CuPy imports
+  (webapp/server.py:74-85); `register()` patches its `system_info` to report
+  the gb300 device.
+
+There is no CPU fallback: if the CUDA library or device is unusable the
+Reconstructor construction fails with the library's error.
+"""
+from __future__ import annotations
+
+import time
+from collections import deque
+from concurrent.futures import ThreadPoolExecutor
+
+import numpy as np
+
+DEVICE = "gb300"
+_registered = False
+
+
+def _torch_xp_class():
+    from octrecon.core.torch_backend import TorchXP
+
+    class GB300XP(TorchXP):
+        """TorchXP on CUDA: satisfies the pipeline's array duck-type for the
+        host-side operator construction; the hot path runs in liboctgb."""
+
+        def __init__(self, device_index: int = 0):
+            super().__init__(f"cuda:{device_index}")
+            self.name = DEVICE
+
+    return GB300XP
+
+
+def register(device_index: int = 0) -> None:
+    """Register device "gb300" with the imported octrecon (idempotent)."""
+    global _registered
+    if _registered:
+        return
+    import octrecon.backend as backend
+    import octrecon.pipeline as pipeline
+
+    GB300XP = _torch_xp_class()
+    orig_get_xp = backend.get_xp
+
+    def get_xp(device: str = "auto"):
+        if device == DEVICE:
+            return GB300XP(device_index), DEVICE
+        return orig_get_xp(device)
+
+    get_xp.__doc__ = orig_get_xp.__doc__
+    backend.get_xp = get_xp
+    pipeline.get_xp = get_xp
+    try:
+        import octrecon.estimation._common as common
+        common.get_xp = get_xp
+        # estimators run on the CPU path when asked for the gb300 device
+        orig_ctx_init = common.VolumeContext.__init__
+
+        def ctx_init(self, volume_folder, device="cpu", dtype=np.float32):
+            orig_ctx_init(self, volume_folder, "cpu" if device == DEVICE else device, dtype)
+
+        common.VolumeContext.__init__ = ctx_init
+    except ImportError:
+        pass
+
+    orig_init = pipeline.Reconstructor.__init__
+
+    def init(self, cfg, *a, **kw):
+        orig_init(self, cfg, *a, **kw)
+        if self.device == DEVICE:
+            _attach(self, device_index)
+
+    pipeline.Reconstructor.__init__ = init
+
+    try:
+        import octrecon.webapp.server as server
+        orig_info = server.system_info
+
+        def system_info():
+            info = dict(orig_info())
+            try:
+                import torch
+                if torch.cuda.is_available():
+                    info.update(gpu_available=True, gpu_kind=DEVICE, gpu_name=torch.cuda.get_device_name(device_index))
+            except Exception:
+                pass
+            return info
+
+        server.system_info = system_info
+    except Exception:
+        pass
+    _registered = True
+
+
+class _RowEngine:
+    """The octgb context of one Reconstructor: geometry, stitch plans."""
+
+    def __init__(self, R, device_index: int):
+        from ._lib import Context
+        hdr = R.hdr
+        if max(1, hdr.bscan_avg) != 1 or max(1, hdr.ascan_avg) != 1:
+            raise NotImplementedError("gb300: B-/A-scan repeat averaging is not supported by the GB300 kernels")
+        if hdr.spectra_avg > 1 or hdr.apod_mode != "lines":
+            raise NotImplementedError("gb300: AScanBinning / frame-mean apodisation are not supported by the GB300 "
+                                      "kernels")
+        self.ctx = Context(device_index)
+        self.ctx.set_geometry(R.sg.sinc_idx, R.sg.sinc_w, R.sg.window)
+        self.plans = {}
+        for key, st in R.stitchers.items():
+            if st.empty:
+                continue
+            Wz = st.WzT.detach().cpu().numpy().T if hasattr(st, "WzT") else np.asarray(st.Wz)
+            WxT = st.WxT.detach().cpu().numpy() if hasattr(st.WxT, "detach") else np.asarray(st.WxT)
+            fz = st.fz.detach().cpu().numpy() if hasattr(st.fz, "detach") else np.asarray(st.fz)
+            oc = R.oc
+            self.plans[key] = self.ctx.stitch_plan(
+                len(R.sg.z_um), st.r0, st.r1, st.c0, st.c1, Wz, WxT, fz,
+                None if oc is None else oc.shift, None if oc is None else oc.pdz)
+        from .stitching import min_weight_threshold
+        self.threshold = min_weight_threshold(np.float32)
+
+
+def _attach(R, device_index: int) -> None:
+    R._gb300 = _RowEngine(R, device_index)
+    R.process_row = _process_row.__get__(R, type(R))
+
+
+def _process_row(self, yi: int, frames=None, pool=None, on_batch=None):
+    """GB300 body of Reconstructor.process_row (octrecon/pipeline.py:223-302)."""
+    from octrecon.pipeline import Cancelled
+    eng = self._gb300
+    cfg, hdr = self.cfg, self.hdr
+    frames = np.arange(self.si.n_y_px) if frames is None else np.asarray(frames)
+    nF = len(frames)
+    _, nz_out, nx_out = self.n_out
+    B = cfg.batch_frames
+    jobs = []
+    for t in self.si.tiles_in_row(yi):
+        if self.stitchers[(t.xi, t.zi)].empty:
+            continue
+        for s in range(0, nF, B):
+            jobs.append((t, s, frames[s:s + B]))
+
+    def read_job(job):
+        t, s, fr = job
+        files = [f for fr_ in fr for f in self.frame_files(int(fr_))]
+        buf = np.empty((len(files), hdr.interf_size, hdr.n_lambda), np.dtype(hdr.raw_dtype))
+        self.reader(t.folder).read_bscans(files, buf)
+        return buf
+
+    ctx = eng.ctx
+    ctx.row_begin(nF, nz_out, nx_out)
+    own_pool = pool is None
+    pool = pool or ThreadPoolExecutor(cfg.io_threads)
+    pending = deque()
+    it = iter(jobs)
+    for _ in range(self.prefetch):
+        j = next(it, None)
+        if j is None:
+            break
+        pending.append((j, pool.submit(read_job, j)))
+    n_done = 0
+    try:
+        while pending:
+            if self.cancel.is_set():
+                raise Cancelled()
+            job, fut = pending.popleft()
+            t0 = time.perf_counter()
+            raw = fut.result()
+            t1 = time.perf_counter()
+            self.timers["io_wait"] += t1 - t0
+            nxt = next(it, None)
+            if nxt is not None:
+                pending.append((nxt, pool.submit(read_job, nxt)))
+            t, s, fr = job
+            # spectral stage + stitching + accumulation of this batch on the device
+            ctx.row_add_batch(eng.plans[(t.xi, t.zi)], raw, hdr.apod_size, fr, s)
+            t2 = time.perf_counter()
+            self.timers["spectral"] += t2 - t1
+            n_done += 1
+            if on_batch:
+                on_batch(n_done, len(jobs))
+    finally:
+        if own_pool:
+            pool.shutdown(wait=True, cancel_futures=True)
+        else:
+            for _, f in pending:
+                f.cancel()
+    t0 = time.perf_counter()
+    out = ctx.row_finalise(eng.threshold, (nF, nz_out, nx_out))
+    self.timers["finalise"] += time.perf_counter() - t0
+    return out

@@ -15,6 +15,11 @@ its NumPy path.  Outputs (committed, small):
                      reference's stitch operators, its float64 and float32
                      planes for output y = 1, and the unmodified-MATLAB golden
                      plane + tie mask from tests/data/legacy_formats_ref.npz.
+  telesto_volume.tar.gz  the same `telesto` scan as the reference's generator
+                     writes it to disk (ScanInfo.json, Thorlabs Header.xml,
+                     data/Spectral*.data, chirp): input of the end-to-end test
+                     that drives the reference's own Reconstructor on device
+                     "gb300".
   spectral_case.npz  one synthetic B-scan (config-0 spectrum model, uint16,
                      25 apodisation + 64 A-scans, seed 7) with the reference
                      geometry (sinc idx/w, window) and its SpectralProcessor
@@ -98,6 +103,10 @@ def main(ref_root: str):
         plane_fp64=out["float64"], plane_fp32=out["float32"], plane_y=np.int64(1),
         matlab_plane=legacy["telesto__planeDb"], matlab_tie=legacy["telesto__tie"],
         **st)
+
+    import tarfile
+    with tarfile.open(HERE / "telesto_volume.tar.gz", "w:gz") as tf:
+        tf.add(vol, arcname="telesto")
 
     # ------------------------------------------------------------ spectral case (config-0 model)
     lam = synthetic.lambda_nm()
