@@ -40,6 +40,10 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "A-scans/s on 1 GB300 (fused vs plain FP32; learned vs search β) at ≤1 LSB"
 APOD = 25
+# DRAM bytes per A-scan of the spectral kernel from one ncu capture
+# (profiles/k_spectral_config1_small.md: (49.47 + 11.77) MB over 12 000 A-scans;
+# caches flushed before the kernel, magnitudes partly still in L2 at its end)
+SPECTRAL_DRAM_BYTES_PER_ASCAN = (49.474304e6 + 11.768576e6) / 12000
 
 
 # ------------------------------------------------------------------------ workload description
@@ -175,7 +179,7 @@ class Volume:
         return sum(int(t.numel()) * 2 for t in self.raw.values())
 
 
-def run_step(ctx, vol, src, db_vol, bits, batch=2):
+def run_step(ctx, vol, src, db_vol, bits, batch=6):
     """One whole-volume reconstruction through the frame-batch API: for each
     y-row and each batch of `batch` frames, every tile's spectral stage and
     the stitched, finalised planes (num/den never leave the chip; the
@@ -286,7 +290,8 @@ def gpu_arm(args, rank, world):
                        frame_batch=args.batch, cuda_graph=graph is not None),
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": None, "kernel": "spectral stage (apod mean + k_spectral, magnitude out)",
+                     "traffic": SPECTRAL_DRAM_BYTES_PER_ASCAN * kascans,
+                     "kernel": "spectral stage (apod mean + k_spectral, magnitude out)",
                      "bytes_per_launch": kbytes, "ms_per_launch": kms, "a_scans_per_launch": kascans,
                      "peak_source": src + " (burst copy)"},
         "clocks": clk,
@@ -453,7 +458,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--ref-frames", type=int, default=4)
-    ap.add_argument("--batch", type=int, default=2, help="frames per frame batch")
+    ap.add_argument("--batch", type=int, default=6, help="frames per frame batch")
     ap.add_argument("--bscans", type=int, default=270, help="B-scans per tile (270 = the full workload)")
     ap.add_argument("--no-graph", action="store_true")
     args = ap.parse_args()

@@ -48,6 +48,7 @@ struct DevBuf {
 struct Plan {
     int n_rows, r0, R, c0, C, n_out_z, n_tile_x, n_y;
     int cblk_first = 0, n_cblk = 0, xs_max = 1, rs_max = 1;
+    std::vector<int2> zblk_h, cblk_h;   // host copies of the block tables
     DevBuf zr, wz0, wz1, xr, wx0, wx1, fz, shift, lo, hi, zblk, cblk;
     bool opc = false;
     StitchDev dev() const {
@@ -77,6 +78,19 @@ struct Plan {
     }
     void release() {
         for (DevBuf* b : {&zr, &wz0, &wz1, &xr, &wx0, &wx1, &fz, &shift, &lo, &hi, &zblk, &cblk}) b->release();
+    }
+};
+
+// Which tiles touch each output block of the frame-batch stitch kernel, with
+// their patch extents and shared-memory offsets; built once per tile list.
+struct SlotTable {
+    std::vector<int> key;        // plan ids, n_out_z, n_out_x
+    DevBuf slots, counts;
+    size_t smem = 0;             // largest patch footprint of a block (bytes)
+    int ns_max = 1;              // most tiles touching one block
+    void release() {
+        slots.release();
+        counts.release();
     }
 };
 
@@ -117,6 +131,7 @@ struct octgb_ctx {
     bool capturing = false;
     int64_t capture_launch0 = 0;
     DevBuf magbuf, dbbuf, planemm, segs, qtable;
+    std::vector<SlotTable*> slot_tables;
     DevBuf num, den;
     int row_nf = 0, row_nz = 0, row_nx = 0;
     bool row_open = false;
@@ -253,6 +268,73 @@ void read_minmax(octgb_ctx* c, const unsigned int* mm_dev, double* out2) {
     }
 }
 
+const SlotTable& slot_table(octgb_ctx* c, int n_tiles, const int* plan_ids, int n_out_z, int n_out_x) {
+    std::vector<int> key(plan_ids, plan_ids + n_tiles);
+    key.push_back(n_out_z);
+    key.push_back(n_out_x);
+    for (SlotTable* t : c->slot_tables)
+        if (t->key == key) return *t;
+    require(!c->capturing, "first use of a tile list during graph capture: run the sequence once before capturing");
+    const int nxb = (n_out_x + kBlk - 1) / kBlk, nzb = (n_out_z + kStitchRows - 1) / kStitchRows;
+    std::vector<StitchSlot> slots(static_cast<size_t>(nxb) * nzb * n_tiles);
+    std::vector<int> counts(static_cast<size_t>(nxb) * nzb, 0);
+    size_t smem = 0;
+    int ns_max = 1;
+    for (int bz = 0; bz < nzb; ++bz) {
+        for (int bx = 0; bx < nxb; ++bx) {
+            const int blk = bz * nxb + bx;
+            int n = 0, off = 0;
+            for (int t = 0; t < n_tiles; ++t) {
+                const Plan& p = *c->plans[plan_ids[t]];
+                const int cbi = bx - p.cblk_first;
+                if (cbi < 0 || cbi >= p.n_cblk || p.cblk_h[cbi].x < 0) continue;
+                int lo = 1 << 30, hi = -1;
+                for (int k = bz * (kStitchRows / kBlk); k < (bz + 1) * (kStitchRows / kBlk); ++k) {
+                    if (k >= static_cast<int>(p.zblk_h.size()) || p.zblk_h[k].x < 0) continue;
+                    lo = lo < p.zblk_h[k].x ? lo : p.zblk_h[k].x;
+                    hi = hi > p.zblk_h[k].y ? hi : p.zblk_h[k].y;
+                }
+                if (hi < 0) continue;
+                StitchSlot s{};
+                s.t = t;
+                s.x_lo = p.cblk_h[cbi].x;
+                s.xs = p.cblk_h[cbi].y - p.cblk_h[cbi].x + 1;
+                s.r_lo = lo;
+                s.rs = hi - lo + 1;
+                s.off = off;
+                s.opc = p.opc ? 1 : 0;
+                off += s.xs * s.rs * (p.opc ? 2 : 1);
+                slots[static_cast<size_t>(blk) * n_tiles + n++] = s;
+            }
+            counts[blk] = n;
+            ns_max = ns_max > n ? ns_max : n;
+            smem = smem > static_cast<size_t>(off) * sizeof(float) ? smem : static_cast<size_t>(off) * sizeof(float);
+        }
+    }
+    require(smem <= 160 * 1024, "stitch patches of one output block exceed shared memory");
+    SlotTable* t = new SlotTable();
+    t->key = key;
+    t->smem = smem;
+    t->ns_max = ns_max;
+    try {
+        ck(t->slots.ensure(slots.size() * sizeof(StitchSlot) + 16), "cudaMalloc(slots)");
+        ck(t->counts.ensure(counts.size() * sizeof(int) + 16), "cudaMalloc(slot counts)");
+        ck(cudaMemcpyAsync(t->slots.p, slots.data(), slots.size() * sizeof(StitchSlot), cudaMemcpyHostToDevice,
+                           c->stream),
+           "H2D slots");
+        ck(cudaMemcpyAsync(t->counts.p, counts.data(), counts.size() * sizeof(int), cudaMemcpyHostToDevice,
+                           c->stream),
+           "H2D slot counts");
+        ck(cudaStreamSynchronize(c->stream), "sync slot table");
+    } catch (...) {
+        t->release();
+        delete t;
+        throw;
+    }
+    c->slot_tables.push_back(t);
+    return *t;
+}
+
 }  // namespace
 
 extern "C" {
@@ -307,6 +389,10 @@ int octgb_destroy(octgb_ctx* c) {
         b->release();
     for (cudaGraphExec_t g : c->graphs)
         if (g) cudaGraphExecDestroy(g);
+    for (SlotTable* t : c->slot_tables) {
+        t->release();
+        delete t;
+    }
     if (c->status_host) cudaFreeHost(c->status_host);
     if (c->own) cudaStreamDestroy(c->own);
     delete c;
@@ -618,6 +704,8 @@ int octgb_stitch_plan(octgb_ctx* c, int n_rows, int r0, int r1, int c0, int c1, 
         require(static_cast<size_t>(2 * xs_max * rs_max + 2 * xs_max * kBlk) * sizeof(float) <= 160 * 1024,
                 "stitch patch too large (output pixel much coarser than the tile sampling)");
         Plan* p = new Plan();
+        p->zblk_h = zb;
+        p->cblk_h = cbt;
         p->cblk_first = cbf;
         p->n_cblk = cbl - cbf + 1;
         p->xs_max = xs_max;
@@ -788,11 +876,9 @@ int octgb_frames_process(octgb_ctx* c, int n_tiles, const int* plan_ids, const v
         require(!(db_loc == OCTGB_HOST && c->capturing), "host output during graph capture");
         TileList tl{};
         tl.n = n_tiles;
-        bool any_opc = false;
         for (int t = 0; t < n_tiles; ++t) {
             require(plan_ids[t] >= 0 && plan_ids[t] < static_cast<int>(c->plans.size()), "bad plan id");
             const Plan& p = *c->plans[plan_ids[t]];
-            any_opc = any_opc || p.opc;
             require(p.n_tile_x == interf - apod, "A-scans per B-scan differ from a plan's tile width");
             require(p.n_out_z == n_out_z && p.c0 + p.C <= n_out_x, "a plan does not fit the output grid");
             require(!p.opc || (f0 >= 0 && f0 + B <= p.n_y), "frames outside the scan");
@@ -832,9 +918,10 @@ int octgb_frames_process(octgb_ctx* c, int n_tiles, const int* plan_ids, const v
             c->launches++;
         }
         ck(c->run_mm.ensure(2 * sizeof(unsigned int)), "cudaMalloc(run mm)");
-        ck(launch_stitch_frames(c->plan_table.as<StitchDev>(), tl, c->magbuf.as<float>(), tile_stride, B, nx, f0,
-                                n_out_z, n_out_x, thr, dst, pmm, c->run_mm.as<unsigned int>(), c->xs_max, c->rs_max,
-                                any_opc, c->stream),
+        const SlotTable& stab = slot_table(c, n_tiles, plan_ids, n_out_z, n_out_x);
+        ck(launch_stitch_frames(c->plan_table.as<StitchDev>(), tl, stab.slots.as<StitchSlot>(), stab.counts.as<int>(),
+                                stab.ns_max, stab.smem, c->magbuf.as<float>(), tile_stride, B, nx, f0, n_out_z, n_out_x, thr, dst,
+                                pmm, c->run_mm.as<unsigned int>(), c->stream),
            "stitch frames kernel");
         c->launches++;
         if (db_loc != OCTGB_DEVICE) copy_out(c, db, OCTGB_HOST, dst, db_bytes);

@@ -174,69 +174,61 @@ __device__ __forceinline__ void warp_minmax(float& mn, float& mx) {
 }
 
 // Frame-batch kernel: one CTA = one frame x 64 output rows x 32 output
-// columns.  All contributing tiles' patches are gathered first (one barrier,
-// many loads in flight), then every voxel sums the tiles in order.
-constexpr int kFZ = 64;                      // output rows per CTA
+// columns.  The tiles touching each block and their patch extents come from a
+// table built once per tile list on the host (StitchSlot), so a CTA starts
+// with a few parallel loads.  All contributing patches and the tiles' row /
+// column interpolation parameters are staged in shared memory first (one
+// barrier, many loads in flight), then every voxel sums the tiles in order.
+constexpr int kFZ = kStitchRows;             // output rows per CTA
 constexpr int kFRows = kFZ / 8;              // rows per thread
 
-struct TileSlot {
-    int plan, x_lo, xs, r_lo, rs, off;       // off: float offset of the slot's patch in smem
-};
-
 __global__ void __launch_bounds__(kStThreads) k_stitch_frames(const StitchDev* __restrict__ plans, const TileList tl,
+                                                              const StitchSlot* __restrict__ slots,
+                                                              const int* __restrict__ slot_count,
                                                               const float* __restrict__ mag, int64_t mag_tile_stride,
                                                               int n_tile_x, int f0, int n_out_z, int n_out_x,
                                                               float thr, float* __restrict__ db,
                                                               unsigned int* __restrict__ plane_mm,
-                                                              unsigned int* __restrict__ run_mm) {
-    extern __shared__ __align__(16) float sm[];
-    __shared__ TileSlot slot[kMaxSeg];
-    __shared__ int n_slot;
+                                                              unsigned int* __restrict__ run_mm, int ns_max) {
+    // dynamic shared memory: per-slot row / column parameters, then the patches
+    extern __shared__ __align__(16) float smem_all[];
+    __shared__ StitchSlot slot[kMaxSeg];
+    int* zr_s = reinterpret_cast<int*>(smem_all);                  // [ns_max][kFZ]
+    float* wz0_s = smem_all + ns_max * kFZ;
+    float* wz1_s = wz0_s + ns_max * kFZ;
+    int* xr_s = reinterpret_cast<int*>(wz1_s + ns_max * kFZ);      // [ns_max][kBlk]
+    float* wx0_s = reinterpret_cast<float*>(xr_s + ns_max * kBlk);
+    float* wx1_s = wx0_s + ns_max * kBlk;
+    float* sm = wx1_s + ns_max * kBlk;
     const int f = blockIdx.z;
     const int zb = blockIdx.y * kFZ;
     const int cb = blockIdx.x * kBlk;
     const int tid = threadIdx.x;
-
-    // 0. which tiles touch this block, and their patch extents (serial, tiny)
-    if (tid == 0) {
-        int n = 0, off = 0;
-        for (int t = 0; t < tl.n; ++t) {
-            const StitchDev& p = plans[tl.id[t]];
-            const int cbi = cb / kBlk - p.cblk_first;
-            if (cbi < 0 || cbi >= p.n_cblk) continue;
-            const int2 xb = p.cblk[cbi];
-            if (xb.x < 0) continue;
-            const int zb0 = zb / kBlk;
-            const int nzb = (p.n_out_z + kBlk - 1) / kBlk;
-            int lo = 1 << 30, hi = -1;
-            for (int k = zb0; k < zb0 + kFZ / kBlk && k < nzb; ++k) {
-                const int2 r = p.zblk[k];
-                if (r.x < 0) continue;
-                lo = min(lo, r.x);
-                hi = max(hi, r.y);
-            }
-            if (hi < 0) continue;
-            TileSlot s;
-            s.plan = t;
-            s.x_lo = xb.x;
-            s.xs = xb.y - xb.x + 1;
-            s.r_lo = lo;
-            s.rs = hi - lo + 1;
-            s.off = off;
-            off += s.xs * s.rs * (p.shift != nullptr ? 2 : 1);
-            slot[n++] = s;
-        }
-        n_slot = n;
-    }
+    const int blk = blockIdx.y * gridDim.x + blockIdx.x;
+    const int ns = slot_count[blk];
+    if (tid < ns) slot[tid] = slots[static_cast<int64_t>(blk) * tl.n + tid];
     __syncthreads();
-    const int ns = n_slot;
 
-    // 1. gather every contributing patch: a * F (and F when the optical-path
-    //    correction makes it depend on the A-scan), depth fastest
+    // 1. stage each contributing tile's interpolation parameters and its
+    //    magnitude patch (a * F, and F when the optical-path correction makes
+    //    it depend on the A-scan); depth fastest in the patch
     for (int k = 0; k < ns; ++k) {
-        const TileSlot s = slot[k];
-        const StitchDev& p = plans[tl.id[s.plan]];
-        const float* mag_f = mag + s.plan * mag_tile_stride + static_cast<int64_t>(f) * n_tile_x * kHalf;
+        const StitchSlot s = slot[k];
+        const StitchDev& p = plans[tl.id[s.t]];
+        if (tid < kFZ) {
+            const int zo = zb + tid;
+            const int zr = zo < p.n_out_z ? p.zr[zo] : -1;
+            zr_s[k * kFZ + tid] = zr;
+            wz0_s[k * kFZ + tid] = zr >= 0 ? p.wz0[zo] : 0.f;
+            wz1_s[k * kFZ + tid] = zr >= 0 ? p.wz1[zo] : 0.f;
+        } else if (tid < kFZ + kBlk) {
+            const int cc = cb + tid - kFZ - p.c0;
+            const int xr = (cc >= 0 && cc < p.C) ? p.xr[cc] : -1;
+            xr_s[k * kBlk + tid - kFZ] = xr;
+            wx0_s[k * kBlk + tid - kFZ] = xr >= 0 ? p.wx0[cc] : 0.f;
+            wx1_s[k * kBlk + tid - kFZ] = xr >= 0 ? p.wx1[cc] : 0.f;
+        }
+        const float* mag_f = mag + s.t * mag_tile_stride + static_cast<int64_t>(f) * n_tile_x * kHalf;
         float* pa = sm + s.off;
         float* pf = pa + s.xs * s.rs;
         const int fy = f0 + f;
@@ -269,27 +261,24 @@ __global__ void __launch_bounds__(kStThreads) k_stitch_frames(const StitchDev* _
 #pragma unroll
     for (int q = 0; q < kFRows; ++q) an[q] = ad[q] = 0.f;
     for (int k = 0; k < ns; ++k) {
-        const TileSlot s = slot[k];
-        const StitchDev& p = plans[tl.id[s.plan]];
-        const int cc = c - p.c0;
-        if (cc < 0 || cc >= p.C) continue;
-        const int xr = p.xr[cc];
+        const int xr = xr_s[k * kBlk + tx];
         if (xr < 0) continue;
+        const StitchSlot s = slot[k];
         const float* pa = sm + s.off;
         const float* pf = pa + s.xs * s.rs;
-        const bool opc = p.shift != nullptr;
+        const bool opc = s.opc != 0;
+        const float* fz = plans[tl.id[s.t]].fz;
         const int x0 = xr - s.x_lo;
         const bool has_x1 = x0 + 1 < s.xs;
-        const float wx0 = p.wx0[cc], wx1 = p.wx1[cc];
+        const float wx0 = wx0_s[k * kBlk + tx], wx1 = wx1_s[k * kBlk + tx];
 #pragma unroll
         for (int q = 0; q < kFRows; ++q) {
-            const int zo = zb + ty + 8 * q;
-            if (zo >= p.n_out_z) continue;
-            const int zr = p.zr[zo];
+            const int z = ty + 8 * q;
+            const int zr = zr_s[k * kFZ + z];
             if (zr < 0) continue;
             const int rr = zr - s.r_lo;
             const bool has_r1 = rr + 1 < s.rs;
-            const float w0 = p.wz0[zo], w1 = p.wz1[zo];
+            const float w0 = wz0_s[k * kFZ + z], w1 = wz1_s[k * kFZ + z];
             const float* a0p = pa + x0 * s.rs + rr;
             const float a00 = a0p[0], a01 = has_r1 ? a0p[1] : 0.f;
             const float a10 = has_x1 ? a0p[s.rs] : 0.f;
@@ -302,8 +291,8 @@ __global__ void __launch_bounds__(kStThreads) k_stitch_frames(const StitchDev* _
                 f10 = has_x1 ? f0p[s.rs] : 0.f;
                 f11 = has_x1 && has_r1 ? f0p[s.rs + 1] : 0.f;
             } else {
-                f00 = p.fz[zr];
-                f01 = has_r1 ? p.fz[zr + 1] : 0.f;
+                f00 = fz[zr];
+                f01 = has_r1 ? fz[zr + 1] : 0.f;
                 f10 = has_x1 ? f00 : 0.f;
                 f11 = has_x1 ? f01 : 0.f;
             }
@@ -531,20 +520,20 @@ cudaError_t launch_stitch(const StitchDev& p, const float* mag, const int* frame
     return cudaGetLastError();
 }
 
-cudaError_t launch_stitch_frames(const StitchDev* plans_dev, const TileList& tiles, const float* mag,
+cudaError_t launch_stitch_frames(const StitchDev* plans_dev, const TileList& tiles, const StitchSlot* slots,
+                                 const int* slot_count, int ns_max, size_t patch_smem_bytes, const float* mag,
                                  int64_t mag_tile_stride, int B, int n_tile_x, int f0, int n_out_z, int n_out_x,
-                                 float thr, float* db, unsigned int* plane_mm, unsigned int* run_mm, int xs_max,
-                                 int rs_max, bool any_opc, cudaStream_t st) {
+                                 float thr, float* db, unsigned int* plane_mm, unsigned int* run_mm, cudaStream_t st) {
     if (B == 0) return cudaSuccess;
-    // every tile slot: xs_max A-scans x (two 32-row blocks of rows) x a*F (and F with optical-path correction)
-    const size_t smem = sizeof(float) * static_cast<size_t>(tiles.n) * xs_max * (2 * rs_max) * (any_opc ? 2 : 1);
-    if (smem > 200 * 1024) return cudaErrorInvalidValue;
+    const size_t smem = patch_smem_bytes + sizeof(float) * static_cast<size_t>(ns_max) * 3 * (kFZ + kBlk) + 16;
+    if (smem > 160 * 1024) return cudaErrorInvalidValue;
     cudaError_t e = cudaFuncSetAttribute(k_stitch_frames, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(smem));
     if (e != cudaSuccess) return e;
     const dim3 grid((n_out_x + kBlk - 1) / kBlk, (n_out_z + kFZ - 1) / kFZ, B);
-    k_stitch_frames<<<grid, kStThreads, smem, st>>>(plans_dev, tiles, mag, mag_tile_stride, n_tile_x, f0, n_out_z,
-                                                     n_out_x, thr, db, plane_mm, run_mm);
+    k_stitch_frames<<<grid, kStThreads, smem, st>>>(plans_dev, tiles, slots, slot_count, mag, mag_tile_stride,
+                                                     n_tile_x, f0, n_out_z, n_out_x, thr, db, plane_mm, run_mm,
+                                                     ns_max);
     return cudaGetLastError();
 }
 
