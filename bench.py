@@ -301,6 +301,12 @@ def gpu_arm(args, rank, world):
                        "h2d_bytes_per_step": vol.raw_bytes(), "d2h_bytes_per_step": int(bits.numel()) * 2}
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline_config1(vol, torch, budget_s=args.cpu_budget)
+    if rank == 0 and not args.no_plain:
+        torch.cuda.synchronize()
+        pf = plain_form_arm(vol, torch, dev)
+        if "value" in pf:
+            pf["speedup_of_value"] = value / world / pf["value"]
+        line["plain_fp32_gpu_form"] = pf
     return line
 
 
@@ -340,6 +346,74 @@ def gpu_arm_config0(args, rank, world, torch, ctx):
             "roofline": {"bound": "hbm", "achieved": 25000 * per / (ms * 1e-3) / 1e9, "peak": hbm, "unit": "GB/s",
                          "frac": 25000 * per / (ms * 1e-3) / 1e9 / hbm, "traffic": None,
                          "peak_source": src}, "clocks": clk}
+
+
+def _import_reference_octrecon():
+    """The reference package from baseline/_ref (offline install), or None."""
+    import types
+    ref = ROOT / "baseline" / "_ref"
+    if not (ref / "octrecon" / "core" / "torch_backend.py").exists():
+        return None
+    if str(ref) not in sys.path:
+        sys.path.insert(0, str(ref))
+    try:
+        import tifffile  # noqa: F401
+    except ImportError:
+        sys.modules.setdefault("tifffile", types.ModuleType("tifffile"))
+    import octrecon.core.torch_backend  # noqa: F401
+    return sys.modules["octrecon"]
+
+
+def plain_form_arm(vol, torch, dev, batch=50):
+    """The reference's own float32 GPU path, unmodified: octrecon's torch backend
+    (TorchSpectralProcessor: gathers + torch.fft, TorchTileStitcher: gather +
+    matmuls, core/torch_backend.py:66-165) on this GPU, driven as
+    Reconstructor.process_row does (pipeline.py:223-300) over y-row 0 of the same
+    volume (6 tiles x 270 frames).  Reported as the plain-FP32 GPU form."""
+    if _import_reference_octrecon() is None:
+        return {"unavailable": "octrecon not installed in baseline/_ref"}
+    from octrecon.core.geometry import build_spectral_geometry
+    from octrecon.core.stitching import TileStitcher, min_weight_threshold
+    from octrecon.core.torch_backend import TorchSpectralProcessor, TorchTileStitcher, TorchXP
+
+    from oct_recon_af_v1_gb300 import synthetic
+    xp = TorchXP(dev)
+    sg = build_spectral_geometry(synthetic.lambda_nm(), synthetic.beta_ref_from_px(1e-5), 1.33, "sinc5")
+    sp = TorchSpectralProcessor(sg, APOD, xp)
+    sts = {(xi, zi): TorchTileStitcher(TileStitcher(vol.tg, None, vol.lay.x_centers_mm[xi], vol.lay.z_depths_mm[zi],
+                                                    vol.focus[zi], 80.0, xp=np, dtype=np.float32), None, xp)
+           for xi, zi in vol.order}
+    thr = min_weight_threshold(np.float32)
+
+    def row(frames_total):
+        num = torch.zeros((frames_total, vol.nz, vol.nx), dtype=torch.float32, device=dev)
+        den = torch.zeros_like(num)
+        for xi, zi in vol.order:
+            st = sts[(xi, zi)]
+            for s0 in range(0, frames_total, batch):
+                raw16 = vol.raw[(0, xi, zi)][s0:s0 + batch]
+                raw = raw16.to(torch.int32) & 0xFFFF          # the uint16 counts
+                fr = torch.arange(s0, s0 + raw.shape[0], device=dev)
+                mag = sp.magnitude(raw)
+                n_, d_ = st.contribute(mag, fr)
+                num[s0:s0 + raw.shape[0], :, st.c0:st.c1] += n_
+                den[s0:s0 + raw.shape[0], :, st.c0:st.c1] += d_
+        den[den < thr] = float("nan")
+        return 20 * torch.log10(num / den)
+
+    row(batch)                                  # warm-up (cuFFT plans, allocator)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    db = row(vol.ny)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    del db
+    ascans = 6 * vol.ny * vol.lay.n_x_px
+    return {"value": ascans / (ms * 1e-3), "unit": "A-scans/s", "ms": ms, "a_scans": ascans,
+            "source": "reference octrecon torch backend (unmodified) on this GPU, y-row 0 of the volume, "
+                      f"batch_frames {batch}; process_row's work (no quantisation)"}
 
 
 def reduce_max(x, world):
@@ -456,6 +530,7 @@ def main():
     ap.add_argument("--config", type=int, default=1, choices=[0, 1])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-plain", action="store_true", help="skip timing the reference's plain float32 GPU path")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--ref-frames", type=int, default=4)
     ap.add_argument("--batch", type=int, default=6, help="frames per frame batch")
