@@ -164,7 +164,11 @@ int octgb_row_finalise(octgb_ctx *ctx, float threshold, float *db, int db_loc, d
  * octgb_clim_reset); plane_minmax (optional, host, B*2 doubles) receives each
  * plane's clim and forces a host sync.  With device raws, device db and no
  * plane_minmax the call does not synchronise and can be graph-captured.
- * n_tiles <= 32. */
+ * Host raws are copied on a separate stream through a ring of three device
+ * slots, so a batch's copy overlaps the previous batch's kernels; with device
+ * db and no plane_minmax the call returns without waiting, so page-locked host
+ * raws must stay unchanged until octgb_synchronize returns (pageable ones are
+ * staged before the call returns).  n_tiles <= 32. */
 int octgb_frames_process(octgb_ctx *ctx, int n_tiles, const int *plan_ids, const void *const *raws, int raw_dtype,
                          int raw_loc, int B, int interf, int apod_size, int f0, int n_out_z, int n_out_x,
                          float threshold, float *db, int db_loc, double *plane_minmax);

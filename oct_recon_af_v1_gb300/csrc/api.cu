@@ -132,6 +132,14 @@ struct octgb_ctx {
     int64_t capture_launch0 = 0;
     DevBuf magbuf, dbbuf, planemm, segs, qtable;
     std::vector<SlotTable*> slot_tables;
+    // host-input staging of the frame API: a copy stream and a ring of device
+    // slots, so the copy of one batch overlaps the kernels of the previous one
+    static constexpr int kRing = 3;
+    cudaStream_t copy = nullptr;
+    DevBuf ring[kRing];
+    cudaEvent_t ring_ready[kRing] = {nullptr, nullptr, nullptr};
+    cudaEvent_t ring_free[kRing] = {nullptr, nullptr, nullptr};
+    int ring_next = 0;
     DevBuf num, den;
     int row_nf = 0, row_nz = 0, row_nx = 0;
     bool row_open = false;
@@ -393,6 +401,13 @@ int octgb_destroy(octgb_ctx* c) {
         t->release();
         delete t;
     }
+    if (c->copy) cudaStreamSynchronize(c->copy);
+    for (int k = 0; k < octgb_ctx::kRing; ++k) {
+        c->ring[k].release();
+        if (c->ring_ready[k]) cudaEventDestroy(c->ring_ready[k]);
+        if (c->ring_free[k]) cudaEventDestroy(c->ring_free[k]);
+    }
+    if (c->copy) cudaStreamDestroy(c->copy);
     if (c->status_host) cudaFreeHost(c->status_host);
     if (c->own) cudaStreamDestroy(c->own);
     delete c;
@@ -888,14 +903,28 @@ int octgb_frames_process(octgb_ctx* c, int n_tiles, const int* plan_ids, const v
         if (B == 0) return;
         const size_t tile_bytes = static_cast<size_t>(B) * interf * kN * raw_elem(dtype);
         const void* segs[kMaxSeg];
+        int slot = -1;
         if (loc == OCTGB_HOST) {
             require(!c->capturing, "host input during graph capture");
-            ck(c->raw.ensure(tile_bytes * n_tiles), "cudaMalloc(raw)");
+            if (c->copy == nullptr) {
+                ck(cudaStreamCreateWithFlags(&c->copy, cudaStreamNonBlocking), "cudaStreamCreate(copy)");
+                for (int k = 0; k < octgb_ctx::kRing; ++k) {
+                    ck(cudaEventCreateWithFlags(&c->ring_ready[k], cudaEventDisableTiming), "cudaEventCreate");
+                    ck(cudaEventCreateWithFlags(&c->ring_free[k], cudaEventDisableTiming), "cudaEventCreate");
+                }
+            }
+            slot = c->ring_next;
+            c->ring_next = (slot + 1) % octgb_ctx::kRing;
+            ck(c->ring[slot].ensure(tile_bytes * n_tiles), "cudaMalloc(raw ring)");
+            // the slot's previous batch must have left the spectral kernel
+            ck(cudaStreamWaitEvent(c->copy, c->ring_free[slot], 0), "cudaStreamWaitEvent");
             for (int t = 0; t < n_tiles; ++t) {
-                void* dst = static_cast<char*>(c->raw.p) + t * tile_bytes;
-                ck(cudaMemcpyAsync(dst, raws[t], tile_bytes, cudaMemcpyHostToDevice, c->stream), "H2D raw");
+                void* dst = static_cast<char*>(c->ring[slot].p) + t * tile_bytes;
+                ck(cudaMemcpyAsync(dst, raws[t], tile_bytes, cudaMemcpyHostToDevice, c->copy), "H2D raw");
                 segs[t] = dst;
             }
+            ck(cudaEventRecord(c->ring_ready[slot], c->copy), "cudaEventRecord");
+            ck(cudaStreamWaitEvent(c->stream, c->ring_ready[slot], 0), "cudaStreamWaitEvent");
         } else {
             for (int t = 0; t < n_tiles; ++t) segs[t] = raws[t];
         }
@@ -903,6 +932,7 @@ int octgb_frames_process(octgb_ctx* c, int n_tiles, const int* plan_ids, const v
         const int64_t tile_stride = static_cast<int64_t>(B) * nx * kHalf;
         ck(c->magbuf.ensure(static_cast<size_t>(tile_stride) * n_tiles * sizeof(float)), "cudaMalloc(mag)");
         launch_spectral_segs(c, segs, n_tiles, dtype, B, interf, apod, kModeMag, c->magbuf.as<float>(), 0, 0, nullptr);
+        if (slot >= 0) ck(cudaEventRecord(c->ring_free[slot], c->stream), "cudaEventRecord");
         const size_t db_bytes = static_cast<size_t>(B) * n_out_z * n_out_x * sizeof(float);
         float* dst = db;
         if (db_loc != OCTGB_DEVICE) {
@@ -935,7 +965,7 @@ int octgb_frames_process(octgb_ctx* c, int n_tiles, const int* plan_ids, const v
                 plane_minmax[2 * f] = none ? NAN : ord2f(h[2 * f]);
                 plane_minmax[2 * f + 1] = none ? NAN : ord2f(h[2 * f + 1]);
             }
-        } else if (db_loc != OCTGB_DEVICE || loc != OCTGB_DEVICE) {
+        } else if (db_loc != OCTGB_DEVICE) {
             check_status(c);
         }
     });

@@ -123,3 +123,39 @@ def test_graph_capture_replays_frame_batch(gpu_ctx, telesto):
         np.testing.assert_array_equal(bits.cpu().numpy().view(np.uint16), O.db_to_bits(ref, clim))
     finally:
         gpu_ctx.set_stream(None)
+
+
+def test_frames_host_input_ring_matches_device_input(gpu_ctx):
+    """Page-locked host raws go through the copy stream and the staging ring;
+    consecutive batches (more than the ring holds) must equal the device path."""
+    torch = pytest.importorskip("torch")
+    from oct_recon_af_v1_gb300 import geometry as G
+    from oct_recon_af_v1_gb300 import stitching as S
+    from oct_recon_af_v1_gb300 import synthetic
+    sg = G.build_spectral_geometry(synthetic.lambda_nm(), synthetic.beta_ref_from_px(1e-5), 1.33)
+    gpu_ctx.set_geometry(sg.sinc_idx, sg.sinc_w, sg.window)
+    lay = S.ScanLayout(np.array([-0.0225, 0.0225]), np.array([0.0]), np.array([0.0, 0.05]), 50, 8, 0.05, 0.008)
+    tg = S.tiled_geometry(lay, sg.z_um, [300.0, 320.0], 1.0)
+    order = [(xi, zi) for xi in range(2) for zi in range(2)]
+    ids = []
+    for xi, zi in order:
+        st = S.TileStitcher.build(tg, lay.x_centers_mm[xi], lay.z_depths_mm[zi], [300.0, 320.0][zi], 80.0)
+        ids.append(st.upload(gpu_ctx))
+    tiles = [synthetic.u16_bits(synthetic.generate(8, 50, 25, seed=40 + k)) for k in range(len(order))]
+    host = [t.pin_memory() for t in tiles]
+    dev = [t.cuda() for t in tiles]
+    nz, nx = len(tg.out_z_mm), len(tg.out_x_mm)
+    thr = S.min_weight_threshold(np.float32)
+    out_h = torch.empty((8, nz, nx), dtype=torch.float32, device="cuda")
+    out_d = torch.empty_like(out_h)
+    for s0 in range(0, 8, 2):                          # 4 batches through a 3-slot ring
+        gpu_ctx.frames_process(ids, [h[s0:s0 + 2] for h in host], 25, s0, nz, nx, thr, out=out_h[s0:s0 + 2],
+                               raw_dtype=0)
+    gpu_ctx.synchronize()
+    for s0 in range(0, 8, 2):
+        gpu_ctx.frames_process(ids, [d[s0:s0 + 2] for d in dev], 25, s0, nz, nx, thr, out=out_d[s0:s0 + 2],
+                               raw_dtype=0)
+    gpu_ctx.synchronize()
+    a, b = out_h.cpu().numpy(), out_d.cpu().numpy()
+    assert np.isfinite(a).any()
+    np.testing.assert_array_equal(a, b)
