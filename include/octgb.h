@@ -191,6 +191,31 @@ int octgb_graph_begin(octgb_ctx *ctx);
 int octgb_graph_end(octgb_ctx *ctx, int *graph_id);
 int octgb_graph_launch(octgb_ctx *ctx, int graph_id);
 
+/* ---------------------------------------------------------------- batched form */
+
+/* One tile of a batch: raw (B, interf, n) and db (B, interf - apod_size,
+ * n_out_z) are device buffers; db is A-scan major (the depth profile of each
+ * A-scan contiguous).  plan_id: octgb_stitch_plan of the tile alone (the
+ * single-tile TileStitcher of octrecon/core/stitching.py:84-120: depth
+ * operator, focus weight, identity lateral operator, no optical-path
+ * correction); n_out_z is the plan's. */
+typedef struct octgb_tile {
+    const void *raw;
+    int B, interf, apod_size;
+    int plan_id;
+    float *db;
+} octgb_tile;
+
+/* Reconstruct n_tiles (<= 256) independent tiles of uneven sizes in ONE
+ * persistent launch: every CTA takes `grab` groups of 4 A-scans at a time
+ * from a device work queue spanning all tiles, runs the spectral stage and
+ * resamples each depth profile with its tile's plan, finalising to dB
+ * (threshold -> NaN, 20*log10(num/den), pipeline.py:296-300).  The finite
+ * [min, max] folds into the running clim.  One apodisation launch precedes
+ * it.  No host sync; graph-capturable once the same tile table has been run. */
+int octgb_batch_process(octgb_ctx *ctx, int n_tiles, const octgb_tile *tiles, int raw_dtype, float threshold,
+                        int grab);
+
 /* ---------------------------------------------------------------- allocation-free */
 
 /* The magnitude of octgb_magnitude for callers that cannot allocate GPU

@@ -50,7 +50,14 @@ SIGNATURES = {
     "octgb_graph_end": (c_int, [c_void_p, POINTER(c_int)]),
     "octgb_graph_launch": (c_int, [c_void_p, c_int]),
     "octgb_magnitude_noalloc": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_void_p]),
+    "octgb_batch_process": (c_int, [c_void_p, c_int, c_void_p, c_int, c_float, c_int]),
 }
+
+
+class OctgbTile(ctypes.Structure):
+    """struct octgb_tile (include/octgb.h)."""
+    _fields_ = [("raw", c_void_p), ("B", c_int), ("interf", c_int), ("apod_size", c_int), ("plan_id", c_int),
+                ("db", c_void_p)]
 
 _lib = None
 
@@ -316,3 +323,15 @@ class Context:
 
     def graph_launch(self, gid: int):
         self._check(self.lib.octgb_graph_launch(self.h, int(gid)))
+
+    # -------------------------------------------------------------- batched form
+    def batch_process(self, tiles, threshold: float, grab: int = 4, raw_dtype: int = U16):
+        """tiles: list of (raw_device_tensor (B, interf, N), apod_size, plan_id, db_device_tensor)."""
+        arr = (OctgbTile * len(tiles))()
+        for k, (raw, apod, plan, db) in enumerate(tiles):
+            B, interf, N = raw.shape
+            if N != self.n:
+                raise ValueError("spectral length differs from the geometry")
+            arr[k] = OctgbTile(raw.data_ptr(), B, interf, int(apod), int(plan), db.data_ptr())
+        self._check(self.lib.octgb_batch_process(self.h, len(tiles), arr, int(raw_dtype), c_float(threshold),
+                                                 int(grab)))

@@ -49,6 +49,8 @@ struct Plan {
     int n_rows, r0, R, c0, C, n_out_z, n_tile_x, n_y;
     int cblk_first = 0, n_cblk = 0, xs_max = 1, rs_max = 1;
     std::vector<int2> zblk_h, cblk_h;   // host copies of the block tables
+    bool lateral_identity = false;      // WxT is the identity (single-tile output grid)
+    bool lateral_quad_local = false;    // every non-zero lateral weight stays inside the column's B-scan quad
     DevBuf zr, wz0, wz1, xr, wx0, wx1, fz, shift, lo, hi, zblk, cblk;
     bool opc = false;
     StitchDev dev() const {
@@ -131,6 +133,8 @@ struct octgb_ctx {
     bool capturing = false;
     int64_t capture_launch0 = 0;
     DevBuf magbuf, dbbuf, planemm, segs, qtable;
+    DevBuf qtiles, qcounter;                 // batched form: tile table and queue head
+    std::vector<QueueTile> qtiles_h;         // the table last uploaded
     std::vector<SlotTable*> slot_tables;
     // host-input staging of the frame API: a copy stream and a ring of device
     // slots, so the copy of one batch overlaps the kernels of the previous one
@@ -393,7 +397,8 @@ int octgb_destroy(octgb_ctx* c) {
         }
     }
     for (DevBuf* b : {&c->w, &c->start, &c->win, &c->tw, &c->wsh, &c->s0, &c->raw, &c->apod, &c->out, &c->mm, &c->frames, &c->num,
-                      &c->den, &c->plan_table, &c->run_mm, &c->magbuf, &c->dbbuf, &c->planemm, &c->segs, &c->qtable})
+                      &c->den, &c->plan_table, &c->run_mm, &c->magbuf, &c->dbbuf, &c->planemm, &c->segs, &c->qtable,
+                      &c->qtiles, &c->qcounter})
         b->release();
     for (cudaGraphExec_t g : c->graphs)
         if (g) cudaGraphExecDestroy(g);
@@ -719,6 +724,20 @@ int octgb_stitch_plan(octgb_ctx* c, int n_rows, int r0, int r1, int c0, int c1, 
         require(static_cast<size_t>(2 * xs_max * rs_max + 2 * xs_max * kBlk) * sizeof(float) <= 160 * 1024,
                 "stitch patch too large (output pixel much coarser than the tile sampling)");
         Plan* p = new Plan();
+        p->lateral_identity = c0 == 0 && C == n_tile_x;
+        // batched form: every quad holding output column cc must also hold the
+        // A-scans it reads (xr with weight wx0, xr + 1 with wx1); quads start
+        // at multiples of 4, the last one of a B-scan at C - 4
+        p->lateral_quad_local = c0 == 0 && C == n_tile_x;
+        const int qpb = (C + kPerCta - 1) / kPerCta;
+        for (int qb = 0; qb < qpb && p->lateral_quad_local; ++qb) {
+            const int q0 = (qb == qpb - 1 && C >= kPerCta) ? C - kPerCta : qb * kPerCta;
+            for (int cc = q0; cc < q0 + kPerCta && cc < C; ++cc) {
+                const bool ok0 = wx0[cc] == 0.f || (xr[cc] >= q0 && xr[cc] < q0 + kPerCta && xr[cc] < C);
+                const bool ok1 = wx1[cc] == 0.f || (xr[cc] + 1 >= q0 && xr[cc] + 1 < q0 + kPerCta && xr[cc] + 1 < C);
+                if (xr[cc] < 0 || !ok0 || !ok1) p->lateral_quad_local = false;
+            }
+        }
         p->zblk_h = zb;
         p->cblk_h = cbt;
         p->cblk_first = cbf;
@@ -1033,6 +1052,96 @@ int octgb_graph_launch(octgb_ctx* c, int graph_id) {
         if (c->cancel.load()) throw Error(OCTGB_ERR_CANCELLED, "cancelled");
         ck(cudaGraphLaunch(c->graphs[graph_id], c->stream), "cudaGraphLaunch");
         c->launches += c->graph_kernels[graph_id];
+    });
+}
+
+
+int octgb_batch_process(octgb_ctx* c, int n_tiles, const octgb_tile* tiles, int dtype, float thr, int grab) {
+    return guarded(c, [&] {
+        if (!c->has_geom) throw Error(OCTGB_ERR_STATE, "octgb_set_geometry has not been called");
+        if (c->cancel.load()) throw Error(OCTGB_ERR_CANCELLED, "cancelled");
+        require(n_tiles >= 1 && n_tiles <= kMaxQueueTiles, "n_tiles must be in [1, 256]");
+        require(tiles != nullptr, "tiles is NULL");
+        require(grab >= 1 && grab <= 4096, "grab must be in [1, 4096]");
+        std::vector<QueueTile> qt(n_tiles);
+        unsigned int quads = 0;
+        int rows = 0;
+        for (int t = 0; t < n_tiles; ++t) {
+            const octgb_tile& d = tiles[t];
+            validate_raw(d.raw, dtype, OCTGB_DEVICE, d.B, d.interf, d.apod_size);
+            require(d.db != nullptr, "tile db is NULL");
+            require(d.plan_id >= 0 && d.plan_id < static_cast<int>(c->plans.size()), "bad plan id");
+            const Plan& p = *c->plans[d.plan_id];
+            require(p.n_tile_x == d.interf - d.apod_size, "A-scans per B-scan differ from the tile's plan");
+            require(p.lateral_quad_local,
+                    "a batched tile's plan must be a single-tile plan (output columns = the tile's A-scans)");
+            require(!p.opc, "the batched form does not take optical-path correction");
+            require(p.n_out_z <= 1600, "the batched form resamples to at most 1600 output rows per A-scan");
+            const int qpb = (d.interf - d.apod_size + kPerCta - 1) / kPerCta;
+            const unsigned int nq = static_cast<unsigned int>(static_cast<int64_t>(d.B) * qpb);
+            require(static_cast<uint64_t>(quads) + nq < (1ull << 31), "batch too large");
+            QueueTile& q = qt[t];
+            q.raw = d.raw;
+            q.out = d.db;
+            q.plan = c->plan_table.as<StitchDev>() + d.plan_id;
+            q.B = d.B;
+            q.interf = d.interf;
+            q.apod = d.apod_size;
+            q.nx = d.interf - d.apod_size;
+            q.nz = p.n_out_z;
+            q.apod_row0 = rows;
+            q.quad0 = quads;
+            q.nquads = nq;
+            q.qpb = qpb;
+            quads += nq;
+            rows += d.B;
+        }
+        if (quads == 0) return;
+        // the table changes only with the batch: upload when it differs (a
+        // graph captured after one call replays with the same table)
+        const bool same = c->qtiles_h.size() == qt.size() &&
+                          memcmp(c->qtiles_h.data(), qt.data(), qt.size() * sizeof(QueueTile)) == 0;
+        if (!same) {
+            require(!c->capturing, "first use of a tile table during graph capture: run the batch once first");
+            ck(c->qtiles.ensure(qt.size() * sizeof(QueueTile)), "cudaMalloc(tile table)");
+            ck(cudaMemcpyAsync(c->qtiles.p, qt.data(), qt.size() * sizeof(QueueTile), cudaMemcpyHostToDevice,
+                               c->stream),
+               "H2D tile table");
+            ck(cudaStreamSynchronize(c->stream), "sync tile table");
+            c->qtiles_h = qt;
+        }
+        ck(c->apod.ensure(static_cast<size_t>(rows) * kN * sizeof(float) + 16), "cudaMalloc(apod)");
+        ck(c->qcounter.ensure(sizeof(unsigned int)), "cudaMalloc(queue head)");
+        ck(c->run_mm.ensure(2 * sizeof(unsigned int)), "cudaMalloc(run mm)");
+        ck(cudaMemsetAsync(c->qcounter.p, 0, sizeof(unsigned int), c->stream), "memset queue head");
+        ck(launch_apod_mean_tiles(c->qtiles.as<QueueTile>(), n_tiles, rows, dtype, c->apod.as<float>(), c->stream),
+           "apod kernel");
+        c->launches++;
+        SpectralArgs a{};
+        a.n_seg = 1;
+        a.B = 1;
+        a.nx = 1;
+        a.apod_mean = c->apod.as<float>();
+        a.g.w = c->w.as<float>();
+        a.g.start = c->start.as<int>();
+        a.g.taps = c->taps;
+        a.g.win = c->win.as<float2>();
+        a.g.tw = c->tw.as<float2>();
+        a.g.wsh = c->wsh.as<float>();
+        a.g.s0 = c->s0.as<int>();
+        a.g.U = c->U;
+        a.minmax = c->run_mm.as<unsigned int>();
+        a.status = c->status_dev;
+        a.qt = c->qtiles.as<QueueTile>();
+        a.n_qt = n_tiles;
+        a.counter = c->qcounter.as<unsigned int>();
+        a.total_quads = quads;
+        a.grab = grab;
+        a.thr = thr;
+        int64_t grid = static_cast<int64_t>(c->num_sms) * spectral_max_ctas_per_sm(dtype, kModeResample);
+        if (grid > quads) grid = quads;
+        ck(launch_spectral(a, dtype, kModeResample, static_cast<int>(grid), c->stream), "spectral kernel");
+        c->launches++;
     });
 }
 

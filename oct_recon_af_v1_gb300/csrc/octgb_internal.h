@@ -18,7 +18,7 @@ constexpr int kThreads = kGroup * kPerCta;
 constexpr int kStatusOk = 0;
 constexpr int kStatusTimeout = 1;
 
-enum OutMode : int { kModeSpec = 0, kModeMag = 1, kModeDb = 2 };
+enum OutMode : int { kModeSpec = 0, kModeMag = 1, kModeDb = 2, kModeResample = 3 };
 
 constexpr int kBlk = 32;          // output rows / columns per stitch block
 constexpr int kMaxSeg = 32;       // tiles per multi-tile launch
@@ -34,6 +34,23 @@ struct DevGeometry {
     const float2* tw;     // [kN] exp(+2*pi*i*k/kN), rounded from float64
 };
 
+struct StitchDev;
+
+// One tile of the batched form: its raw B-scans, its depth operator (a stitch
+// plan with the identity lateral operator) and its dB output (A-scan major).
+struct QueueTile {
+    const void* raw;          // (B, interf, kN) device
+    float* out;               // (B * nx, nz) float32 dB
+    const StitchDev* plan;    // device pointer into the context's plan table
+    int B, interf, apod, nx, nz;
+    int apod_row0;            // first row of the tile in the apodisation-mean buffer
+    unsigned int quad0;       // first global quad (4 A-scans) of the tile
+    unsigned int nquads;      // B * qpb
+    int qpb;                  // quads per B-scan (quads never span two B-scans)
+    int pad_;
+};
+constexpr int kMaxQueueTiles = 256;
+
 struct SpectralArgs {
     const void* raw;          // (B, interf, kN), segment 0
     const void* seg[kMaxSeg]; // raw batches of n_seg tiles, each (B, interf, kN); seg[0] == raw
@@ -44,12 +61,22 @@ struct SpectralArgs {
     DevGeometry g;
     float* out;               // spec (M, kN, 2) | mag (M, kHalf) | db (M, nz)
     int z0, nz;               // depth crop (db mode)
-    unsigned int* minmax;     // [2] ordered-uint min / max (db mode), may be null
+    unsigned int* minmax;     // [2] ordered-uint min / max (db / resample modes), may be null
     int* status;              // device status word
+    // work-queue mode (resample): tiles of uneven size, quads taken from a counter
+    const QueueTile* qt;
+    int n_qt;
+    unsigned int* counter;    // queue head in quads, zero before the launch
+    unsigned int total_quads;
+    int grab;                 // quads taken per atomic grab
+    float thr;                // weight threshold (pipeline.py:296-297)
 };
 
 // spectral.cu
 cudaError_t launch_apod_mean(const SpectralArgs& a, int dtype, cudaStream_t st);
+// apodisation mean of every B-scan of the queue tiles (rows by tile.apod_row0)
+cudaError_t launch_apod_mean_tiles(const QueueTile* tiles_dev, int n_tiles, int total_rows, int dtype,
+                                   float* apod_mean, cudaStream_t st);
 cudaError_t launch_spectral(const SpectralArgs& a, int dtype, int mode, int grid, cudaStream_t st);
 int spectral_max_ctas_per_sm(int dtype, int mode);
 size_t spectral_smem_bytes(int dtype);

@@ -206,17 +206,81 @@ __device__ __forceinline__ void group_sync(int g) {
 // source window (d is stored skewed by one word per 32) and 4*U FMAs, summed
 // in the reference's tap order.  FFT: 128 threads per A-scan, radix 16,16,8
 // Stockham through the padded spec line, per-group named barriers.
+// Where slot s of quad q reads its raw row and apodisation row and writes
+// its result.  Static mode: quads of one batch (n_seg segments of B x nx
+// A-scans).  Queue mode: quads of the tile table (quad0 prefix in shared
+// memory, binary search).
+struct SlotRef {
+    const void* row;     // raw row (kN samples)
+    int64_t apod_row;    // row of the apodisation-mean buffer
+    int64_t as;          // static: global A-scan index; queue: A-scan index within the tile
+    int tile;            // queue: tile index
+    bool valid;
+};
+
+template <typename RawT, bool Queue>
+__device__ __forceinline__ SlotRef slot_ref(const SpectralArgs& a, const unsigned int* quad0_s, int64_t q, int s) {
+    SlotRef r;
+    if (!Queue) {
+        const int64_t as = q * kPerCta + s;
+        r.valid = as < a.n_ascans;
+        const int64_t asc = r.valid ? as : 0;
+        const int64_t bt = asc / a.nx, x = asc - bt * a.nx;   // bt = segment * B + b
+        const int sg = static_cast<int>(bt / a.B);
+        const int64_t b = bt - static_cast<int64_t>(sg) * a.B;
+        r.row = static_cast<const RawT*>(a.seg[sg]) + ((b * a.interf + a.apod + x) * kN);
+        r.apod_row = bt;
+        r.as = as;
+        r.tile = 0;
+    } else {
+        int lo = 0, hi = a.n_qt - 1;                // last tile with quad0 <= q
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (quad0_s[mid] <= static_cast<unsigned int>(q)) lo = mid; else hi = mid - 1;
+        }
+        const QueueTile& t = a.qt[lo];
+        const int64_t lq = q - t.quad0;
+        const int64_t b = lq / t.qpb;                  // quads are aligned to B-scans
+        const int qb = static_cast<int>(lq - b * t.qpb);
+        // the last quad of a B-scan ends on its last A-scan (it may repeat up
+        // to three A-scans of the previous quad), so both edge columns find
+        // their lateral neighbour in the same quad
+        const int xs = (qb == t.qpb - 1 && t.nx >= kPerCta) ? t.nx - kPerCta : qb * kPerCta;
+        const int64_t x = xs + s;
+        r.valid = x < t.nx;
+        const int64_t xc = r.valid ? x : 0;
+        r.row = static_cast<const RawT*>(t.raw) + ((b * t.interf + t.apod + xc) * kN);
+        r.apod_row = t.apod_row0 + b;
+        r.as = b * t.nx + x;                           // A-scan index within the tile
+        r.tile = lo;
+    }
+    return r;
+}
+
+// One CTA (512 threads) = 4 A-scans per iteration of a persistent loop.
+// Sinc: thread t owns output samples 4t..4t+3 of all four A-scans; its band
+// weights live in registers for the whole kernel in a shifted dense form
+// wr[r][u] (the weight of source sample s0_t + u for output 4t + r, zero
+// outside the band), so each A-scan costs U conflict-free shared loads of the
+// source window (d is stored skewed by one word per 32) and 4*U FMAs, summed
+// in the reference's tap order.  FFT: 128 threads per A-scan, radix 16,16,8
+// Stockham through the padded spec line, per-group named barriers.
+// Work: static grid-stride over one batch's quads, or (resample mode) quads
+// taken `grab` at a time from a device work queue spanning many tiles of
+// uneven size.
 template <typename RawT, int Mode, int U>
 __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) {
+    constexpr bool kQueue = Mode == kModeResample;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     Smem<RawT>& S = *reinterpret_cast<Smem<RawT>*>(smem_raw);
+    __shared__ int64_t qbuf[2];                        // quad held by each stage buffer (-1: none)
+    __shared__ unsigned int quad0_s[kQueue ? kMaxQueueTiles : 1];
 
     const int tid = threadIdx.x;
     const int g = tid / kGroup;        // A-scan slot of the iteration
     const int lt = tid % kGroup;       // thread within the A-scan group
     const int warp = tid / 32, lane = tid % 32;
-    const int64_t M = a.n_ascans;
-    const int64_t nquads = (M + kPerCta - 1) / kPerCta;
+    const int64_t nquads = kQueue ? static_cast<int64_t>(a.total_quads) : (a.n_ascans + kPerCta - 1) / kPerCta;
 
     // this thread's shifted sinc weights and source window base
     float wr[4][U];
@@ -242,6 +306,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
         S.mm[0] = 0xffffffffu;
         S.mm[1] = 0u;
     }
+    if (kQueue)
+        for (int k = tid; k < a.n_qt; k += kThreads) quad0_s[k] = a.qt[k].quad0;
     for (int k = tid; k < kPerCta * kTail; k += kThreads) S.d[k / kTail][skew(kN + k % kTail)] = 0.f;
     for (int k = tid; k < 16 * 16; k += kThreads) {
         const int r = k / 16, j = k % 16;
@@ -254,36 +320,58 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
     float run_min = __int_as_float(0x7f800000), run_max = -__int_as_float(0x7f800000);
     __syncthreads();
 
-    auto issue = [&](int64_t quad, int buf) {
-        const int64_t a0 = quad * kPerCta;
-        const int nvalid = static_cast<int>(M - a0 < kPerCta ? M - a0 : kPerCta);
-        mbar_expect_tx(&S.bar[buf], static_cast<uint32_t>(nvalid) * kN * sizeof(RawT));
-        for (int s = 0; s < nvalid; ++s) {
-            const int64_t as = a0 + s;
-            const int64_t bt = as / a.nx, x = as - bt * a.nx;   // bt = segment * B + b
-            const int sg = static_cast<int>(bt / a.B);
-            const int64_t b = bt - static_cast<int64_t>(sg) * a.B;
-            const RawT* src = static_cast<const RawT*>(a.seg[sg]) + ((b * a.interf + a.apod + x) * kN);
-            tma_bulk_g2s(&S.stage[buf][s][0], src, kN * sizeof(RawT), &S.bar[buf]);
+    // thread 0 owns the schedule: the next quad after `cur`
+    int64_t item_next = 0, item_end = 0;               // queue mode: current grab [next, end)
+    auto next_quad = [&](int64_t cur) -> int64_t {
+        if (!kQueue) {
+            const int64_t n = cur < 0 ? blockIdx.x : cur + gridDim.x;
+            return n < nquads ? n : -1;
         }
+        if (item_next < item_end) return item_next++;
+        const int64_t base = atomicAdd(a.counter, static_cast<unsigned int>(a.grab));
+        if (base >= nquads) return -1;
+        item_next = base + 1;
+        item_end = base + a.grab < nquads ? base + a.grab : nquads;
+        return base;
+    };
+    auto issue = [&](int64_t quad, int buf) {
+        int nvalid = 0;
+        SlotRef r[kPerCta];
+#pragma unroll
+        for (int k = 0; k < kPerCta; ++k) {
+            r[k] = slot_ref<RawT, kQueue>(a, quad0_s, quad, k);
+            nvalid += r[k].valid ? 1 : 0;
+        }
+        mbar_expect_tx(&S.bar[buf], static_cast<uint32_t>(nvalid) * kN * sizeof(RawT));
+#pragma unroll
+        for (int k = 0; k < kPerCta; ++k)
+            if (r[k].valid) tma_bulk_g2s(&S.stage[buf][k][0], r[k].row, kN * sizeof(RawT), &S.bar[buf]);
     };
 
-    if (tid == 0 && blockIdx.x < nquads) issue(blockIdx.x, 0);
+    if (tid == 0) {
+        const int64_t q0 = next_quad(-1);
+        qbuf[0] = q0;
+        if (q0 >= 0) issue(q0, 0);
+    }
+    __syncthreads();
 
-    int it = 0;
-    for (int64_t quad = blockIdx.x; quad < nquads; quad += gridDim.x, ++it) {
+    for (int it = 0;; ++it) {
         const int buf = it & 1;
-        const int64_t next = quad + gridDim.x;
-        if (tid == 0 && next < nquads) issue(next, buf ^ 1);
+        const int64_t quad = qbuf[buf];
+        if (quad < 0) break;
+        if (tid == 0) {
+            const int64_t nq = next_quad(quad);
+            qbuf[buf ^ 1] = nq;
+            if (nq >= 0) issue(nq, buf ^ 1);
+        }
 
         const bool ok = mbar_wait_bounded(&S.bar[buf], (it >> 1) & 1, a.status);
         if (__syncthreads_or(!ok)) return;
 
         // ---- (b) background: d = raw - apod, line mean (group g, A-scan g) ----
-        const int64_t as = quad * kPerCta + g;
-        const bool valid = as < M;
-        const int64_t bsc = valid ? as / a.nx : 0;
-        const float* apod = a.apod_mean + bsc * kN;
+        const SlotRef me = slot_ref<RawT, kQueue>(a, quad0_s, quad, g);
+        const bool valid = me.valid;
+        const float* apod = a.apod_mean + me.apod_row * kN;
         // d = raw - apod goes to shared memory now; the line mean m is
         // subtracted when the sinc loads its window (the same float32 value
         // d - m the reference stores, cpu_kernels.py:35-36)
@@ -330,7 +418,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
                     const float2 sp = make_float2(v * wre[r], v * wim[r]);
                     if (Mode == kModeSpec) {
                         // spec output undoes the 1/N ifft scaling folded into the window
-                        if (a0 + k < M)
+                        if (a0 + k < a.n_ascans)
                             reinterpret_cast<float2*>(a.out)[(a0 + k) * kN + i0 + r] =
                                 make_float2(sp.x * kN, sp.y * kN);
                     } else {
@@ -368,6 +456,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
             for (int r = 0; r < 16; ++r) X[pad(idxD + 16 * r)] = v[r];
             group_sync(g);
         }
+        float magv[2][4];
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
             const int j = lt + 128 * h;
@@ -378,30 +467,100 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
             for (int r = 1; r < 8; ++r) v[r] = cmul(v[r], S.tw3[r][j]);
             float2 Xk[4];
             dft8_low(v, Xk);
+#pragma unroll
+            for (int r = 0; r < 4; ++r) magv[h][r] = __fsqrt_rn(fmaf(Xk[r].x, Xk[r].x, Xk[r].y * Xk[r].y));
+        }
+        if (Mode == kModeMag || Mode == kModeDb) {
             if (valid) {
 #pragma unroll
-                for (int r = 0; r < 4; ++r) {
-                    const int k = j + 256 * r;
-                    const float mag = __fsqrt_rn(fmaf(Xk[r].x, Xk[r].x, Xk[r].y * Xk[r].y));
-                    if (Mode == kModeMag) {
-                        a.out[as * kHalf + k] = mag;
-                    } else {
-                        const int z = k - a.z0;
-                        if (z >= 0 && z < a.nz) {
-                            const float db = 20.0f * log10f(mag);
-                            a.out[as * a.nz + z] = db;
-                            if (isfinite(db)) {
-                                run_min = fminf(run_min, db);
-                                run_max = fmaxf(run_max, db);
+                for (int h = 0; h < 2; ++h)
+#pragma unroll
+                    for (int r = 0; r < 4; ++r) {
+                        const int k = lt + 128 * h + 256 * r;
+                        const float mag = magv[h][r];
+                        if (Mode == kModeMag) {
+                            a.out[me.as * kHalf + k] = mag;
+                        } else {
+                            const int z = k - a.z0;
+                            if (z >= 0 && z < a.nz) {
+                                const float db = 20.0f * log10f(mag);
+                                a.out[me.as * a.nz + z] = db;
+                                if (isfinite(db)) {
+                                    run_min = fminf(run_min, db);
+                                    run_max = fmaxf(run_max, db);
+                                }
                             }
                         }
+                    }
+            }
+        } else {
+            // ---- (g) resample: the tile's depth operator and focus weight per
+            // A-scan (u = Wz (a F)), then the lateral operator between the
+            // quad's A-scans (num = WxT u, den likewise), as
+            // TileStitcher.contribute for one tile (stitching.py:126-139), and
+            // finalise (pipeline.py:296-300).  The lateral operator of a single
+            // tile is the identity except for the reference's 1e-10 widening
+            // of its first node, which blends A-scan 1 into column 0 with a
+            // weight ~1e-7; quads are aligned to B-scans so that neighbour is
+            // always in this CTA (checked on the host for every column).
+            float* M = reinterpret_cast<float*>(X);        // |X[k]|, k < N/2, reuses the line
+            float* Uz = M + kHalf;                          // u[zo] of this A-scan
+            const QueueTile& tile = a.qt[me.tile];
+            const StitchDev& p = *tile.plan;
+            group_sync(g);
+#pragma unroll
+            for (int h = 0; h < 2; ++h)
+#pragma unroll
+                for (int r = 0; r < 4; ++r) M[lt + 128 * h + 256 * r] = magv[h][r];
+            group_sync(g);
+            for (int zo = lt; zo < tile.nz; zo += kGroup) {
+                const int zr = p.zr[zo];
+                float u = 0.f;
+                if (zr >= 0) {
+                    const bool has1 = zr + 1 < p.R;
+                    const float w0 = p.wz0[zo], w1 = p.wz1[zo];
+                    const float a0v = M[p.r0 + zr] * p.fz[zr];
+                    const float a1v = has1 ? M[p.r0 + zr + 1] * p.fz[zr + 1] : 0.f;
+                    u = fmaf(a1v, w1, a0v * w0);
+                }
+                Uz[zo] = u;
+            }
+            __syncthreads();                               // every A-scan of the quad has its u
+            if (valid) {
+                const int64_t x = me.as % tile.nx;
+                const int xq0 = static_cast<int>(x) - g;   // A-scan of slot 0
+                const int xr = p.xr[x];
+                const float wx0 = p.wx0[x], wx1 = p.wx1[x];
+                const int s0i = xr - xq0, s1i = xr + 1 - xq0;
+                const bool in0 = xr >= 0 && s0i >= 0 && s0i < kPerCta, in1 = xr >= 0 && s1i >= 0 && s1i < kPerCta;
+                const float* U0 = reinterpret_cast<const float*>(S.spec[in0 ? s0i : 0]) + kHalf;
+                const float* U1 = reinterpret_cast<const float*>(S.spec[in1 ? s1i : 0]) + kHalf;
+                float* out = tile.out + me.as * tile.nz;
+                for (int zo = lt; zo < tile.nz; zo += kGroup) {
+                    const int zr = p.zr[zo];
+                    float v = __int_as_float(0x7fc00000);
+                    if (zr >= 0 && xr >= 0) {
+                        const bool has1 = zr + 1 < p.R;
+                        const float w0 = p.wz0[zo], w1 = p.wz1[zo];
+                        const float f0 = p.fz[zr], f1 = has1 ? p.fz[zr + 1] : 0.f;
+                        const float d = fmaf(f1, w1, f0 * w0);
+                        const float u0 = in0 ? U0[zo] : 0.f, u1 = in1 ? U1[zo] : 0.f;
+                        const float d0 = in0 ? d : 0.f, d1 = in1 ? d : 0.f;
+                        const float num = fmaf(u1, wx1, u0 * wx0);
+                        const float den = fmaf(d1, wx1, d0 * wx0);
+                        if (!(den < a.thr) && !isnan(den)) v = 20.0f * log10f(__fdiv_rn(num, den));
+                    }
+                    out[zo] = v;
+                    if (isfinite(v)) {
+                        run_min = fminf(run_min, v);
+                        run_max = fmaxf(run_max, v);
                     }
                 }
             }
         }
     }
 
-    if (Mode == kModeDb && a.minmax != nullptr) {
+    if ((Mode == kModeDb || Mode == kModeResample) && a.minmax != nullptr) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             run_min = fminf(run_min, __shfl_xor_sync(0xffffffffu, run_min, o));
@@ -441,6 +600,32 @@ __global__ void k_apod_mean(const SpectralArgs a, float* __restrict__ out) {
     out[static_cast<int64_t>(bt) * kN + j] = static_cast<float>(s / apod);
 }
 
+// apodisation mean of the queue tiles: block row = global B-scan row
+template <typename RawT>
+__global__ void k_apod_mean_tiles(const QueueTile* __restrict__ tiles, int n_tiles, float* __restrict__ out) {
+    const int row = blockIdx.y;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    int lo = 0, hi = n_tiles - 1;              // last tile with apod_row0 <= row
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (tiles[mid].apod_row0 <= row) lo = mid; else hi = mid - 1;
+    }
+    const QueueTile& t = tiles[lo];
+    const int b = row - t.apod_row0;
+    if (b >= t.B || j >= kN) return;
+    const RawT* p = static_cast<const RawT*>(t.raw) + static_cast<int64_t>(b) * t.interf * kN + j;
+    double s;
+    if (sizeof(RawT) == 2) {
+        int acc = 0;
+        for (int k = 0; k < t.apod; ++k) acc += static_cast<int>(p[static_cast<int64_t>(k) * kN]);
+        s = static_cast<double>(acc);
+    } else {
+        s = 0.0;
+        for (int k = 0; k < t.apod; ++k) s += static_cast<double>(p[static_cast<int64_t>(k) * kN]);
+    }
+    out[static_cast<int64_t>(row) * kN + j] = static_cast<float>(s / t.apod);
+}
+
 template <typename RawT, int Mode, int U>
 cudaError_t launch_t(const SpectralArgs& a, int grid, cudaStream_t st) {
     const size_t smem = sizeof(Smem<RawT>);
@@ -466,6 +651,7 @@ cudaError_t launch_mode(const SpectralArgs& a, int mode, int grid, cudaStream_t 
     switch (mode) {
         case kModeSpec: return launch_u<RawT, kModeSpec>(a, grid, st);
         case kModeMag: return launch_u<RawT, kModeMag>(a, grid, st);
+        case kModeResample: return launch_u<RawT, kModeResample>(a, grid, st);
         default: return launch_u<RawT, kModeDb>(a, grid, st);
     }
 }
@@ -481,6 +667,19 @@ cudaError_t launch_apod_mean(const SpectralArgs& a, int dtype, cudaStream_t st) 
         k_apod_mean<int16_t><<<grid, 256, 0, st>>>(a, out);
     else
         k_apod_mean<float><<<grid, 256, 0, st>>>(a, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_apod_mean_tiles(const QueueTile* tiles_dev, int n_tiles, int total_rows, int dtype,
+                                   float* apod_mean, cudaStream_t st) {
+    if (total_rows == 0) return cudaSuccess;
+    const dim3 grid(kN / 256, total_rows);
+    if (dtype == 0)
+        k_apod_mean_tiles<uint16_t><<<grid, 256, 0, st>>>(tiles_dev, n_tiles, apod_mean);
+    else if (dtype == 1)
+        k_apod_mean_tiles<int16_t><<<grid, 256, 0, st>>>(tiles_dev, n_tiles, apod_mean);
+    else
+        k_apod_mean_tiles<float><<<grid, 256, 0, st>>>(tiles_dev, n_tiles, apod_mean);
     return cudaGetLastError();
 }
 
