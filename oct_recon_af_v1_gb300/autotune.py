@@ -1,0 +1,53 @@
+"""Launch-shape autotuner for the batched form (octgb_batch_process).
+
+The persistent spectral kernel takes `grab` groups of 4 A-scans per atomic
+operation on the work queue: small grabs balance load across SMs at the end
+of the batch, large grabs cut queue traffic and keep each CTA on one tile
+(fewer tile switches and depth-table reloads).  The order of the tile table
+decides which tiles meet at the end of the queue.  `tune_batch` times every
+candidate (grab, order) on the actual batch with CUDA events on the launching
+stream, keeps the fastest, and caches it per batch signature (tile count and
+total A-scans, bucketed) for the life of the process.
+"""
+from __future__ import annotations
+
+import math
+
+_CACHE: dict = {}
+GRABS = (1, 2, 4, 8, 16, 32)
+ORDERS = ("given", "largest_first")
+
+
+def signature(tiles) -> tuple:
+    total = sum(int(r.shape[0]) * (int(r.shape[1]) - int(apod)) for r, apod, _, _ in tiles)
+    return len(tiles), int(round(math.log2(max(total, 1)) * 4))
+
+
+def ordered(tiles, order: str):
+    if order == "largest_first":
+        return sorted(tiles, key=lambda t: -int(t[0].shape[0]) * (int(t[0].shape[1]) - int(t[1])))
+    return list(tiles)
+
+
+def tune_batch(ctx, tiles, threshold: float, stream, reps: int = 2, grabs=GRABS, orders=ORDERS):
+    """Return (grab, order, table of timings in ms) for this batch."""
+    import torch
+    sig = signature(tiles)
+    if sig in _CACHE:
+        return _CACHE[sig]
+    timings = {}
+    for order in orders:
+        work = ordered(tiles, order)
+        for grab in grabs:
+            ctx.batch_process(work, threshold, grab=grab)          # warm (tile table upload, caches)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            for _ in range(reps):
+                ctx.batch_process(work, threshold, grab=grab)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            timings[(grab, order)] = e0.elapsed_time(e1) / reps
+    best = min(timings, key=timings.get)
+    _CACHE[sig] = (best[0], best[1], {f"{g}/{o}": round(t, 3) for (g, o), t in timings.items()})
+    return _CACHE[sig]

@@ -25,9 +25,15 @@ namespace {
 struct DevBuf {
     void* p = nullptr;
     size_t cap = 0;
+    // once a captured graph may hold p, growing keeps the old allocation
+    // alive (until release) instead of freeing it under the graph
+    bool keep_old = false;
+    std::vector<void*> retired;
     cudaError_t ensure(size_t bytes) {
         if (bytes <= cap) return cudaSuccess;
-        if (p) cudaFree(p);
+        if (p) {
+            if (keep_old) retired.push_back(p); else cudaFree(p);
+        }
         p = nullptr;
         cap = 0;
         cudaError_t e = cudaMalloc(&p, bytes);
@@ -36,6 +42,8 @@ struct DevBuf {
     }
     void release() {
         if (p) cudaFree(p);
+        for (void* q : retired) cudaFree(q);
+        retired.clear();
         p = nullptr;
         cap = 0;
     }
@@ -96,6 +104,16 @@ struct SlotTable {
     }
 };
 
+// A device tile table of the batched form.  A graph captured over a batch
+// call holds the table's address, so a table is never overwritten once a
+// capture used it (pinned); unpinned tables are recycled least recently used.
+struct QTable {
+    std::vector<QueueTile> key;  // the uploaded contents
+    DevBuf buf;
+    bool pinned = false;
+    uint64_t last_use = 0;
+};
+
 struct Error : std::exception {
     int code;
     std::string msg;
@@ -133,8 +151,9 @@ struct octgb_ctx {
     bool capturing = false;
     int64_t capture_launch0 = 0;
     DevBuf magbuf, dbbuf, planemm, segs, qtable;
-    DevBuf qtiles, qcounter;                 // batched form: tile table and queue head
-    std::vector<QueueTile> qtiles_h;         // the table last uploaded
+    DevBuf qcounter;                         // batched form: queue head
+    std::vector<QTable*> qtables;            // batched form: device tile tables by content
+    uint64_t qtable_clock = 0;
     std::vector<SlotTable*> slot_tables;
     // host-input staging of the frame API: a copy stream and a ring of device
     // slots, so the copy of one batch overlaps the kernels of the previous one
@@ -347,6 +366,43 @@ const SlotTable& slot_table(octgb_ctx* c, int n_tiles, const int* plan_ids, int 
     return *t;
 }
 
+// The device copy of a batched-form tile table.  Tables are kept by content:
+// a batch repeated with the same tiles reuses its table, a table used while a
+// graph is captured is pinned (the graph replays with its address), and at
+// most kMaxFreeTables unpinned tables are kept, the least recently used one
+// being overwritten (in stream order, after every kernel that read it).
+constexpr int kMaxFreeTables = 8;
+
+const QueueTile* tile_table(octgb_ctx* c, const std::vector<QueueTile>& qt) {
+    const size_t bytes = qt.size() * sizeof(QueueTile);
+    ++c->qtable_clock;
+    for (QTable* t : c->qtables)
+        if (t->key.size() == qt.size() && memcmp(t->key.data(), qt.data(), bytes) == 0) {
+            t->last_use = c->qtable_clock;
+            if (c->capturing) t->pinned = true;
+            return t->buf.as<QueueTile>();
+        }
+    require(!c->capturing, "first use of a tile table during graph capture: run the batch once first");
+    QTable* t = nullptr;
+    int n_free = 0;
+    for (QTable* u : c->qtables)
+        if (!u->pinned) {
+            ++n_free;
+            if (t == nullptr || u->last_use < t->last_use) t = u;
+        }
+    if (n_free < kMaxFreeTables) {
+        t = new QTable();
+        c->qtables.push_back(t);
+    }
+    t->key.clear();                       // a failed upload leaves no matching entry
+    ck(t->buf.ensure(static_cast<size_t>(kMaxQueueTiles) * sizeof(QueueTile)), "cudaMalloc(tile table)");
+    t->key = qt;
+    t->last_use = c->qtable_clock;
+    // from pageable memory: the call returns once the source is staged
+    ck(cudaMemcpyAsync(t->buf.p, t->key.data(), bytes, cudaMemcpyHostToDevice, c->stream), "H2D tile table");
+    return t->buf.as<QueueTile>();
+}
+
 }  // namespace
 
 extern "C" {
@@ -398,8 +454,12 @@ int octgb_destroy(octgb_ctx* c) {
     }
     for (DevBuf* b : {&c->w, &c->start, &c->win, &c->tw, &c->wsh, &c->s0, &c->raw, &c->apod, &c->out, &c->mm, &c->frames, &c->num,
                       &c->den, &c->plan_table, &c->run_mm, &c->magbuf, &c->dbbuf, &c->planemm, &c->segs, &c->qtable,
-                      &c->qtiles, &c->qcounter})
+                      &c->qcounter})
         b->release();
+    for (QTable* t : c->qtables) {
+        t->buf.release();
+        delete t;
+    }
     for (cudaGraphExec_t g : c->graphs)
         if (g) cudaGraphExecDestroy(g);
     for (SlotTable* t : c->slot_tables) {
@@ -1040,6 +1100,12 @@ int octgb_graph_end(octgb_ctx* c, int* graph_id) {
         ck(e, "cudaGraphInstantiate");
         c->graphs.push_back(ge);
         c->graph_kernels.push_back(c->launches.load() - c->capture_launch0);
+        // the graph holds the addresses of the context's buffers: from now on
+        // a buffer that grows keeps its old allocation until octgb_destroy
+        for (DevBuf* b : {&c->raw, &c->apod, &c->out, &c->mm, &c->frames, &c->num, &c->den, &c->plan_table,
+                          &c->run_mm, &c->magbuf, &c->dbbuf, &c->planemm, &c->segs, &c->qtable, &c->qcounter})
+            b->keep_old = true;
+        for (int k = 0; k < octgb_ctx::kRing; ++k) c->ring[k].keep_old = true;
         c->launches.store(c->capture_launch0);
         *graph_id = static_cast<int>(c->graphs.size() - 1);
     });
@@ -1097,24 +1163,12 @@ int octgb_batch_process(octgb_ctx* c, int n_tiles, const octgb_tile* tiles, int 
             rows += d.B;
         }
         if (quads == 0) return;
-        // the table changes only with the batch: upload when it differs (a
-        // graph captured after one call replays with the same table)
-        const bool same = c->qtiles_h.size() == qt.size() &&
-                          memcmp(c->qtiles_h.data(), qt.data(), qt.size() * sizeof(QueueTile)) == 0;
-        if (!same) {
-            require(!c->capturing, "first use of a tile table during graph capture: run the batch once first");
-            ck(c->qtiles.ensure(qt.size() * sizeof(QueueTile)), "cudaMalloc(tile table)");
-            ck(cudaMemcpyAsync(c->qtiles.p, qt.data(), qt.size() * sizeof(QueueTile), cudaMemcpyHostToDevice,
-                               c->stream),
-               "H2D tile table");
-            ck(cudaStreamSynchronize(c->stream), "sync tile table");
-            c->qtiles_h = qt;
-        }
+        const QueueTile* qdev = tile_table(c, qt);
         ck(c->apod.ensure(static_cast<size_t>(rows) * kN * sizeof(float) + 16), "cudaMalloc(apod)");
         ck(c->qcounter.ensure(sizeof(unsigned int)), "cudaMalloc(queue head)");
         ck(c->run_mm.ensure(2 * sizeof(unsigned int)), "cudaMalloc(run mm)");
         ck(cudaMemsetAsync(c->qcounter.p, 0, sizeof(unsigned int), c->stream), "memset queue head");
-        ck(launch_apod_mean_tiles(c->qtiles.as<QueueTile>(), n_tiles, rows, dtype, c->apod.as<float>(), c->stream),
+        ck(launch_apod_mean_tiles(qdev, n_tiles, rows, dtype, c->apod.as<float>(), c->stream),
            "apod kernel");
         c->launches++;
         SpectralArgs a{};
@@ -1132,7 +1186,7 @@ int octgb_batch_process(octgb_ctx* c, int n_tiles, const octgb_tile* tiles, int 
         a.g.U = c->U;
         a.minmax = c->run_mm.as<unsigned int>();
         a.status = c->status_dev;
-        a.qt = c->qtiles.as<QueueTile>();
+        a.qt = qdev;
         a.n_qt = n_tiles;
         a.counter = c->qcounter.as<unsigned int>();
         a.total_quads = quads;

@@ -247,11 +247,14 @@ __device__ __forceinline__ SlotRef slot_ref(const SpectralArgs& a, const unsigne
         // their lateral neighbour in the same quad
         const int xs = (qb == t.qpb - 1 && t.nx >= kPerCta) ? t.nx - kPerCta : qb * kPerCta;
         const int64_t x = xs + s;
-        r.valid = x < t.nx;
+        // a quad outside this tile's range (only possible with a table that
+        // does not match total_quads) reads and writes nothing
+        r.valid = x < t.nx && lq >= 0 && lq < static_cast<int64_t>(t.nquads);
         const int64_t xc = r.valid ? x : 0;
-        r.row = static_cast<const RawT*>(t.raw) + ((b * t.interf + t.apod + xc) * kN);
-        r.apod_row = t.apod_row0 + b;
-        r.as = b * t.nx + x;                           // A-scan index within the tile
+        const int64_t bc = r.valid ? b : 0;
+        r.row = static_cast<const RawT*>(t.raw) + ((bc * t.interf + t.apod + xc) * kN);
+        r.apod_row = t.apod_row0 + bc;
+        r.as = bc * t.nx + xc;                         // A-scan index within the tile
         r.tile = lo;
     }
     return r;

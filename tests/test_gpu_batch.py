@@ -108,3 +108,40 @@ def test_batch_close_to_oracle(gpu_ctx):
         # float32 spectra of two FFTs: dB agree within a few 1e-3 except at deep nulls
         err = np.abs(got[fin] - ref[fin])
         assert np.quantile(err, 0.999) < 5e-3 and err.max() < 0.5
+
+
+def test_graph_replay_survives_other_batches(gpu_ctx):
+    """A graph captured over a batch keeps replaying that batch after other
+    batches (single tiles, a larger raw batch) ran on the same context: its
+    tile table and buffers are never overwritten or freed under it."""
+    torch = pytest.importorskip("torch")
+    from oct_recon_af_v1_gb300 import stitching as S
+    sg, tiles = _tiles(gpu_ctx, torch, SPECS, seed=80)
+    thr = S.min_weight_threshold(np.float32)
+    work = [(t["raw"], 25, t["plan"], t["db"]) for t in tiles]
+    stream = torch.cuda.Stream()
+    gpu_ctx.set_stream(stream.cuda_stream)
+    try:
+        gpu_ctx.batch_process(work, thr, grab=4)
+        gpu_ctx.synchronize()
+        got = [t["db"].cpu().numpy().copy() for t in tiles]
+        gpu_ctx.graph_begin()
+        gpu_ctx.batch_process(work, thr, grab=4)
+        gid = gpu_ctx.graph_end()
+        # more distinct tables than the context keeps unpinned, and a batch
+        # with more apodisation rows than the captured one (the apod buffer grows)
+        for rep in range(3):
+            for w in work:
+                gpu_ctx.batch_process([w], thr, grab=1 + rep)
+            gpu_ctx.batch_process(work[::-1], thr, grab=2)
+            gpu_ctx.batch_process(work + work[:2], thr, grab=3)
+        gpu_ctx.synchronize()
+        for t in tiles:
+            t["db"].fill_(-1.0)
+        torch.cuda.synchronize()
+        gpu_ctx.graph_launch(gid)
+        gpu_ctx.synchronize()
+        for t, g in zip(tiles, got):
+            np.testing.assert_array_equal(t["db"].cpu().numpy(), g)
+    finally:
+        gpu_ctx.set_stream(None)
