@@ -216,6 +216,38 @@ typedef struct octgb_tile {
 int octgb_batch_process(octgb_ctx *ctx, int n_tiles, const octgb_tile *tiles, int raw_dtype, float threshold,
                         int grab);
 
+/* ---------------------------------------------------------------- estimation */
+
+/* Dispersion scorer (DispersionScorer, octrecon/estimation/dispersion.py:66-107).
+ * octgb_disp_load replaces the constructor's linearisation (:80-85): the
+ * context's geometry must be the dispersion-free one with a window of ones
+ * (octgb_set_geometry with window = 1 + 0i), so the spectral stage yields the
+ * plain linearised interferogram (SpectralProcessor.linearise, core/spectral.py:
+ * 118-134), which is multiplied by hann (n doubles, Hann/rms) in float64 and
+ * rounded once to float32 (dispersion.py:84).  raw holds n_bscans x rep
+ * B-scans, repeats of one B-scan consecutive.  The result stays on the device. */
+int octgb_disp_load(octgb_ctx *ctx, const void *raw, int raw_dtype, int raw_loc, int n_bscans, int rep, int interf,
+                    int apod_size, const double *hann);
+/* dk2[j] = (k_eq[j] - mean(k_eq))^2, n doubles (dispersion.py:78-79). */
+int octgb_disp_set_dk2(octgb_ctx *ctx, const double *dk2);
+/* Score n_beta candidate betas on loaded B-scans b0 .. b0+nb-1 in one launch
+ * (DispersionScorer.magnitude + _metric, dispersion.py:46-63,91-107): phase
+ * exp(-i beta dk2) formed in float64 and rounded to complex64, inverse FFT,
+ * |.| of the first n/2 bins, mean over repeats.  metric: 0 none, 1
+ * top_percentile (log of the mean of the top_k largest I = A^2 over depths >=
+ * z_min; the reference's top_k = max(1, int(nX (n/2 - z_min) * 0.01))), 2
+ * kurtosis, 3 entropy, 4 legacy_peak.  scores: host (n_beta, nb) doubles, or
+ * NULL with metric 0.  mag (optional): the magnitudes (n_beta, nb, nX, n/2)
+ * float32 at mag_loc.  Synchronises. */
+int octgb_disp_eval(octgb_ctx *ctx, int n_beta, const double *betas, int b0, int nb, int metric, int64_t top_k,
+                    int z_min, double *scores, float *mag, int mag_loc);
+/* Median over x of every depth column of (n_frames, nx, nz) float32
+ * magnitudes, as float64 (numpy.median(..., axis=x) of focus.py:146,156;
+ * ignore_nan = 1 gives numpy.nanmedian, focus.py:215,255): out is host
+ * (n_frames, nz) doubles.  nx <= 4096.  Synchronises. */
+int octgb_xmedian(octgb_ctx *ctx, const float *mag, int mag_loc, int n_frames, int nx, int nz, int ignore_nan,
+                  double *out);
+
 /* ---------------------------------------------------------------- allocation-free */
 
 /* The magnitude of octgb_magnitude for callers that cannot allocate GPU

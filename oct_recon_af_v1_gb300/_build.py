@@ -17,7 +17,7 @@ CSRC = PKG / "csrc"
 OUT_DIR = PKG / "_lib"
 LIB = OUT_DIR / "liboctgb.so"
 INCLUDE = PKG.parent / "include"
-SOURCES = ["api.cu", "spectral.cu", "stitch.cu"]
+SOURCES = ["api.cu", "spectral.cu", "stitch.cu", "estimate.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3",
               "--expt-relaxed-constexpr", "-I", str(INCLUDE), "-I", str(CSRC)]
@@ -31,7 +31,7 @@ def nvcc() -> str:
 
 
 def _inputs():
-    files = [CSRC / s for s in SOURCES] + list(CSRC.glob("*.h")) + list(INCLUDE.glob("*.h"))
+    files = [CSRC / s for s in SOURCES] + list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + list(INCLUDE.glob("*.h"))
     files.append(Path(__file__))
     return files
 

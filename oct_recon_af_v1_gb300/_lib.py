@@ -51,6 +51,11 @@ SIGNATURES = {
     "octgb_graph_launch": (c_int, [c_void_p, c_int]),
     "octgb_magnitude_noalloc": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_void_p]),
     "octgb_batch_process": (c_int, [c_void_p, c_int, c_void_p, c_int, c_float, c_int]),
+    "octgb_disp_load": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_int, c_int, c_void_p]),
+    "octgb_disp_set_dk2": (c_int, [c_void_p, c_void_p]),
+    "octgb_disp_eval": (c_int, [c_void_p, c_int, c_void_p, c_int, c_int, c_int, c_int64, c_int, c_void_p,
+                                c_void_p, c_int]),
+    "octgb_xmedian": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_int, c_void_p]),
 }
 
 
@@ -214,6 +219,44 @@ class Context:
         self._check(self.lib.octgb_db(self.h, p, dt, loc, B, interf, apod_size, int(z0), int(nz), op, oloc,
                                       mm.ctypes.data if minmax else None))
         return out, (float(mm[0]), float(mm[1]))
+
+    # -------------------------------------------------------------- estimation
+    def disp_load(self, raw, apod_size: int, n_bscans: int, rep: int, hann: np.ndarray, raw_dtype=None):
+        """Linearise + Hann/rms-window n_bscans x rep B-scans once (the geometry must
+        carry a window of ones)."""
+        raw, p, loc, dt, B, interf = self._raw_args(raw, apod_size, raw_dtype)
+        if B != n_bscans * rep:
+            raise ValueError("raw must hold n_bscans x rep B-scans")
+        h = np.ascontiguousarray(hann, dtype=np.float64)
+        self._check(self.lib.octgb_disp_load(self.h, p, dt, loc, int(n_bscans), int(rep), interf, int(apod_size),
+                                             h.ctypes.data))
+
+    def disp_set_dk2(self, dk2: np.ndarray):
+        d = np.ascontiguousarray(dk2, dtype=np.float64)
+        self._check(self.lib.octgb_disp_set_dk2(self.h, d.ctypes.data))
+
+    def disp_eval(self, betas, b0: int, nb: int, metric: int, top_k: int = 0, z_min: int = 20, mag=None):
+        """Scores (n_beta, nb) float64 (None with metric 0); mag (optional) receives the
+        magnitudes (n_beta, nb, nX, N/2) float32 (numpy array or CUDA tensor)."""
+        b = np.ascontiguousarray(np.atleast_1d(np.asarray(betas, dtype=np.float64)))
+        scores = np.empty((len(b), nb), np.float64) if metric else None
+        mp, mloc = (None, HOST) if mag is None else _ptr(mag)
+        self._check(self.lib.octgb_disp_eval(self.h, len(b), b.ctypes.data, int(b0), int(nb), int(metric),
+                                             int(top_k), int(z_min),
+                                             None if scores is None else scores.ctypes.data, mp, mloc))
+        return scores
+
+    def xmedian(self, mag, ignore_nan: bool = False) -> np.ndarray:
+        """numpy.median / nanmedian over x of (frames, nX, nZ) float32 -> (frames, nZ) float64."""
+        if isinstance(mag, np.ndarray):
+            mag = np.ascontiguousarray(mag, dtype=np.float32)
+        elif not mag.is_contiguous():
+            mag = mag.contiguous()
+        F, nx, nz = mag.shape
+        p, loc = _ptr(mag)
+        out = np.empty((F, nz), np.float64)
+        self._check(self.lib.octgb_xmedian(self.h, p, loc, F, nx, nz, int(bool(ignore_nan)), out.ctypes.data))
+        return out
 
     # -------------------------------------------------------------- quantisation
     def quantise(self, db, clim, out=None):

@@ -14,6 +14,8 @@
 #include <exception>
 #include <string>
 #include <vector>
+#include <cmath>
+#include <algorithm>
 
 #include "../../include/octgb.h"
 #include "octgb_internal.h"
@@ -152,6 +154,11 @@ struct octgb_ctx {
     int64_t capture_launch0 = 0;
     DevBuf magbuf, dbbuf, planemm, segs, qtable;
     DevBuf qcounter;                         // batched form: queue head
+    // dispersion scorer and focus profiles
+    bool win_is_one = false;                 // geometry window is exactly 1 (plain linearisation)
+    DevBuf disp_x, disp_hann, disp_phase, disp_a, disp_score, xmed;
+    int disp_b = 0, disp_rep = 0, disp_nx = 0;
+    std::vector<double> dk2;
     std::vector<QTable*> qtables;            // batched form: device tile tables by content
     uint64_t qtable_clock = 0;
     std::vector<SlotTable*> slot_tables;
@@ -454,7 +461,7 @@ int octgb_destroy(octgb_ctx* c) {
     }
     for (DevBuf* b : {&c->w, &c->start, &c->win, &c->tw, &c->wsh, &c->s0, &c->raw, &c->apod, &c->out, &c->mm, &c->frames, &c->num,
                       &c->den, &c->plan_table, &c->run_mm, &c->magbuf, &c->dbbuf, &c->planemm, &c->segs, &c->qtable,
-                      &c->qcounter})
+                      &c->qcounter, &c->disp_x, &c->disp_hann, &c->disp_phase, &c->disp_a, &c->disp_score, &c->xmed})
         b->release();
     for (QTable* t : c->qtables) {
         t->buf.release();
@@ -587,6 +594,9 @@ int octgb_set_geometry(octgb_ctx* c, int n, int taps, const int64_t* idx, const 
         c->U = U;
         c->taps = taps;
         c->has_geom = true;
+        c->win_is_one = true;
+        for (int i = 0; i < kN; ++i)
+            if (window[2 * i] != 1.0 || window[2 * i + 1] != 0.0) c->win_is_one = false;
     });
 }
 
@@ -1103,7 +1113,8 @@ int octgb_graph_end(octgb_ctx* c, int* graph_id) {
         // the graph holds the addresses of the context's buffers: from now on
         // a buffer that grows keeps its old allocation until octgb_destroy
         for (DevBuf* b : {&c->raw, &c->apod, &c->out, &c->mm, &c->frames, &c->num, &c->den, &c->plan_table,
-                          &c->run_mm, &c->magbuf, &c->dbbuf, &c->planemm, &c->segs, &c->qtable, &c->qcounter})
+                          &c->run_mm, &c->magbuf, &c->dbbuf, &c->planemm, &c->segs, &c->qtable, &c->qcounter,
+                          &c->disp_x, &c->disp_hann, &c->disp_phase, &c->disp_a, &c->disp_score, &c->xmed})
             b->keep_old = true;
         for (int k = 0; k < octgb_ctx::kRing; ++k) c->ring[k].keep_old = true;
         c->launches.store(c->capture_launch0);
@@ -1196,6 +1207,143 @@ int octgb_batch_process(octgb_ctx* c, int n_tiles, const octgb_tile* tiles, int 
         if (grid > quads) grid = quads;
         ck(launch_spectral(a, dtype, kModeResample, static_cast<int>(grid), c->stream), "spectral kernel");
         c->launches++;
+    });
+}
+
+// ---------------------------------------------------------------------------
+// Dispersion scorer (octrecon/estimation/dispersion.py:66-107) and focus
+// depth profiles (octrecon/estimation/focus.py:146,156,255).
+
+int octgb_disp_load(octgb_ctx* c, const void* raw, int dtype, int loc, int n_bscans, int rep, int interf, int apod,
+                    const double* hann) {
+    return guarded(c, [&] {
+        validate_raw(raw, dtype, loc, n_bscans, interf, apod);
+        require(c->has_geom && c->win_is_one,
+                "octgb_disp_load needs the dispersion-free geometry with a window of ones (plain linearisation)");
+        require(n_bscans >= 1 && rep >= 1, "n_bscans and rep must be >= 1");
+        require(hann != nullptr, "hann is NULL");
+        const int B = n_bscans * rep, nx = interf - apod;
+        const size_t lines = static_cast<size_t>(B) * nx;
+        // linearised interferogram (window 1: the kernel's output is sum + m),
+        // then windowed in float64 and rounded once, as
+        // (eq * hann).astype(complex64) (dispersion.py:84)
+        ck(c->out.ensure(lines * kN * sizeof(float2)), "cudaMalloc(spec)");
+        run_spectral(c, raw, dtype, loc, B, interf, apod, kModeSpec, c->out.as<float>(), 0, 0, nullptr);
+        ck(c->disp_x.ensure(lines * kN * sizeof(float)), "cudaMalloc(X)");
+        ck(c->disp_hann.ensure(kN * sizeof(double)), "cudaMalloc(hann)");
+        ck(cudaMemcpyAsync(c->disp_hann.p, hann, kN * sizeof(double), cudaMemcpyHostToDevice, c->stream), "H2D hann");
+        ck(launch_window_pack(c->out.as<float2>(), c->disp_hann.as<double>(), static_cast<int64_t>(lines),
+                              c->disp_x.as<float>(), c->stream),
+           "window kernel");
+        c->launches++;
+        check_status(c);
+        c->disp_b = n_bscans;
+        c->disp_rep = rep;
+        c->disp_nx = nx;
+    });
+}
+
+int octgb_disp_set_dk2(octgb_ctx* c, const double* dk2) {
+    return guarded(c, [&] {
+        require(dk2 != nullptr, "dk2 is NULL");
+        c->dk2.assign(dk2, dk2 + kN);
+    });
+}
+
+int octgb_disp_eval(octgb_ctx* c, int n_beta, const double* betas, int b0, int nb, int metric, int64_t top_k,
+                    int z_min, double* scores, float* mag, int mag_loc) {
+    return guarded(c, [&] {
+        require(c->disp_b > 0, "octgb_disp_load has not been called");
+        require(static_cast<int>(c->dk2.size()) == kN, "octgb_disp_set_dk2 has not been called");
+        require(n_beta >= 1 && betas != nullptr, "no betas");
+        require(b0 >= 0 && nb >= 1 && b0 + nb <= c->disp_b, "B-scan range outside the loaded B-scans");
+        require(metric >= 0 && metric <= 4, "metric must be 0 (none) .. 4");
+        require(metric == 0 || scores != nullptr, "scores is NULL");
+        require(metric != 1 || (top_k >= 1 && top_k <= static_cast<int64_t>(c->disp_nx) * (kHalf - z_min)),
+                "top_k out of range");
+        require(z_min >= 0 && z_min < kHalf, "z_min must be in [0, N/2)");
+        require(metric != 0 || mag != nullptr, "nothing to compute (metric 0 and no magnitude output)");
+        if (c->cancel.load()) throw Error(OCTGB_ERR_CANCELLED, "cancelled");
+        const int nx = c->disp_nx;
+        const size_t seg_floats = static_cast<size_t>(nx) * kHalf;
+        // betas in chunks whose magnitudes fit a 1 GiB scratch (unless written to the caller's device buffer)
+        const int per = mag != nullptr && mag_loc == OCTGB_DEVICE
+                            ? n_beta
+                            : std::max(1, static_cast<int>((size_t(1) << 30) / (seg_floats * nb * sizeof(float))));
+        std::vector<float2> ph(static_cast<size_t>(std::min(per, n_beta)) * kN);
+        ck(c->disp_score.ensure(static_cast<size_t>(n_beta) * nb * sizeof(double)), "cudaMalloc(scores)");
+        for (int g0 = 0; g0 < n_beta; g0 += per) {
+            const int ng = std::min(per, n_beta - g0);
+            // exp(-i beta dk^2) in float64, rounded to complex64 (dispersion.py:88-89), times 1/N
+            for (int gi = 0; gi < ng; ++gi) {
+                const double beta = betas[g0 + gi];
+                for (int j = 0; j < kN; ++j) {
+                    const double t = beta * c->dk2[j];
+                    ph[static_cast<size_t>(gi) * kN + j] =
+                        make_float2(static_cast<float>(std::cos(t)) * (1.0f / kN),
+                                    static_cast<float>(-std::sin(t)) * (1.0f / kN));
+                }
+            }
+            ck(c->disp_phase.ensure(static_cast<size_t>(per) * kN * sizeof(float2)), "cudaMalloc(phase)");
+            ck(cudaMemcpyAsync(c->disp_phase.p, ph.data(), static_cast<size_t>(ng) * kN * sizeof(float2),
+                               cudaMemcpyHostToDevice, c->stream),
+               "H2D phase");
+            float* A = nullptr;
+            if (mag != nullptr && mag_loc == OCTGB_DEVICE) {
+                A = mag + static_cast<size_t>(g0) * nb * seg_floats;
+            } else {
+                ck(c->disp_a.ensure(static_cast<size_t>(per) * nb * seg_floats * sizeof(float)), "cudaMalloc(A)");
+                A = c->disp_a.as<float>();
+            }
+            DispArgs a{};
+            a.X = c->disp_x.as<float>();
+            a.phase = c->disp_phase.as<float2>();
+            a.tw = c->tw.as<float2>();
+            a.A = A;
+            a.n_beta = ng;
+            a.nb = nb;
+            a.b0 = b0;
+            a.nx = nx;
+            a.rep = c->disp_rep;
+            ck(launch_disp_mag(a, c->num_sms, c->stream), "dispersion magnitude kernel");
+            c->launches++;
+            if (metric != 0) {
+                ck(launch_disp_metric(A, ng * nb, nx, z_min, metric, static_cast<unsigned int>(top_k),
+                                      c->disp_score.as<double>() + static_cast<size_t>(g0) * nb, c->stream),
+                   "dispersion metric kernel");
+                c->launches++;
+            }
+            if (mag != nullptr && mag_loc != OCTGB_DEVICE)
+                copy_out(c, mag + static_cast<size_t>(g0) * nb * seg_floats, OCTGB_HOST, A,
+                         static_cast<size_t>(ng) * nb * seg_floats * sizeof(float));
+        }
+        if (metric != 0)
+            ck(cudaMemcpyAsync(scores, c->disp_score.p, static_cast<size_t>(n_beta) * nb * sizeof(double),
+                               cudaMemcpyDeviceToHost, c->stream),
+               "D2H scores");
+        check_status(c);
+    });
+}
+
+int octgb_xmedian(octgb_ctx* c, const float* mag, int mag_loc, int n_frames, int nx, int nz, int ignore_nan,
+                  double* out) {
+    return guarded(c, [&] {
+        require(mag != nullptr && out != nullptr, "NULL buffer");
+        require(n_frames >= 1 && nx >= 1 && nx <= 4096 && nz >= 1, "shape must have 1..4096 A-scans per frame");
+        const size_t n = static_cast<size_t>(n_frames) * nx * nz;
+        const float* src = mag;
+        if (mag_loc != OCTGB_DEVICE) {
+            ck(c->out.ensure(n * sizeof(float)), "cudaMalloc(mag)");
+            ck(cudaMemcpyAsync(c->out.p, mag, n * sizeof(float), cudaMemcpyHostToDevice, c->stream), "H2D mag");
+            src = c->out.as<float>();
+        }
+        ck(c->xmed.ensure(static_cast<size_t>(n_frames) * nz * sizeof(double)), "cudaMalloc(median)");
+        ck(launch_xmedian(src, n_frames, nx, nz, ignore_nan, c->xmed.as<double>(), c->stream), "x-median kernel");
+        c->launches++;
+        ck(cudaMemcpyAsync(out, c->xmed.p, static_cast<size_t>(n_frames) * nz * sizeof(double),
+                           cudaMemcpyDeviceToHost, c->stream),
+           "D2H median");
+        check_status(c);
     });
 }
 

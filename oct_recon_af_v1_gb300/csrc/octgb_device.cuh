@@ -1,0 +1,193 @@
+// Device helpers shared by the spectral and estimation kernels: complex
+// arithmetic, the inverse DFT blocks of the 2048-point shared-memory FFT,
+// bulk-copy/mbarrier primitives with a bounded wait, and the FFT itself.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "octgb_internal.h"
+
+namespace octgb {
+namespace {
+
+constexpr int kPadShift = 4;                              // one pad slot per 16 complex
+constexpr int kSpecStride = kN + (kN >> kPadShift);       // padded complex line length
+
+__device__ __forceinline__ int pad(int e) { return e + (e >> kPadShift); }
+
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+    return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+__device__ __forceinline__ float2 muli(float2 a) { return make_float2(-a.y, a.x); }
+
+// inverse DFT-4 (omega = +i), natural order in and out
+__device__ __forceinline__ void dft4(float2& x0, float2& x1, float2& x2, float2& x3) {
+    const float2 a = cadd(x0, x2), b = csub(x0, x2), c = cadd(x1, x3), d = muli(csub(x1, x3));
+    x0 = cadd(a, c);
+    x2 = csub(a, c);
+    x1 = cadd(b, d);
+    x3 = csub(b, d);
+}
+
+// cos/sin of multiples of pi/8 (float64 literals rounded to float32)
+constexpr float kC1 = 0.92387953251128675613f;   // cos(pi/8)
+constexpr float kS1 = 0.38268343236508977173f;   // sin(pi/8)
+constexpr float kC2 = 0.70710678118654752440f;   // cos(pi/4)
+
+// inverse DFT-16 as 4 x 4: X[4*k1 + k2] = sum_n1 w4^(n1 k1) w16^(n1 k2) sum_n2 x[n1 + 4 n2] w4^(n2 k2)
+__device__ __forceinline__ void dft16(float2 (&v)[16]) {
+#pragma unroll
+    for (int n1 = 0; n1 < 4; ++n1) dft4(v[n1], v[n1 + 4], v[n1 + 8], v[n1 + 12]);
+    // twiddles w16^(n1*k2) on element v[n1 + 4*k2]
+    v[1 + 4] = cmul(v[1 + 4], make_float2(kC1, kS1));     // n1=1,k2=1: w^1
+    v[1 + 8] = cmul(v[1 + 8], make_float2(kC2, kC2));     // n1=1,k2=2: w^2
+    v[1 + 12] = cmul(v[1 + 12], make_float2(kS1, kC1));   // n1=1,k2=3: w^3
+    v[2 + 4] = cmul(v[2 + 4], make_float2(kC2, kC2));     // n1=2,k2=1: w^2
+    v[2 + 8] = muli(v[2 + 8]);                            // n1=2,k2=2: w^4 = i
+    v[2 + 12] = cmul(v[2 + 12], make_float2(-kC2, kC2));  // n1=2,k2=3: w^6
+    v[3 + 4] = cmul(v[3 + 4], make_float2(kS1, kC1));     // n1=3,k2=1: w^3
+    v[3 + 8] = cmul(v[3 + 8], make_float2(-kC2, kC2));    // n1=3,k2=2: w^6
+    v[3 + 12] = cmul(v[3 + 12], make_float2(-kC1, -kS1)); // n1=3,k2=3: w^9
+#pragma unroll
+    for (int k2 = 0; k2 < 4; ++k2) dft4(v[4 * k2], v[4 * k2 + 1], v[4 * k2 + 2], v[4 * k2 + 3]);
+    // X[4*k1 + k2] sits in v[k1 + 4*k2]: transpose the 4x4 block
+    float2 t;
+    t = v[1]; v[1] = v[4]; v[4] = t;
+    t = v[2]; v[2] = v[8]; v[8] = t;
+    t = v[3]; v[3] = v[12]; v[12] = t;
+    t = v[6]; v[6] = v[9]; v[9] = t;
+    t = v[7]; v[7] = v[13]; v[13] = t;
+    t = v[11]; v[11] = v[14]; v[14] = t;
+}
+
+// inverse DFT-8 as 2 x 4, returning only X[0..3] (the last stage keeps k < N/2)
+__device__ __forceinline__ void dft8_low(float2 (&v)[8], float2 (&X)[4]) {
+    dft4(v[0], v[2], v[4], v[6]);
+    dft4(v[1], v[3], v[5], v[7]);
+    const float2 y1 = cmul(v[3], make_float2(kC2, kC2));
+    const float2 y2 = muli(v[5]);
+    const float2 y3 = cmul(v[7], make_float2(-kC2, kC2));
+    X[0] = cadd(v[0], v[1]);
+    X[1] = cadd(v[2], y1);
+    X[2] = cadd(v[4], y2);
+    X[3] = cadd(v[6], y3);
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ void tma_bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Bounded wait on an mbarrier phase: gives up after ~2 s of wall time and
+// reports it through the status word (the copy it waits for is 4 KiB and
+// normally lands within microseconds).
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int* status) {
+    if (mbar_test(bar, parity)) return true;
+    const uint64_t t0 = globaltimer_ns();
+    for (uint32_t it = 0; it < (1u << 30); ++it) {
+        if (mbar_test(bar, parity)) return true;
+        __nanosleep(64);
+        if ((it & 255u) == 255u && globaltimer_ns() - t0 > 2000000000ull) break;
+    }
+    atomicExch(status, kStatusTimeout);
+    return false;
+}
+
+__device__ __forceinline__ void group_sync(int g) {
+    asm volatile("bar.sync %0, %1;" ::"r"(1 + g), "r"(kGroup) : "memory");
+}
+
+// Inverse FFT of one 2048-point line X (padded, see pad()) by the 128 threads
+// of group g (thread lt of the group), Stockham radix 16, 16, 8 with the last
+// stage pruned to the low half: on return mag[h][r] = |X[k]| for
+// k = lt + 128 h + 256 r (k < N/2), the square root correctly rounded.  The
+// transform is unnormalised (any 1/N is folded into the input).  X is
+// overwritten.  tw2[r][j] = w^(r j N/256), tw3[r][j] = w^(r j), w = e^(2 pi i/N).
+// ifft2048_low_mag_regs is the same transform with the first stage's inputs
+// v[r] = x[lt + 128 r] already in registers (X is then only work space).
+__device__ __forceinline__ void ifft2048_low_mag_regs(float2 (&v0)[16], float2* X, const float2 (*tw2)[16],
+                                                      const float2 (*tw3)[256], int g, int lt,
+                                                      float (&mag)[2][4]) {
+    {
+        float2 (&v)[16] = v0;
+        dft16(v);
+        group_sync(g);
+#pragma unroll
+        for (int r = 0; r < 16; ++r) X[pad(16 * lt + r)] = v[r];
+        group_sync(g);
+    }
+    {
+        float2 v[16];
+        const int jm = lt & 15;
+#pragma unroll
+        for (int r = 0; r < 16; ++r) v[r] = X[pad(lt + 128 * r)];
+#pragma unroll
+        for (int r = 1; r < 16; ++r) v[r] = cmul(v[r], tw2[r][jm]);
+        dft16(v);
+        group_sync(g);
+        const int idxD = (lt >> 4) * 256 + jm;
+#pragma unroll
+        for (int r = 0; r < 16; ++r) X[pad(idxD + 16 * r)] = v[r];
+        group_sync(g);
+    }
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int j = lt + 128 * h;
+        float2 v[8];
+#pragma unroll
+        for (int r = 0; r < 8; ++r) v[r] = X[pad(j + 256 * r)];
+#pragma unroll
+        for (int r = 1; r < 8; ++r) v[r] = cmul(v[r], tw3[r][j]);
+        float2 Xk[4];
+        dft8_low(v, Xk);
+#pragma unroll
+        for (int r = 0; r < 4; ++r) mag[h][r] = __fsqrt_rn(fmaf(Xk[r].x, Xk[r].x, Xk[r].y * Xk[r].y));
+    }
+}
+
+__device__ __forceinline__ void ifft2048_low_mag(float2* X, const float2 (*tw2)[16], const float2 (*tw3)[256],
+                                                 int g, int lt, float (&mag)[2][4]) {
+    float2 v[16];
+#pragma unroll
+    for (int r = 0; r < 16; ++r) v[r] = X[pad(lt + 128 * r)];
+    ifft2048_low_mag_regs(v, X, tw2, tw3, g, lt, mag);
+}
+
+}  // namespace
+}  // namespace octgb

@@ -136,6 +136,26 @@ cudaError_t launch_quantise_dev(const float* db, int64_t n, const unsigned int* 
 cudaError_t launch_minmax(const float* x, int64_t n, unsigned int* minmax, cudaStream_t st);
 cudaError_t launch_minmax_init(unsigned int* minmax, int count, cudaStream_t st);
 
+// dispersion scorer: A[(gi * nb + bi) * nx + x][k] = mean over repeats of
+// |ifft(X line * phase[gi])|[k], k < N/2, for B-scans b0 .. b0 + nb - 1
+struct DispArgs {
+    const float* X;        // (B, rep, nx, kN) linearised, windowed, real
+    const float2* phase;   // (n_beta, kN) exp(-i beta dk^2) / N
+    const float2* tw;      // (kN) e^(2 pi i k / N)
+    float* A;              // (n_beta, nb, nx, kHalf)
+    int n_beta, nb, b0, nx, rep;
+};
+cudaError_t launch_disp_mag(const DispArgs& a, int num_sms, cudaStream_t st);
+// X[l][j] = float32(float64(spec[l][j].re) * hann[j]) over `lines` lines of kN
+cudaError_t launch_window_pack(const float2* spec, const double* hann, int64_t lines, float* X, cudaStream_t st);
+// per segment (n_seg rows of nx x kHalf magnitudes): metric 1 top_percentile
+// (top_k elements), 2 kurtosis, 3 entropy, 4 legacy_peak, depths >= z_min
+cudaError_t launch_disp_metric(const float* A, int n_seg, int nx, int z_min, int metric, unsigned int top_k,
+                               double* score, cudaStream_t st);
+// median over x of every (frame, z) column of (n_frames, nx, nz) float32, as float64
+cudaError_t launch_xmedian(const float* mag, int n_frames, int nx, int nz, int ignore_nan, double* out,
+                           cudaStream_t st);
+
 // ordered-uint encoding of float32 for atomic min/max
 __host__ __device__ inline unsigned int f2ord(float f) {
 #ifdef __CUDA_ARCH__

@@ -1,0 +1,234 @@
+"""Estimators on the GB300 kernels: dispersion scorer and search, focus helpers.
+
+Dispersion (octrecon/estimation/dispersion.py): the scorer linearises and
+Hann/rms-windows its B-scans once on the device (octgb_disp_load); every
+candidate beta then costs one phase multiply, inverse FFT and |.| per A-scan
+and a per-B-scan sharpness metric, all on the device (octgb_disp_eval), and a
+whole list of betas (the coarse grid) runs in one launch.  `search_dispersion`
+is the reference's search (dispersion.py:213-246): normalised coarse-grid
+curves, bounded scalar refinement of their mean (scipy's bounded Brent, the
+reference's optimiser), per-B-scan optima and their robust spread.
+
+Focus (octrecon/estimation/focus.py): the x-median depth profiles run on the
+device (octgb_xmedian); the 1-D rules on a profile of ~1000 pixels
+(imgaussfilt_1d, findpeaks_matlab, detect_peak_near, interface_pix) stay on the
+host in float64, as MATLAB defines them.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import geometry as G
+from ._lib import Context
+
+Z_MIN_PIX = 20              # depth pixels ignored by the metrics (dispersion.py:40)
+TOP_FRACTION = 0.01         # top_percentile (dispersion.py:41)
+METRICS = ("top_percentile", "kurtosis", "entropy", "legacy_peak")
+_METRIC_ID = {"top_percentile": 1, "kurtosis": 2, "entropy": 3, "legacy_peak": 4}
+
+
+def hann_rms(n: int) -> np.ndarray:
+    """MATLAB hann(n) (symmetric) scaled to unit rms (dispersion.py:76-77)."""
+    h = 0.5 * (1 - np.cos(2 * np.pi * np.arange(n) / (n - 1)))
+    return h / np.sqrt(np.mean(h ** 2))
+
+
+class DispersionScorer:
+    """GB300 form of DispersionScorer (octrecon/estimation/dispersion.py:66-107).
+
+    raw_list: B-scans, each (rep, interf, N) raw counts (repeats of one y
+    frame, as VolumeContext.read_raw returns them).  Same interface as the
+    reference: window(beta), magnitude(beta, idx) -> (B or 1, nX, N/2) float32,
+    scores(beta, idx) -> (B,) or (1,) float64, n_evals; plus scores_grid(betas)
+    -> (len(betas), B), one launch for all betas.
+    """
+
+    def __init__(self, lambda_nm, raw_list, metric: str, apod_size: int, device: int = 0):
+        if metric not in METRICS:
+            raise ValueError(f"unknown metric {metric!r}; choose from {METRICS}")
+        self.metric = metric
+        lam = np.asarray(lambda_nm, float)
+        sg = G.build_spectral_geometry(lam, 0.0, 1.33)       # sinc band and k_eq do not depend on beta or n
+        N = len(lam)
+        self.n = N
+        self.nz = N // 2
+        raws = [np.asarray(r) for r in raw_list]
+        if not raws:
+            raise ValueError("no B-scans")
+        rep = raws[0].shape[0]
+        if any(r.shape != raws[0].shape or r.dtype != raws[0].dtype for r in raws):
+            raise ValueError("all B-scans must have the same shape and dtype")
+        self.nrep = rep
+        self.B = len(raws)
+        interf = raws[0].shape[1]
+        self.nx = interf - int(apod_size)
+        k_eq = 2 * np.pi / sg.lambda_eq_nm
+        self.dk2 = (k_eq - k_eq.mean()) ** 2                   # float64 (dispersion.py:78-79)
+        self.ctx = Context(device)
+        self.ctx.set_geometry(sg.sinc_idx, sg.sinc_w, np.ones(N, np.complex128))
+        self.ctx.disp_load(np.concatenate(raws, 0), int(apod_size), self.B, rep, hann_rms(N))
+        self.ctx.disp_set_dk2(self.dk2)
+        self.top_k = max(1, int(self.nx * (self.nz - Z_MIN_PIX) * TOP_FRACTION))
+        self.n_evals = 0
+
+    @classmethod
+    def from_context(cls, ctx, raw_list, metric: str, device: int = 0):
+        """Build from the reference's VolumeContext (estimation/_common.py:38-118)."""
+        h = ctx.hdr
+        if max(1, h.spectra_avg) != 1 or h.apod_mode != "lines":
+            raise NotImplementedError("gb300 scorer: AScanBinning / frame-mean apodisation are not supported")
+        return cls(ctx.lambda_nm, raw_list, metric, h.apod_size, device)
+
+    def close(self):
+        self.ctx.close()
+
+    def window(self, beta):
+        return np.exp(-1j * float(beta) * self.dk2).astype(np.complex64)
+
+    def _range(self, idx):
+        return (0, self.B) if idx is None else (int(idx), 1)
+
+    def magnitude(self, beta, idx=None) -> np.ndarray:
+        b0, nb = self._range(idx)
+        out = np.empty((1, nb, self.nx, self.nz), np.float32)
+        self.ctx.disp_eval([beta], b0, nb, 0, mag=out)
+        return out[0]
+
+    def scores(self, beta, idx=None) -> np.ndarray:
+        self.n_evals += 1
+        b0, nb = self._range(idx)
+        return self.ctx.disp_eval([beta], b0, nb, _METRIC_ID[self.metric], self.top_k, Z_MIN_PIX)[0]
+
+    def scores_grid(self, betas, idx=None) -> np.ndarray:
+        betas = np.asarray(betas, float)
+        self.n_evals += len(betas)
+        b0, nb = self._range(idx)
+        return self.ctx.disp_eval(betas, b0, nb, _METRIC_ID[self.metric], self.top_k, Z_MIN_PIX)
+
+
+def search_dispersion(scorer, lo: float, hi: float, initial: float, n_grid: int = 41) -> dict:
+    """The search of estimate_dispersion (dispersion.py:213-246) on any scorer:
+    coarse grid, each B-scan's curve normalised to [0, 1], bounded refinement of
+    the mean curve's maximum, per-B-scan optima.  Returns the result keys that
+    do not depend on the volume."""
+    from scipy.optimize import minimize_scalar
+
+    grid = np.linspace(lo, hi, int(n_grid))
+    if hasattr(scorer, "scores_grid"):
+        S = np.asarray(scorer.scores_grid(grid), float)
+    else:
+        S = np.array([scorer.scores(b) for b in grid])
+    smin, smax = S.min(0), S.max(0)
+    rngs = np.where(smax > smin, smax - smin, 1.0)
+    Sn = (S - smin) / rngs
+    agg = Sn.mean(1)
+    gi = int(np.argmax(agg))
+
+    def bracket(i):
+        return grid[max(i - 1, 0)], grid[min(i + 1, len(grid) - 1)]
+
+    tol = max(abs(initial), abs(lo), abs(hi)) * 2e-5
+    a, b = bracket(gi)
+    r = minimize_scalar(lambda x: -float(np.mean((scorer.scores(x) - smin) / rngs)), bounds=(a, b),
+                        method="bounded", options={"xatol": tol})
+    value = float(r.x) if -r.fun >= agg[gi] else float(grid[gi])
+    per = []
+    for j in range(S.shape[1]):
+        i = int(np.argmax(S[:, j]))
+        a, b = bracket(i)
+        rj = minimize_scalar(lambda x: -float(scorer.scores(x, j)[0]), bounds=(a, b), method="bounded",
+                             options={"xatol": tol})
+        per.append(float(rj.x) if -rj.fun >= S[i, j] else float(grid[i]))
+    per = np.array(per)
+    step = (hi - lo) / (n_grid - 1)
+    return {"value": value, "candidates": grid, "score_curve": agg, "score_curves_per_bscan": Sn.T,
+            "scores": S, "per_bscan_values": per, "median_per_bscan": float(np.median(per)),
+            "spread_mad": float(1.4826 * np.median(np.abs(per - np.median(per)))),
+            "at_bound": bool(value <= lo + step or value >= hi - step), "n_evaluations": scorer.n_evals}
+
+
+# --------------------------------------------------------------------------- focus helpers
+def matlab_round(x):
+    """MATLAB round(): halves away from zero."""
+    x = np.asarray(x, float)
+    return np.sign(x) * np.floor(np.abs(x) + 0.5)
+
+
+def imgaussfilt_1d(v, sigma: float = 4.0) -> np.ndarray:
+    """MATLAB imgaussfilt on a vector (focus.py:44-52): Gaussian of
+    2*ceil(2 sigma)+1 taps normalised to sum 1, replicate padding."""
+    v = np.asarray(v, float).ravel()
+    h = int(np.ceil(2 * sigma))
+    taps = np.exp(-np.arange(-h, h + 1) ** 2 / (2 * sigma ** 2))
+    taps = taps / taps.sum()
+    padded = np.concatenate([np.repeat(v[:1], h), v, np.repeat(v[-1:], h)])
+    return np.convolve(padded, taps, mode="valid")
+
+
+def findpeaks_matlab(v) -> np.ndarray:
+    """0-based indices of MATLAB findpeaks maxima (focus.py:55-72): larger than
+    the left neighbour, a plateau reported at its first sample when the sample
+    after it is smaller, end points never."""
+    v = np.asarray(v, float)
+    n = len(v)
+    out = []
+    i = 1
+    while i < n - 1:
+        if not v[i] > v[i - 1]:
+            i += 1
+            continue
+        j = i
+        while j + 1 < n - 1 and v[j + 1] == v[i]:
+            j += 1
+        if v[j + 1] < v[i]:                  # j <= n - 2 here
+            out.append(i)
+        i = j + 1
+    return np.asarray(out, int)
+
+
+def detect_peak_near(profile, guess_pix, search_px: int = 60, baseline_sigma: float = 30.0,
+                     smooth_sigma: float = 4.0):
+    """Confocal peak of a depth profile near a 1-based guess (focus.py:191-206):
+    10 log10 with gaps interpolated, minus a sigma-30 baseline after sigma-4
+    smoothing, the strongest MATLAB peak within +-search_px.  -> (pix or nan,
+    prominence dB)."""
+    prof = np.asarray(profile, float)
+    lp = np.full(prof.shape, np.nan)
+    ok = np.isfinite(prof) & (prof > 0)
+    lp[ok] = 10 * np.log10(prof[ok])
+    if ok.sum() < 10:
+        return np.nan, 0.0
+    lp = np.interp(np.arange(len(lp)), np.nonzero(ok)[0], lp[ok])
+    detr = imgaussfilt_1d(lp, smooth_sigma) - imgaussfilt_1d(lp, baseline_sigma)
+    p = findpeaks_matlab(detr) + 1
+    p = p[np.abs(p - guess_pix) <= search_px]
+    if p.size == 0:
+        return np.nan, 0.0
+    best = p[np.argmax(detr[p - 1])]
+    return int(best), float(detr[best - 1])
+
+
+def interface_pix_from_medians(medians):
+    """Step-1 rule (focus.py:209-218) on per-frame x-median profiles
+    (frames, nZ): the first maximum below the top third, 1-based, then the
+    rounded median over frames."""
+    med = np.array(medians, float, copy=True)
+    nz = med.shape[-1]
+    med[:, : int(matlab_round(nz / 3))] = np.nan
+    vals = [int(np.nanargmax(m)) + 1 for m in med]
+    return int(matlab_round(np.median(vals))), vals
+
+
+def interface_pix(ctx: Context, mag_opc):
+    """interface_pix (focus.py:209-218) with the x-medians on the device."""
+    return interface_pix_from_medians(ctx.xmedian(mag_opc, ignore_nan=True))
+
+
+def depth_profile(ctx: Context, mag, ignore_nan: bool = True) -> np.ndarray:
+    """mean over frames of the x-median depth profiles (focus.py:156,255)."""
+    med = ctx.xmedian(mag, ignore_nan=ignore_nan)
+    with np.errstate(all="ignore"):
+        import warnings
+        with warnings.catch_warnings():
+            warnings.simplefilter("ignore", RuntimeWarning)
+            return np.nanmean(med, axis=0) if ignore_nan else med.mean(axis=0)

@@ -21,6 +21,9 @@ files, so `Reconstructor`, the CLI (`--set device=gb300`) and the web app
   `on_batch(done, total)` callbacks, the `timers` keys, and returns float32 dB
   (nFrames, nOutZ, nOutX) on the host.  Tiles are processed x-major/z-minor
   and every batch is added in that order, as in the reference.
+* Estimators asked for device gb300 (estimate_dispersion, detect_focus,
+  octrecon/estimation) keep their host logic; their spectral processors and
+  the DispersionScorer run on the GB300 kernels (`_register_estimators`).
 * The web app's GPU card only lights up when CuPy imports
   (webapp/server.py:74-85); `register()` patches its `system_info` to report
   the gb300 device.
@@ -74,15 +77,7 @@ def register(device_index: int = 0) -> None:
     backend.get_xp = get_xp
     pipeline.get_xp = get_xp
     try:
-        import octrecon.estimation._common as common
-        common.get_xp = get_xp
-        # estimators run on the CPU path when asked for the gb300 device
-        orig_ctx_init = common.VolumeContext.__init__
-
-        def ctx_init(self, volume_folder, device="cpu", dtype=np.float32):
-            orig_ctx_init(self, volume_folder, "cpu" if device == DEVICE else device, dtype)
-
-        common.VolumeContext.__init__ = ctx_init
+        _register_estimators(get_xp, device_index)
     except ImportError:
         pass
 
@@ -113,6 +108,71 @@ def register(device_index: int = 0) -> None:
     except Exception:
         pass
     _registered = True
+
+
+class _GB300Processor:
+    """SpectralProcessor.magnitude (octrecon/core/spectral.py:136-153) of one
+    geometry on the GB300 kernels; host arrays in and out, as the estimators'
+    CPU path."""
+
+    def __init__(self, sg, apod_size: int, device_index: int):
+        from ._lib import Context
+        self.ctx = Context(device_index)
+        self.ctx.set_geometry(sg.sinc_idx, sg.sinc_w, sg.window)
+        self.apod_size = int(apod_size)
+        self.n = len(sg.lambda_nm)
+        self.nz = self.n // 2
+
+    def magnitude(self, raw):
+        return self.ctx.magnitude(np.asarray(raw), self.apod_size)
+
+
+def _register_estimators(get_xp, device_index: int) -> None:
+    """Estimators on device gb300 (octrecon/estimation): VolumeContext
+    (_common.py:38-118) keeps its host readers and NumPy namespace, its
+    processors run the GB300 magnitude kernel, and DispersionScorer
+    (dispersion.py:66-107) becomes the GB300 scorer; estimate_dispersion and
+    detect_focus themselves run unchanged."""
+    import octrecon.estimation._common as common
+    import octrecon.estimation.dispersion as disp
+
+    from .estimation import DispersionScorer as GB300Scorer
+    common.get_xp = get_xp
+    VC = common.VolumeContext
+    orig_ctx_init, orig_processor = VC.__init__, VC.processor
+
+    def ctx_init(self, volume_folder, device="cpu", dtype=np.float32):
+        gb = device == DEVICE
+        orig_ctx_init(self, volume_folder, "cpu" if gb else device, dtype)
+        self._gb300 = {} if gb else None
+        if gb:
+            h = self.hdr
+            if max(1, h.spectra_avg) != 1 or h.apod_mode != "lines":
+                raise NotImplementedError("gb300: AScanBinning / frame-mean apodisation are not supported by the "
+                                          "GB300 kernels")
+            self.device = DEVICE
+
+    def processor(self, dispersion, n_medium=None):
+        cache = getattr(self, "_gb300", None)
+        if cache is None:
+            return orig_processor(self, dispersion, n_medium)
+        key = (float(dispersion), self.si.tissue_ri if n_medium is None else float(n_medium))
+        sp = cache.get(key)
+        if sp is None:
+            sp = cache[key] = _GB300Processor(self.geometry(dispersion, n_medium), self.hdr.apod_size,
+                                              device_index)
+        return sp
+
+    VC.__init__ = ctx_init
+    VC.processor = processor
+    orig_scorer = disp.DispersionScorer
+
+    def scorer(ctx, raw_list, metric):
+        if getattr(ctx, "_gb300", None) is not None:
+            return GB300Scorer.from_context(ctx, raw_list, metric, device_index)
+        return orig_scorer(ctx, raw_list, metric)
+
+    disp.DispersionScorer = scorer
 
 
 class _RowEngine:

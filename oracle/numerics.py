@@ -385,3 +385,53 @@ def lsb_report(a_db, b_db, clim, floor_db=None):
     d = np.abs(qa - qb)[sel]
     return {"max_lsb": int(d.max()) if d.size else 0, "exact_frac": float((d == 0).mean()) if d.size else 1.0,
             "n": int(d.size)}
+
+
+# ----------------------------------------------------------------------------- estimation
+Z_MIN_PIX = 20                                           # estimation/dispersion.py:40
+TOP_FRACTION = 0.01                                      # estimation/dispersion.py:41
+
+
+def disp_metric(A, name):
+    """estimation/dispersion.py:46-63: (B, nX, nZ) float32 magnitude -> (B,)
+    sharpness, depth pixels >= 20 only; I = (A^2 in float32) as float64."""
+    B = A.shape[0]
+    if name == "legacy_peak":
+        return np.log(A[:, :, Z_MIN_PIX:] + 1e-12).mean(axis=1).max(axis=1)
+    I = (A[:, :, Z_MIN_PIX:] ** 2).reshape(B, -1).astype(np.float64)
+    if name == "top_percentile":
+        M = I.shape[1]
+        k = max(1, int(M * TOP_FRACTION))
+        return np.log(np.partition(I, M - k, axis=1)[:, M - k:].mean(axis=1))
+    if name == "kurtosis":
+        return (I ** 2).sum(axis=1) / I.sum(axis=1) ** 2
+    if name == "entropy":
+        p = I / I.sum(axis=1, keepdims=True)
+        return (p * np.log(p + 1e-30)).sum(axis=1)
+    raise ValueError(name)
+
+
+class DispScorer:
+    """estimation/dispersion.py:66-107 over raw arrays: X = linearise * Hann/rms
+    once (complex64), then per beta ifft(X * exp(-i beta dk^2)) |.| of the
+    first N/2 bins, mean over repeats, metric.  raw_list: (rep, interf, N)."""
+
+    def __init__(self, lambda_nm, raw_list, metric, apod_size):
+        g = spectral_geometry(lambda_nm, 0.0, 1.33)
+        N = len(g.lambda_nm)
+        self.nz = N // 2
+        self.metric = metric
+        hann = 0.5 * (1 - np.cos(2 * np.pi * np.arange(N) / (N - 1)))
+        hann = hann / np.sqrt(np.mean(hann ** 2))
+        k_eq = 2 * np.pi / g.lambda_eq_nm
+        self.dk2 = (k_eq - k_eq.mean()) ** 2
+        self.X = np.stack([(linearise_numpy(r, g, apod_size, np.float32) * hann).astype(np.complex64)
+                           for r in raw_list])                      # (B, rep, nX, N)
+
+    def magnitude(self, beta, idx=None):
+        X = self.X if idx is None else self.X[idx:idx + 1]
+        spec = X * np.exp(-1j * float(beta) * self.dk2).astype(np.complex64)
+        return np.abs(ifft_rows(spec)[..., : self.nz]).mean(axis=1)
+
+    def scores(self, beta, idx=None):
+        return disp_metric(self.magnitude(beta, idx), self.metric)

@@ -1,0 +1,128 @@
+"""Estimators on the host (no GPU): the oracle's DispersionScorer restatement
+against the reference's scores, the package's 1-D focus rules against the
+reference's outputs, and the package's dispersion search driven by the oracle
+scorer on the B-scans the reference chose, against the reference's estimate.
+
+Fixtures: tests/golden/scorer_case.npz, estimation_case.npz and
+estimation_volume.tar.xz (make_golden_estimation.py).
+"""
+from __future__ import annotations
+
+import json
+import tarfile
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle import numerics as O
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+
+
+@pytest.fixture(scope="module")
+def scorer_case():
+    return dict(np.load(GOLDEN / "scorer_case.npz"))
+
+
+@pytest.fixture(scope="module")
+def est_case():
+    d = np.load(GOLDEN / "estimation_case.npz")
+    out = {k: d[k] for k in d.files}
+    out["estimate"] = json.loads(str(d["estimate_json"]))
+    out["focus"] = json.loads(str(d["focus_json"]))
+    return out
+
+
+def scorer_raws(tag):
+    """The raw B-scans of scorer_case.npz, regenerated from their seeds."""
+    from oct_recon_af_v1_gb300 import synthetic
+    if tag == "r1":
+        raw, rep = synthetic.generate_numpy(3, 96, 25, seed=11), 1
+    else:
+        raw, rep = synthetic.generate_numpy(4, 64, 25, seed=12), 2
+    return [raw[i:i + rep] for i in range(0, raw.shape[0], rep)], rep
+
+
+@pytest.mark.parametrize("tag", ["r1", "r2"])
+def test_oracle_scorer_matches_reference(scorer_case, tag):
+    raws, _ = scorer_raws(tag)
+    betas = scorer_case["betas"]
+    for metric in ("top_percentile", "kurtosis", "entropy", "legacy_peak"):
+        sc = O.DispScorer(scorer_case["lambda_nm"], raws, metric, 25)
+        got = np.array([sc.scores(b) for b in betas])
+        np.testing.assert_allclose(got, scorer_case[f"scores_{tag}_{metric}"], rtol=1e-12, atol=0)
+        got1 = np.array([sc.scores(b, 1) for b in betas[::4]])
+        np.testing.assert_allclose(got1, scorer_case[f"scores_{tag}_{metric}_idx1"], rtol=1e-12, atol=0)
+    sc = O.DispScorer(scorer_case["lambda_nm"], raws, "top_percentile", 25)
+    beta0 = betas[len(betas) // 2]
+    np.testing.assert_allclose(sc.magnitude(beta0, 0), scorer_case[f"mag_{tag}"], rtol=1e-6, atol=0)
+
+
+def test_focus_rules_match_reference(est_case):
+    from oct_recon_af_v1_gb300 import estimation as E
+    i = 0
+    while f"prof{i}" in est_case:
+        p = est_case[f"prof{i}"]
+        np.testing.assert_array_equal(E.imgaussfilt_1d(p, 4), est_case[f"prof{i}_gauss4"])
+        np.testing.assert_array_equal(E.imgaussfilt_1d(p, 30), est_case[f"prof{i}_gauss30"])
+        lp = 10 * np.log10(np.where(p > 0, p, np.nan))
+        np.testing.assert_array_equal(E.findpeaks_matlab(np.nan_to_num(lp, nan=-300.0)), est_case[f"prof{i}_peaks"])
+        pix, prom = E.detect_peak_near(p, 300, 60)
+        ref = est_case[f"prof{i}_near300"]
+        assert (np.isnan(ref[0]) and np.isnan(pix)) or pix == ref[0]
+        assert prom == ref[1]
+        i += 1
+    assert i >= 1
+    np.testing.assert_array_equal(E.findpeaks_matlab(est_case["plateau"]), est_case["plateau_peaks"])
+    import warnings
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore", RuntimeWarning)
+        med = np.nanmedian(est_case["iface_mags"], axis=1)
+    assert E.interface_pix_from_medians(med)[0] == int(est_case["iface_out"])
+
+
+def test_findpeaks_edge_cases():
+    from oct_recon_af_v1_gb300 import estimation as E
+    assert E.findpeaks_matlab([]).size == 0
+    assert E.findpeaks_matlab([1.0, 2.0]).size == 0
+    assert list(E.findpeaks_matlab([0, 2, 2, 2])) == []          # plateau to the end: no peak
+    assert list(E.findpeaks_matlab([0, 2, 2, 1])) == [1]         # plateau reported at its first sample
+    assert list(E.findpeaks_matlab([3, 1, 2, 1, 5])) == [2]      # end points never
+
+
+def test_search_matches_reference_estimate(est_case, tmp_path):
+    """The package's search (dispersion.py:213-246) with the oracle scorer on
+    the B-scans the reference picked reproduces the reference's estimate."""
+    from octrecon_ref import import_octrecon
+    import_octrecon()
+    from octrecon.estimation._common import VolumeContext
+
+    from oct_recon_af_v1_gb300 import estimation as E
+    est = est_case["estimate"]
+    with tarfile.open(GOLDEN / "estimation_volume.tar.xz") as tf:
+        tf.extractall(tmp_path, filter="data")
+    ctx = VolumeContext(tmp_path / "estimation", device="cpu")
+    try:
+        raws = [ctx.read_raw(u["folder"], [u["frame"]]) for u in est["tiles_used"]]
+        lam = ctx.lambda_nm
+        apod = ctx.hdr.apod_size
+    finally:
+        ctx.close()
+
+    class Counting(O.DispScorer):
+        n_evals = 0
+
+        def scores(self, beta, idx=None):
+            Counting.n_evals += 1
+            return super().scores(beta, idx)
+
+    sc = Counting(lam, raws, est["metric"], apod)
+    lo, hi = est["bounds"]
+    r = E.search_dispersion(sc, lo, hi, est["initial"], len(est["candidates"]))
+    np.testing.assert_allclose(r["candidates"], est["candidates"], rtol=0, atol=0)
+    np.testing.assert_allclose(r["score_curve"], est["score_curve"], rtol=0, atol=1e-12)
+    assert r["value"] == pytest.approx(est["value"], abs=1e-6 * (hi - lo))
+    np.testing.assert_allclose(r["per_bscan_values"], est["per_bscan_values"], rtol=0, atol=1e-6 * (hi - lo))
+    assert r["at_bound"] == est["at_bound"]
+    assert r["n_evaluations"] == est["n_evaluations"]
