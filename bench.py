@@ -231,6 +231,8 @@ def gpu_arm(args, rank, world):
         return gpu_arm_config0(args, rank, world, torch, ctx)
     if args.config == 3:
         return gpu_arm_config3(args, rank, world, torch, ctx, stream, dev)
+    if args.config == 4:
+        return gpu_arm_config4(args, rank, world, torch, ctx, stream, dev)
     vol = Volume(ctx, torch, dev, host_copy=not args.no_e2e, bscans=args.bscans)
     n_out = (2 * vol.ny, vol.nz, vol.nx)
     db_vol = torch.empty(n_out, dtype=torch.float32, device=dev)
@@ -427,6 +429,161 @@ def gpu_arm_config3(args, rank, world, torch, ctx, stream, dev):
             "e2e": {"value": ascans / (ms_e2e * 1e-3), "unit": "A-scans/s", "ms_per_step": ms_e2e,
                     "h2d_bytes_per_step": raw_bytes, "d2h_bytes_per_step": out_bytes}}
     return line
+
+
+def config4_desc(n_train, n_base, epochs):
+    return {"workload": f"config4: learned beta/focus vs plain search; {n_train} training images from {n_base} "
+                        "dispersion-free B-scans x 10 synthetic dispersions (phase trick), 500 held-out B-scans "
+                        "x 500 A-scans x 2048 uint16 with beta_px ~ U[-5e-5, 5e-5] in the spectra and a confocal "
+                        "focus ~ U[100, 900] px (reflector amplitude x exp(-((d - f)/150)^2)); 3 probe "
+                        "reconstructions -> 256x256 dB images -> CNN",
+            "held_out_bscans": 500, "ascans_per_bscan": 500, "training_images": n_train, "epochs": epochs,
+            "search": "per-B-scan: 41-point grid over +-1.2 x 7.5e7 nm^2/rad (one launch) + bounded Brent, "
+                      "top_percentile; focus: x-mean profile rules",
+            "l2_flush": "held-out raw (1.05 GB) and magnitudes larger than L2"}
+
+
+def gpu_arm_config4(args, rank, world, torch, ctx, stream, dev):
+    from oct_recon_af_v1_gb300 import estimation as E
+    from oct_recon_af_v1_gb300 import learned as L
+    from oct_recon_af_v1_gb300 import synthetic as S
+    from oct_recon_af_v1_gb300._lib import U16
+    lam = S.lambda_nm()
+    NX, n_test, shifts = 500, 500, 10
+    n_base = max(1, args.train4 // shifts)
+    n_train = n_base * shifts
+    rng = np.random.default_rng(404)
+    # ---- training images: dispersion-free B-scans rendered at 10 dispersions each
+    t0 = time.perf_counter()
+    mk = L.ImageMaker(lam, APOD)
+    X = torch.empty((n_train, 3, L.IMG, L.IMG), dtype=torch.float32, device=dev)
+    Y = np.empty((n_train, 2), np.float32)
+    focus_base = rng.uniform(100, 900, n_base)
+    k, chunk = 0, 50
+    for c0 in range(0, n_base, chunk):
+        nb = min(chunk, n_base - c0)
+        raw = S.u16_bits(S.generate(nb, NX, APOD, seed=10_000 + c0, device=dev, beta_px=0.0,
+                                    focus_px=focus_base[c0:c0 + nb], chunk=nb, precision="float32"))
+        mk.load(raw, raw_dtype=U16)
+        for _ in range(shifts):
+            bc = -S.beta_ref_from_px(rng.uniform(-5e-5, 5e-5))
+            mk.render(bc, out=X[k:k + nb])
+            Y[k:k + nb] = L.targets(np.full(nb, bc), focus_base[c0:c0 + nb])
+            k += nb
+        del raw
+    torch.cuda.synchronize()
+    t_data = time.perf_counter() - t0
+    # ---- training (hand-written kernels; torch only holds tensors and shuffles)
+    from oct_recon_af_v1_gb300._lib import Context
+    net_ctx = Context(torch.cuda.current_device())
+    net_ctx.set_stream(stream.cuda_stream)
+    net = L.BetaFocusNet(net_ctx, seed=0)
+    Yd = torch.tensor(Y, device=dev)
+    bs, epochs = 128, args.epochs4
+    steps_per_epoch = n_train // bs
+    total = epochs * steps_per_epoch
+    losses = []
+    t0 = time.perf_counter()
+    it = 0
+    for ep in range(epochs):
+        perm = torch.randperm(n_train, device=dev)
+        for i in range(steps_per_epoch):
+            idx = perm[i * bs:(i + 1) * bs]
+            lr = 1e-5 + 0.5 * (2e-3 - 1e-5) * (1 + np.cos(np.pi * it / total))
+            loss = net.train_step(X.index_select(0, idx), Yd.index_select(0, idx), float(lr))
+            it += 1
+        losses.append(float(loss.item()))
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    del X, Yd
+    # ---- held-out B-scans with the dispersion in their spectra
+    beta_px_t = rng.uniform(-5e-5, 5e-5, n_test)
+    focus_t = rng.uniform(100, 900, n_test)
+    truth_beta = -np.asarray(beta_px_t) / S.dk_per_px() ** 2
+    raw_t = S.u16_bits(S.generate(n_test, NX, APOD, seed=777, device=dev, beta_px=beta_px_t, focus_px=focus_t,
+                                  chunk=50, precision="float32"))
+    img_buf = torch.empty((n_test, 3, L.IMG, L.IMG), dtype=torch.float32, device=dev)
+    pred_host = torch.empty((n_test, 2), dtype=torch.float32, pin_memory=True)
+
+    def learned_step(src):
+        imgs = mk.images(src, out=img_buf, raw_dtype=U16)
+        pred = net.forward(imgs)
+        pred_host.copy_(pred, non_blocking=True)
+
+    def timed(fn, steps, warm):
+        for _ in range(warm):
+            fn()
+        torch.cuda.synchronize()
+        n0 = mk.ctx.launches + net_ctx.launches
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps, mk.ctx.launches + net_ctx.launches - n0
+
+    clocks = Clocks(int(os.environ.get("LOCAL_RANK", 0)))
+    clocks.start()
+    ms_learned, launches = timed(lambda: learned_step(raw_t), args.steps, args.warmup)
+    clk = clocks.stop()
+    beta_l, focus_l = L.decode(pred_host.numpy())
+    host_raw = raw_t.cpu().pin_memory()
+    dev_raw = torch.empty_like(raw_t)
+
+    def e2e_step():
+        dev_raw.copy_(host_raw, non_blocking=True)
+        learned_step(dev_raw)
+
+    ms_e2e, _ = timed(e2e_step, args.steps, 1)
+    # ---- the plain search on the same B-scans (GPU scorer + host Brent + focus rules)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sc = E.DispersionScorer(lam, raw_t, "top_percentile", APOD, rep=1, raw_dtype=U16)
+    lo, hi = -1.2 * L.beta_scale(), 1.2 * L.beta_scale()
+    beta_s, grid, Sg = L.search_per_bscan(sc, lo, hi, 41)
+    mag0 = torch.empty((1, n_test, NX, 1024), dtype=torch.float32, device=dev)
+    sc.ctx.disp_eval([0.0], 0, n_test, 0, mag=mag0)
+    focus_s = L.focus_plain(sc.ctx, mag0[0])
+    torch.cuda.synchronize()
+    t_search = time.perf_counter() - t0
+    n_evals = sc.n_evals
+    # ---- sharpness at the chosen betas (not timed)
+    s_l = np.array([sc.scores(beta_l[j], j)[0] for j in range(n_test)])
+    s_s = np.array([sc.scores(beta_s[j], j)[0] for j in range(n_test)])
+    s_t = np.array([sc.scores(truth_beta[j], j)[0] for j in range(n_test)])
+    rng_j = Sg.max(0) - Sg.min(0)
+    gap = (s_s - s_l) / rng_j
+    sc.close()
+    ascans = n_test * NX
+    v_l = ascans / (ms_learned * 1e-3)
+    v_s = ascans / t_search
+    hbm, src = peaks()
+    raw_bytes = int(raw_t.numel()) * 2
+    return {"metric": METRIC, "value": v_l, "unit": "A-scans/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_learned, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 (uint16 in)", "data": "synthetic (seeded, generated on device)",
+            "config": config4_desc(n_train, n_base, epochs), "gpu_launches": int(launches),
+            "roofline": {"bound": "hbm", "achieved": raw_bytes / (ms_learned * 1e-3) / 1e9, "peak": hbm,
+                         "unit": "GB/s", "frac": raw_bytes / (ms_learned * 1e-3) / 1e9 / hbm, "traffic": None,
+                         "kernel": "whole learned step (linearise, 3 probe FFT passes, pooling, CNN forward)",
+                         "bytes_per_launch": raw_bytes, "peak_source": src + " (burst copy)"},
+            "clocks": clk,
+            "search": {"value": v_s, "unit": "A-scans/s", "seconds": t_search, "evaluations": n_evals,
+                       "learned_speedup": v_l / v_s},
+            "accuracy": {"beta_rmse_learned": float(np.sqrt(np.mean((beta_l - truth_beta) ** 2))),
+                         "beta_rmse_search": float(np.sqrt(np.mean((beta_s - truth_beta) ** 2))),
+                         "beta_unit": "nm^2/rad (training range +-7.49e7)",
+                         "sharpness_gap_mean": float(np.mean(gap)),
+                         "sharpness_gap_p95": float(np.quantile(gap, 0.95)),
+                         "sharpness_gap_unit": "(S(search) - S(learned)) / (max - min of the B-scan's grid curve)",
+                         "sharpness_truth_minus_search_mean": float(np.mean((s_t - s_s) / rng_j)),
+                         "focus_mae_learned_px": float(np.mean(np.abs(focus_l - focus_t))),
+                         "focus_mae_plain_px": float(np.mean(np.abs(focus_s - focus_t)))},
+            "training": {"images_s": t_data, "train_s": t_train, "epochs": epochs, "batch": bs,
+                         "loss_per_epoch": losses},
+            "e2e": {"value": ascans / (ms_e2e * 1e-3), "unit": "A-scans/s", "ms_per_step": ms_e2e,
+                    "h2d_bytes_per_step": raw_bytes, "d2h_bytes_per_step": n_test * 2 * 4}}
 
 
 def gpu_arm_config0(args, rank, world, torch, ctx):
@@ -646,7 +803,9 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--config", type=int, default=1, choices=[0, 1, 3])
+    ap.add_argument("--config", type=int, default=1, choices=[0, 1, 3, 4])
+    ap.add_argument("--train4", type=int, default=20000, help="training images of the learned estimator (config 4)")
+    ap.add_argument("--epochs4", type=int, default=8, help="training epochs (config 4)")
     ap.add_argument("--tiles3", type=int, default=64, help="tiles of the batched workload (config 3)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")

@@ -58,7 +58,10 @@ int octgb_destroy(octgb_ctx *ctx);
  * octgb_create). */
 const char *octgb_last_error(const octgb_ctx *ctx);
 /* Launch on `cuda_stream` (a cudaStream_t) instead of the context's own stream;
- * NULL restores the context stream. */
+ * NULL restores the context stream.  The context's own stream is a blocking
+ * stream: its work is ordered with the legacy default stream (work a caller
+ * queues there before a call is done before the call's kernels run, and vice
+ * versa).  Capture graphs on a caller's non-default stream. */
 int octgb_set_stream(octgb_ctx *ctx, void *cuda_stream);
 int octgb_synchronize(octgb_ctx *ctx);
 /* Cancellation (the reference's threading.Event, octrecon/pipeline.py:45-46,
@@ -247,6 +250,50 @@ int octgb_disp_eval(octgb_ctx *ctx, int n_beta, const double *betas, int b0, int
  * (n_frames, nz) doubles.  nx <= 4096.  Synchronises. */
 int octgb_xmedian(octgb_ctx *ctx, const float *mag, int mag_loc, int n_frames, int nx, int nz, int ignore_nan,
                   double *out);
+
+/* Mean over x of every depth column of (n_frames, nx, nz) float32
+ * magnitudes, as float64 (NaN ignored): the depth profile of sparse
+ * reflectors, whose x-median is the noise floor.  No counterpart in the
+ * reference.  nx <= 4096.  Synchronises. */
+int octgb_xmean(octgb_ctx *ctx, const float *mag, int mag_loc, int n_frames, int nx, int nz, double *out);
+
+/* ---------------------------------------------------------------- learned estimator */
+
+/* A small CNN that predicts the dispersion term and the focus of a B-scan
+ * from three probe reconstructions (the reference has no learned estimator;
+ * its searches, octrecon/estimation/dispersion.py and focus.py, judge it).
+ * Every pointer is a device pointer; tensors are float32 NCHW; all calls are
+ * asynchronous on the context's stream. */
+
+/* Probe images: mag (n_probe, nb, nx, n/2) (octgb_disp_eval magnitudes) ->
+ * img (nb, n_probe, 256, 256) = 20 log10 of the adaptive average pool of
+ * depths < z_keep (rows) x A-scans (columns); normalise = 1 standardises each
+ * image over all its probes and pixels. */
+int octgb_cnn_images(octgb_ctx *ctx, const float *mag, int n_probe, int nb, int nx, int z_keep, float *img,
+                     int normalise);
+/* y = conv3x3(x, w) + b, stride 1, zero padding 1: x (n, cin, h, w), w (cout, cin, 3, 3), b (cout) or NULL. */
+int octgb_cnn_conv3x3(octgb_ctx *ctx, const float *x, const float *w, const float *b, float *y, int n, int cin,
+                      int cout, int h, int wd);
+/* Gradients of octgb_cnn_conv3x3: dw, db from dy and x; dx (optional) with
+ * w_scratch (cout * cin * 9 floats) for the flipped kernel. */
+int octgb_cnn_conv3x3_bwd(octgb_ctx *ctx, const float *x, const float *w, const float *dy, float *dx, float *dw,
+                          float *db, float *w_scratch, int n, int cin, int cout, int h, int wd);
+/* p = 2x2 mean of relu(y) over `planes` planes of h x w (even), and its gradient. */
+int octgb_cnn_relu_pool(octgb_ctx *ctx, const float *y, float *p, int64_t planes, int h, int wd);
+int octgb_cnn_relu_pool_bwd(octgb_ctx *ctx, const float *dp, const float *y, float *dy, int64_t planes, int h,
+                            int wd);
+/* Dense layer: pre = x w^T + b (x (m, in), w (out, in)); act = relu(pre) when not NULL. */
+int octgb_cnn_dense(octgb_ctx *ctx, const float *x, const float *w, const float *b, float *pre, float *act, int m,
+                    int in, int out);
+/* Its gradients: dy (m, out) is first masked by pre > 0 when pre is given
+ * (in place); dw, db; dx (optional). */
+int octgb_cnn_dense_bwd(octgb_ctx *ctx, const float *x, const float *w, float *dy, const float *pre, float *dx,
+                        float *dw, float *db, int m, int in, int out);
+/* loss (one device double) = mean((pred - target)^2) over n values; grad = 2 (pred - target) / n. */
+int octgb_cnn_mse(octgb_ctx *ctx, const float *pred, const float *target, int n, float *grad, double *loss);
+/* One Adam step (bias-corrected, `step` counted from 1) on n parameters. */
+int octgb_cnn_adam(octgb_ctx *ctx, float *p, const float *g, float *m, float *v, int64_t n, float lr, float beta1,
+                   float beta2, float eps, int step);
 
 /* ---------------------------------------------------------------- allocation-free */
 

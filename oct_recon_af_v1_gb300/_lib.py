@@ -56,6 +56,20 @@ SIGNATURES = {
     "octgb_disp_eval": (c_int, [c_void_p, c_int, c_void_p, c_int, c_int, c_int, c_int64, c_int, c_void_p,
                                 c_void_p, c_int]),
     "octgb_xmedian": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_int, c_void_p]),
+    "octgb_xmean": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_void_p]),
+    "octgb_cnn_images": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_int]),
+    "octgb_cnn_conv3x3": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_int,
+                                  c_int]),
+    "octgb_cnn_conv3x3_bwd": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                      c_void_p, c_int, c_int, c_int, c_int, c_int]),
+    "octgb_cnn_relu_pool": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_int, c_int]),
+    "octgb_cnn_relu_pool_bwd": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_int64, c_int, c_int]),
+    "octgb_cnn_dense": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, c_int]),
+    "octgb_cnn_dense_bwd": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                    c_int, c_int, c_int]),
+    "octgb_cnn_mse": (c_int, [c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_void_p]),
+    "octgb_cnn_adam": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int64, c_float, c_float, c_float,
+                               c_float, c_int]),
 }
 
 
@@ -256,6 +270,18 @@ class Context:
         p, loc = _ptr(mag)
         out = np.empty((F, nz), np.float64)
         self._check(self.lib.octgb_xmedian(self.h, p, loc, F, nx, nz, int(bool(ignore_nan)), out.ctypes.data))
+        return out
+
+    def xmean(self, mag) -> np.ndarray:
+        """float64 mean over x (NaN ignored) of (frames, nX, nZ) float32 -> (frames, nZ)."""
+        if isinstance(mag, np.ndarray):
+            mag = np.ascontiguousarray(mag, dtype=np.float32)
+        elif not mag.is_contiguous():
+            mag = mag.contiguous()
+        F, nx, nz = mag.shape
+        p, loc = _ptr(mag)
+        out = np.empty((F, nz), np.float64)
+        self._check(self.lib.octgb_xmean(self.h, p, loc, F, nx, nz, out.ctypes.data))
         return out
 
     # -------------------------------------------------------------- quantisation

@@ -427,7 +427,9 @@ int octgb_create(int device, octgb_ctx** out) {
         if (prop.major * 10 + prop.minor < 100)
             throw Error(OCTGB_ERR_STATE, std::string("device ") + prop.name + " is not sm_100 or newer");
         c->num_sms = prop.multiProcessorCount;
-        ck(cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking), "cudaStreamCreate");
+        // a blocking stream: ordered with the legacy default stream, on which
+        // callers such as torch's default stream produce and read buffers
+        ck(cudaStreamCreateWithFlags(&c->own, cudaStreamDefault), "cudaStreamCreate");
         c->stream = c->own;
         ck(cudaHostAlloc(reinterpret_cast<void**>(&c->status_host), sizeof(int), cudaHostAllocMapped),
            "cudaHostAlloc(status)");
@@ -1325,25 +1327,143 @@ int octgb_disp_eval(octgb_ctx* c, int n_beta, const double* betas, int b0, int n
     });
 }
 
+namespace {
+void xprofile(octgb_ctx* c, const float* mag, int mag_loc, int n_frames, int nx, int nz, int ignore_nan,
+              int mean_mode, double* out) {
+    require(mag != nullptr && out != nullptr, "NULL buffer");
+    require(n_frames >= 1 && nx >= 1 && nx <= 4096 && nz >= 1, "shape must have 1..4096 A-scans per frame");
+    const size_t n = static_cast<size_t>(n_frames) * nx * nz;
+    const float* src = mag;
+    if (mag_loc != OCTGB_DEVICE) {
+        ck(c->out.ensure(n * sizeof(float)), "cudaMalloc(mag)");
+        ck(cudaMemcpyAsync(c->out.p, mag, n * sizeof(float), cudaMemcpyHostToDevice, c->stream), "H2D mag");
+        src = c->out.as<float>();
+    }
+    ck(c->xmed.ensure(static_cast<size_t>(n_frames) * nz * sizeof(double)), "cudaMalloc(median)");
+    ck(launch_xmedian(src, n_frames, nx, nz, ignore_nan, mean_mode, c->xmed.as<double>(), c->stream),
+       "x-profile kernel");
+    c->launches++;
+    ck(cudaMemcpyAsync(out, c->xmed.p, static_cast<size_t>(n_frames) * nz * sizeof(double),
+                       cudaMemcpyDeviceToHost, c->stream),
+       "D2H profile");
+    check_status(c);
+}
+}  // namespace
+
 int octgb_xmedian(octgb_ctx* c, const float* mag, int mag_loc, int n_frames, int nx, int nz, int ignore_nan,
                   double* out) {
+    return guarded(c, [&] { xprofile(c, mag, mag_loc, n_frames, nx, nz, ignore_nan, 0, out); });
+}
+
+int octgb_xmean(octgb_ctx* c, const float* mag, int mag_loc, int n_frames, int nx, int nz, double* out) {
+    return guarded(c, [&] { xprofile(c, mag, mag_loc, n_frames, nx, nz, 1, 1, out); });
+}
+
+// ---------------------------------------------------------------------------
+// Learned beta/focus estimator: device pointers only, asynchronous on the
+// context's stream (no counterpart in the reference).
+
+int octgb_cnn_images(octgb_ctx* c, const float* mag, int n_probe, int nb, int nx, int z_keep, float* img,
+                     int normalise) {
     return guarded(c, [&] {
-        require(mag != nullptr && out != nullptr, "NULL buffer");
-        require(n_frames >= 1 && nx >= 1 && nx <= 4096 && nz >= 1, "shape must have 1..4096 A-scans per frame");
-        const size_t n = static_cast<size_t>(n_frames) * nx * nz;
-        const float* src = mag;
-        if (mag_loc != OCTGB_DEVICE) {
-            ck(c->out.ensure(n * sizeof(float)), "cudaMalloc(mag)");
-            ck(cudaMemcpyAsync(c->out.p, mag, n * sizeof(float), cudaMemcpyHostToDevice, c->stream), "H2D mag");
-            src = c->out.as<float>();
-        }
-        ck(c->xmed.ensure(static_cast<size_t>(n_frames) * nz * sizeof(double)), "cudaMalloc(median)");
-        ck(launch_xmedian(src, n_frames, nx, nz, ignore_nan, c->xmed.as<double>(), c->stream), "x-median kernel");
+        require(mag && img, "NULL buffer");
+        require(n_probe >= 1 && nb >= 1 && nx >= 1 && z_keep >= 1 && z_keep <= kHalf, "bad image shape");
+        ck(launch_image_pool(mag, n_probe, nb, nx, z_keep, img, c->stream), "image pool kernel");
         c->launches++;
-        ck(cudaMemcpyAsync(out, c->xmed.p, static_cast<size_t>(n_frames) * nz * sizeof(double),
-                           cudaMemcpyDeviceToHost, c->stream),
-           "D2H median");
-        check_status(c);
+        if (normalise) {
+            ck(launch_image_norm(img, nb, static_cast<int64_t>(n_probe) * 256 * 256, c->stream), "image norm kernel");
+            c->launches++;
+        }
+    });
+}
+
+int octgb_cnn_conv3x3(octgb_ctx* c, const float* x, const float* w, const float* b, float* y, int n, int cin,
+                      int cout, int h, int wd) {
+    return guarded(c, [&] {
+        require(x && w && y, "NULL buffer");
+        require(n >= 1 && cin >= 1 && cout >= 1 && h >= 1 && wd >= 1 && n <= 65535, "bad convolution shape");
+        ck(launch_conv3x3(x, w, b, y, n, cin, cout, h, wd, c->stream), "conv kernel");
+        c->launches++;
+    });
+}
+
+int octgb_cnn_conv3x3_bwd(octgb_ctx* c, const float* x, const float* w, const float* dy, float* dx, float* dw,
+                          float* db, float* w_scratch, int n, int cin, int cout, int h, int wd) {
+    return guarded(c, [&] {
+        require(x && w && dy && dw && db, "NULL buffer");
+        require(n >= 1 && cin >= 1 && cout >= 1 && h >= 1 && wd >= 1 && n <= 65535, "bad convolution shape");
+        ck(launch_conv3x3_wgrad(x, dy, dw, n, cin, cout, h, wd, c->stream), "conv weight-gradient kernel");
+        ck(launch_bias_grad(dy, n, cout, static_cast<int64_t>(h) * wd, db, c->stream), "bias-gradient kernel");
+        c->launches += 2;
+        if (dx != nullptr) {
+            require(w_scratch != nullptr, "w_scratch is NULL");
+            ck(launch_flip_weights(w, cout, cin, w_scratch, c->stream), "weight flip kernel");
+            ck(launch_conv3x3(dy, w_scratch, nullptr, dx, n, cout, cin, h, wd, c->stream), "conv kernel");
+            c->launches += 2;
+        }
+    });
+}
+
+int octgb_cnn_relu_pool(octgb_ctx* c, const float* y, float* p, int64_t planes, int h, int wd) {
+    return guarded(c, [&] {
+        require(y && p && planes >= 1 && h >= 2 && wd >= 2 && h % 2 == 0 && wd % 2 == 0, "bad pooling shape");
+        ck(launch_relu_pool(y, planes, h, wd, p, c->stream), "relu/pool kernel");
+        c->launches++;
+    });
+}
+
+int octgb_cnn_relu_pool_bwd(octgb_ctx* c, const float* dp, const float* y, float* dy, int64_t planes, int h, int wd) {
+    return guarded(c, [&] {
+        require(dp && y && dy && planes >= 1 && h % 2 == 0 && wd % 2 == 0, "bad pooling shape");
+        ck(launch_relu_pool_bwd(dp, y, planes, h, wd, dy, c->stream), "relu/pool gradient kernel");
+        c->launches++;
+    });
+}
+
+int octgb_cnn_dense(octgb_ctx* c, const float* x, const float* w, const float* b, float* pre, float* act, int m,
+                    int in, int out) {
+    return guarded(c, [&] {
+        require(x && w && b && pre && m >= 1 && in >= 1 && out >= 1, "bad dense shape");
+        ck(launch_gemm(x, in, 1, w, 1, in, pre, out, m, out, in, 0, c->stream), "gemm kernel");
+        ck(launch_bias_relu(pre, b, m, out, act, c->stream), "bias kernel");
+        c->launches += 2;
+    });
+}
+
+int octgb_cnn_dense_bwd(octgb_ctx* c, const float* x, const float* w, float* dy, const float* pre, float* dx,
+                        float* dw, float* db, int m, int in, int out) {
+    return guarded(c, [&] {
+        require(x && w && dy && dw && db && m >= 1 && in >= 1 && out >= 1, "bad dense shape");
+        if (pre != nullptr) {
+            ck(launch_relu_bwd(dy, pre, static_cast<int64_t>(m) * out, c->stream), "relu gradient kernel");
+            c->launches++;
+        }
+        ck(launch_gemm(dy, 1, out, x, in, 1, dw, in, out, in, m, 0, c->stream), "gemm kernel");
+        ck(launch_bias_grad(dy, m, out, 1, db, c->stream), "bias-gradient kernel");
+        c->launches += 2;
+        if (dx != nullptr) {
+            ck(launch_gemm(dy, out, 1, w, in, 1, dx, in, m, in, out, 0, c->stream), "gemm kernel");
+            c->launches++;
+        }
+    });
+}
+
+int octgb_cnn_mse(octgb_ctx* c, const float* pred, const float* target, int n, float* grad, double* loss) {
+    return guarded(c, [&] {
+        require(pred && target && grad && loss && n >= 1, "bad loss arguments");
+        ck(launch_mse(pred, target, n, grad, loss, c->stream), "loss kernel");
+        c->launches++;
+    });
+}
+
+int octgb_cnn_adam(octgb_ctx* c, float* p, const float* g, float* m, float* v, int64_t n, float lr, float beta1,
+                   float beta2, float eps, int step) {
+    return guarded(c, [&] {
+        require(p && g && m && v && n >= 1 && step >= 1, "bad optimiser arguments");
+        const float c1 = 1.0f - std::pow(beta1, static_cast<float>(step));
+        const float c2 = 1.0f - std::pow(beta2, static_cast<float>(step));
+        ck(launch_adam(p, g, m, v, n, lr, beta1, beta2, eps, c1, c2, c->stream), "adam kernel");
+        c->launches++;
     });
 }
 

@@ -21,7 +21,8 @@
 // Focus (octrecon/estimation/focus.py:146,156,255): k_xmedian takes the
 // median over x of every depth column of (frames, nX, nZ) magnitudes, as
 // float64, optionally ignoring NaN (nanmedian), by a bitonic sort per column
-// in shared memory (one warp per column).
+// in shared memory (one warp per column); or, in mean mode, the float64 mean
+// of the column's non-NaN values.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -297,8 +298,9 @@ __global__ void __launch_bounds__(kSelThreads, 1) k_moments(const float* __restr
 constexpr int kMedCols = 8;                       // depth columns per CTA (one warp each)
 constexpr int kMedMaxX = 4096;
 
+// mean_mode: the float64 mean of the non-NaN values instead of the median
 __global__ void __launch_bounds__(kMedCols * 32) k_xmedian(const float* __restrict__ mag, int n_frames, int nx,
-                                                          int nz, int p2, int ignore_nan,
+                                                          int nz, int p2, int ignore_nan, int mean_mode,
                                                           double* __restrict__ out) {
     extern __shared__ __align__(16) float col[];  // [kMedCols][p2]
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -322,6 +324,18 @@ __global__ void __launch_bounds__(kMedCols * 32) k_xmedian(const float* __restri
     }
     __syncthreads();
     float* s = col + w * p2;
+    if (mean_mode) {
+        const int z = z0 + w;
+        double acc = 0.0;
+        for (int i = lane; i < nx; i += 32)
+            if (!isinf(s[i])) acc += static_cast<double>(s[i]);
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0 && z < nz) {
+            const int n = nx - n_nan[w];
+            out[static_cast<int64_t>(f) * nz + z] = n > 0 ? acc / n : __longlong_as_double(0x7ff8000000000000ll);
+        }
+        return;
+    }
     for (int k = 2; k <= p2; k <<= 1)
         for (int j = k >> 1; j > 0; j >>= 1) {
             for (int i = lane; i < p2; i += 32) {
@@ -394,8 +408,8 @@ cudaError_t launch_disp_metric(const float* A, int n_seg, int nx, int z_min, int
     return cudaGetLastError();
 }
 
-cudaError_t launch_xmedian(const float* mag, int n_frames, int nx, int nz, int ignore_nan, double* out,
-                           cudaStream_t st) {
+cudaError_t launch_xmedian(const float* mag, int n_frames, int nx, int nz, int ignore_nan, int mean_mode,
+                           double* out, cudaStream_t st) {
     int p2 = 32;
     while (p2 < nx) p2 <<= 1;
     if (p2 > kMedMaxX) return cudaErrorInvalidValue;
@@ -404,7 +418,7 @@ cudaError_t launch_xmedian(const float* mag, int n_frames, int nx, int nz, int i
                                          static_cast<int>(smem));
     if (e != cudaSuccess) return e;
     dim3 grid((nz + kMedCols - 1) / kMedCols, n_frames);
-    k_xmedian<<<grid, kMedCols * 32, smem, st>>>(mag, n_frames, nx, nz, p2, ignore_nan, out);
+    k_xmedian<<<grid, kMedCols * 32, smem, st>>>(mag, n_frames, nx, nz, p2, ignore_nan, mean_mode, out);
     return cudaGetLastError();
 }
 

@@ -153,8 +153,28 @@ cudaError_t launch_window_pack(const float2* spec, const double* hann, int64_t l
 cudaError_t launch_disp_metric(const float* A, int n_seg, int nx, int z_min, int metric, unsigned int top_k,
                                double* score, cudaStream_t st);
 // median over x of every (frame, z) column of (n_frames, nx, nz) float32, as float64
-cudaError_t launch_xmedian(const float* mag, int n_frames, int nx, int nz, int ignore_nan, double* out,
-                           cudaStream_t st);
+cudaError_t launch_xmedian(const float* mag, int n_frames, int nx, int nz, int ignore_nan, int mean_mode,
+                           double* out, cudaStream_t st);
+
+// learned beta/focus estimator (cnn.cu)
+cudaError_t launch_image_pool(const float* A, int n_probe, int nb, int nx, int z_keep, float* img, cudaStream_t st);
+cudaError_t launch_image_norm(float* img, int n_images, int64_t per_image, cudaStream_t st);
+cudaError_t launch_conv3x3(const float* x, const float* w, const float* b, float* y, int Nn, int C, int K, int H,
+                           int W, cudaStream_t st);
+cudaError_t launch_flip_weights(const float* w, int K, int C, float* wf, cudaStream_t st);
+cudaError_t launch_conv3x3_wgrad(const float* x, const float* dy, float* dw, int Nn, int C, int K, int H, int W,
+                                 cudaStream_t st);
+cudaError_t launch_relu_pool(const float* y, int64_t nk, int H, int W, float* p, cudaStream_t st);
+cudaError_t launch_relu_pool_bwd(const float* dp, const float* y, int64_t nk, int H, int W, float* dy,
+                                 cudaStream_t st);
+cudaError_t launch_gemm(const float* A, int64_t sa0, int64_t sa1, const float* B, int64_t sb0, int64_t sb1, float* C,
+                        int64_t ldc, int M, int N, int K, int accumulate, cudaStream_t st);
+cudaError_t launch_bias_relu(float* y, const float* b, int M, int N, float* out, cudaStream_t st);
+cudaError_t launch_bias_grad(const float* g, int Nn, int K, int64_t inner, float* db, cudaStream_t st);
+cudaError_t launch_relu_bwd(float* g, const float* pre, int64_t n, cudaStream_t st);
+cudaError_t launch_mse(const float* pred, const float* t, int n, float* grad, double* loss, cudaStream_t st);
+cudaError_t launch_adam(float* p, const float* g, float* m, float* v, int64_t n, float lr, float b1, float b2,
+                        float eps, float c1, float c2, cudaStream_t st);
 
 // ordered-uint encoding of float32 for atomic min/max
 __host__ __device__ inline unsigned int f2ord(float f) {

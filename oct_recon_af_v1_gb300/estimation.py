@@ -43,7 +43,10 @@ class DispersionScorer:
     -> (len(betas), B), one launch for all betas.
     """
 
-    def __init__(self, lambda_nm, raw_list, metric: str, apod_size: int, device: int = 0):
+    def __init__(self, lambda_nm, raw_list, metric: str, apod_size: int, device: int = 0, rep: int | None = None,
+                 raw_dtype=None):
+        """raw_list: a list of host (rep, interf, N) arrays, or one array or CUDA
+        tensor (B * rep, interf, N) with `rep` given (repeats consecutive)."""
         if metric not in METRICS:
             raise ValueError(f"unknown metric {metric!r}; choose from {METRICS}")
         self.metric = metric
@@ -52,21 +55,27 @@ class DispersionScorer:
         N = len(lam)
         self.n = N
         self.nz = N // 2
-        raws = [np.asarray(r) for r in raw_list]
-        if not raws:
-            raise ValueError("no B-scans")
-        rep = raws[0].shape[0]
-        if any(r.shape != raws[0].shape or r.dtype != raws[0].dtype for r in raws):
-            raise ValueError("all B-scans must have the same shape and dtype")
+        if rep is None:
+            raws = [np.asarray(r) for r in raw_list]
+            if not raws:
+                raise ValueError("no B-scans")
+            rep = raws[0].shape[0]
+            if any(r.shape != raws[0].shape or r.dtype != raws[0].dtype for r in raws):
+                raise ValueError("all B-scans must have the same shape and dtype")
+            raw = np.concatenate(raws, 0)
+        else:
+            raw = raw_list
+            if raw.shape[0] % rep:
+                raise ValueError("the B-scan count is not a multiple of rep")
         self.nrep = rep
-        self.B = len(raws)
-        interf = raws[0].shape[1]
+        self.B = raw.shape[0] // rep
+        interf = raw.shape[1]
         self.nx = interf - int(apod_size)
         k_eq = 2 * np.pi / sg.lambda_eq_nm
         self.dk2 = (k_eq - k_eq.mean()) ** 2                   # float64 (dispersion.py:78-79)
         self.ctx = Context(device)
         self.ctx.set_geometry(sg.sinc_idx, sg.sinc_w, np.ones(N, np.complex128))
-        self.ctx.disp_load(np.concatenate(raws, 0), int(apod_size), self.B, rep, hann_rms(N))
+        self.ctx.disp_load(raw, int(apod_size), self.B, rep, hann_rms(N), raw_dtype=raw_dtype)
         self.ctx.disp_set_dk2(self.dk2)
         self.top_k = max(1, int(self.nx * (self.nz - Z_MIN_PIX) * TOP_FRACTION))
         self.n_evals = 0

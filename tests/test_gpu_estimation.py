@@ -1,7 +1,7 @@
 """Estimators on the GPU: the GB300 DispersionScorer against the reference's
 scores (tests/golden/scorer_case.npz), its exact top-k selection (ties
-included) against the oracle metric on the same magnitudes, the x-median
-kernel against numpy.median / nanmedian, and octrecon's estimate_dispersion /
+included) against the oracle metric on the same magnitudes, the x-median and
+x-mean kernels against numpy.median / nanmedian / nanmean, and octrecon's estimate_dispersion /
 detect_focus on device "gb300" against the reference's own results on the
 same volume (tests/golden/estimation_case.npz)."""
 from __future__ import annotations
@@ -110,6 +110,10 @@ def test_xmedian_matches_numpy(built):
             np.testing.assert_array_equal(ctx.xmedian(m, ignore_nan=False), ref)
             dev = built.from_numpy(m).cuda()
             np.testing.assert_array_equal(ctx.xmedian(dev, ignore_nan=True), ref_nan)
+            with warnings.catch_warnings():
+                warnings.simplefilter("ignore", RuntimeWarning)
+                ref_mean = np.nanmean(m.astype(float), axis=1)
+            np.testing.assert_allclose(ctx.xmean(dev), ref_mean, rtol=1e-13, atol=0)
     finally:
         ctx.close()
 
