@@ -57,6 +57,8 @@ SIGNATURES = {
                                 c_void_p, c_int]),
     "octgb_xmedian": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_int, c_void_p]),
     "octgb_xmean": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_void_p]),
+    "octgb_linearise_precision": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_int, c_void_p, c_int]),
+    "octgb_magnitude_precision": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_int, c_void_p, c_int]),
     "octgb_cnn_images": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_int]),
     "octgb_cnn_conv3x3": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_int,
                                   c_int]),
@@ -222,6 +224,25 @@ class Context:
             out = np.empty((B, interf - apod_size, self.n // 2), np.float32)
         op, oloc = _ptr(out)
         self._check(self.lib.octgb_magnitude(self.h, p, dt, loc, B, interf, apod_size, op, oloc))
+        return out
+
+    def linearise_precision(self, raw, apod_size: int, out=None, raw_dtype=None):
+        """Precision form, stage (c): the linearised interferogram (B, nX, N)
+        float32 from the tensor-core sinc (no window)."""
+        raw, p, loc, dt, B, interf = self._raw_args(raw, apod_size, raw_dtype)
+        if out is None:
+            out = np.empty((B, interf - apod_size, self.n), np.float32)
+        op, oloc = _ptr(out)
+        self._check(self.lib.octgb_linearise_precision(self.h, p, dt, loc, B, interf, apod_size, op, oloc))
+        return out
+
+    def magnitude_precision(self, raw, apod_size: int, out=None, raw_dtype=None):
+        """Precision form of magnitude(): tensor-core sinc, then window, FFT, |.|."""
+        raw, p, loc, dt, B, interf = self._raw_args(raw, apod_size, raw_dtype)
+        if out is None:
+            out = np.empty((B, interf - apod_size, self.n // 2), np.float32)
+        op, oloc = _ptr(out)
+        self._check(self.lib.octgb_magnitude_precision(self.h, p, dt, loc, B, interf, apod_size, op, oloc))
         return out
 
     def db(self, raw, apod_size: int, z0: int, nz: int, out=None, minmax: bool = True, raw_dtype=None):

@@ -154,6 +154,9 @@ struct octgb_ctx {
     int64_t capture_launch0 = 0;
     DevBuf magbuf, dbbuf, planemm, segs, qtable;
     DevBuf qcounter;                         // batched form: queue head
+    // precision form (tensor-core sinc)
+    bool prec_ok = false;
+    DevBuf prec_w, prec_kb, prec_hi, prec_lo, prec_m, prec_x;
     // dispersion scorer and focus profiles
     bool win_is_one = false;                 // geometry window is exactly 1 (plain linearisation)
     DevBuf disp_x, disp_hann, disp_phase, disp_a, disp_score, xmed;
@@ -463,7 +466,8 @@ int octgb_destroy(octgb_ctx* c) {
     }
     for (DevBuf* b : {&c->w, &c->start, &c->win, &c->tw, &c->wsh, &c->s0, &c->raw, &c->apod, &c->out, &c->mm, &c->frames, &c->num,
                       &c->den, &c->plan_table, &c->run_mm, &c->magbuf, &c->dbbuf, &c->planemm, &c->segs, &c->qtable,
-                      &c->qcounter, &c->disp_x, &c->disp_hann, &c->disp_phase, &c->disp_a, &c->disp_score, &c->xmed})
+                      &c->qcounter, &c->disp_x, &c->disp_hann, &c->disp_phase, &c->disp_a, &c->disp_score, &c->xmed,
+                      &c->prec_w, &c->prec_kb, &c->prec_hi, &c->prec_lo, &c->prec_m, &c->prec_x})
         b->release();
     for (QTable* t : c->qtables) {
         t->buf.release();
@@ -592,6 +596,19 @@ int octgb_set_geometry(octgb_ctx* c, int n, int taps, const int64_t* idx, const 
            "H2D wsh");
         ck(cudaMemcpyAsync(c->s0.p, s0v.data(), s0v.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream),
            "H2D s0");
+        // tensor-core sinc tiles of the precision form (when every output block's band fits its window)
+        std::vector<uint16_t> ptiles;
+        std::vector<int> pkb;
+        c->prec_ok = build_prec_tiles(st.data(), len.data(), wt.data(), ptiles, pkb);
+        if (c->prec_ok) {
+            ck(c->prec_w.ensure(ptiles.size() * sizeof(uint16_t)), "cudaMalloc(precision tiles)");
+            ck(c->prec_kb.ensure(pkb.size() * sizeof(int)), "cudaMalloc(precision windows)");
+            ck(cudaMemcpyAsync(c->prec_w.p, ptiles.data(), ptiles.size() * sizeof(uint16_t), cudaMemcpyHostToDevice,
+                               c->stream),
+               "H2D precision tiles");
+            ck(cudaMemcpyAsync(c->prec_kb.p, pkb.data(), pkb.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream),
+               "H2D precision windows");
+        }
         ck(cudaStreamSynchronize(c->stream), "sync geometry");
         c->U = U;
         c->taps = taps;
@@ -1116,7 +1133,8 @@ int octgb_graph_end(octgb_ctx* c, int* graph_id) {
         // a buffer that grows keeps its old allocation until octgb_destroy
         for (DevBuf* b : {&c->raw, &c->apod, &c->out, &c->mm, &c->frames, &c->num, &c->den, &c->plan_table,
                           &c->run_mm, &c->magbuf, &c->dbbuf, &c->planemm, &c->segs, &c->qtable, &c->qcounter,
-                          &c->disp_x, &c->disp_hann, &c->disp_phase, &c->disp_a, &c->disp_score, &c->xmed})
+                          &c->disp_x, &c->disp_hann, &c->disp_phase, &c->disp_a, &c->disp_score, &c->xmed,
+                          &c->prec_hi, &c->prec_lo, &c->prec_m, &c->prec_x})
             b->keep_old = true;
         for (int k = 0; k < octgb_ctx::kRing; ++k) c->ring[k].keep_old = true;
         c->launches.store(c->capture_launch0);
@@ -1357,6 +1375,91 @@ int octgb_xmedian(octgb_ctx* c, const float* mag, int mag_loc, int n_frames, int
 
 int octgb_xmean(octgb_ctx* c, const float* mag, int mag_loc, int n_frames, int nx, int nz, double* out) {
     return guarded(c, [&] { xprofile(c, mag, mag_loc, n_frames, nx, nz, 1, 1, out); });
+}
+
+// ---------------------------------------------------------------------------
+// Precision form: the sinc on the tensor cores (split-FP16, three products).
+
+namespace {
+// X (B * nx lines of kN float32, device) = linearised interferogram of a raw batch
+float* precision_linearise(octgb_ctx* c, const void* raw, int dtype, int loc, int B, int interf, int apod) {
+    if (!c->has_geom) throw Error(OCTGB_ERR_STATE, "octgb_set_geometry has not been called");
+    if (!c->prec_ok)
+        throw Error(OCTGB_ERR_STATE, "the precision form needs every 64-output block's sinc band within 96 samples");
+    if (c->cancel.load()) throw Error(OCTGB_ERR_CANCELLED, "cancelled");
+    const int nx = interf - apod;
+    const int64_t n = static_cast<int64_t>(B) * nx;
+    const size_t bytes = static_cast<size_t>(B) * interf * kN * raw_elem(dtype);
+    const void* rd = stage_raw(c, raw, dtype, loc, bytes);
+    ck(c->apod.ensure(static_cast<size_t>(B) * kN * sizeof(double) + 16), "cudaMalloc(apod)");
+    SpectralArgs a{};
+    a.raw = rd;
+    a.seg[0] = rd;
+    a.n_seg = 1;
+    a.B = B;
+    a.interf = interf;
+    a.apod = apod;
+    a.nx = nx;
+    a.n_ascans = n;
+    ck(c->prec_hi.ensure(static_cast<size_t>(n) * kN * sizeof(__half)), "cudaMalloc(d hi)");
+    ck(c->prec_lo.ensure(static_cast<size_t>(n) * kN * sizeof(__half)), "cudaMalloc(d lo)");
+    ck(c->prec_m.ensure(static_cast<size_t>(n) * sizeof(float)), "cudaMalloc(line means)");
+    ck(c->prec_x.ensure(static_cast<size_t>(n) * kN * sizeof(float)), "cudaMalloc(X)");
+    ck(launch_prec_split(a, dtype, c->apod.as<double>(), c->prec_hi.as<__half>(), c->prec_lo.as<__half>(),
+                         c->prec_m.as<float>(), c->stream),
+       "background / split kernels");
+    CUtensorMap mh, ml;
+    if (!encode_prec_map(&mh, c->prec_hi.p, n) || !encode_prec_map(&ml, c->prec_lo.p, n))
+        throw Error(OCTGB_ERR_CUDA, "cuTensorMapEncodeTiled failed");
+    ck(launch_prec_sinc(mh, ml, c->prec_w.as<uint8_t>(), c->prec_kb.as<int>(), c->prec_m.as<float>(),
+                        c->prec_x.as<float>(), n, c->status_dev, c->num_sms, c->stream),
+       "tensor-core sinc kernel");
+    c->launches += 3;
+    return c->prec_x.as<float>();
+}
+}  // namespace
+
+int octgb_linearise_precision(octgb_ctx* c, const void* raw, int dtype, int loc, int B, int interf, int apod,
+                              float* x, int x_loc) {
+    return guarded(c, [&] {
+        validate_raw(raw, dtype, loc, B, interf, apod);
+        require(x != nullptr, "x is NULL");
+        if (B == 0) return;
+        const float* X = precision_linearise(c, raw, dtype, loc, B, interf, apod);
+        copy_out(c, x, x_loc, X, static_cast<size_t>(B) * (interf - apod) * kN * sizeof(float));
+        check_status(c);
+    });
+}
+
+int octgb_magnitude_precision(octgb_ctx* c, const void* raw, int dtype, int loc, int B, int interf, int apod,
+                              float* mag, int mag_loc) {
+    return guarded(c, [&] {
+        validate_raw(raw, dtype, loc, B, interf, apod);
+        require(mag != nullptr, "mag is NULL");
+        if (B == 0) return;
+        const float* X = precision_linearise(c, raw, dtype, loc, B, interf, apod);
+        const size_t ob = static_cast<size_t>(B) * (interf - apod) * kHalf * sizeof(float);
+        float* dst = mag;
+        if (mag_loc != OCTGB_DEVICE) {
+            ck(c->out.ensure(ob), "cudaMalloc(out)");
+            dst = c->out.as<float>();
+        }
+        // window (Hann/rms x dispersion phase / N), inverse FFT, |.|: the scorer's FFT kernel
+        DispArgs a{};
+        a.X = X;
+        a.phase = c->win.as<float2>();
+        a.tw = c->tw.as<float2>();
+        a.A = dst;
+        a.n_beta = 1;
+        a.nb = B;
+        a.b0 = 0;
+        a.nx = interf - apod;
+        a.rep = 1;
+        ck(launch_disp_mag(a, c->num_sms, c->stream), "FFT kernel");
+        c->launches++;
+        if (mag_loc != OCTGB_DEVICE) copy_out(c, mag, OCTGB_HOST, dst, ob);
+        check_status(c);
+    });
 }
 
 // ---------------------------------------------------------------------------

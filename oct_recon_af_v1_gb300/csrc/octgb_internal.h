@@ -156,6 +156,29 @@ cudaError_t launch_disp_metric(const float* A, int n_seg, int nx, int z_min, int
 cudaError_t launch_xmedian(const float* mag, int n_frames, int nx, int nz, int ignore_nan, int mean_mode,
                            double* out, cudaStream_t st);
 
+// precision form (precision.cu): tensor-core sinc
+constexpr int kPM = 128;                 // A-scans per tile (MMA M)
+constexpr int kPN = 64;                  // output samples per block (MMA N)
+constexpr int kPKW = 96;                 // source window per block (6 K-steps of 16)
+constexpr int kPChunks = kPKW / 8;       // 8-sample column chunks of a window
+constexpr int kPBlocks = kN / kPN;       // output blocks per A-scan
+}  // namespace octgb
+#include <cuda.h>
+#include <cuda_fp16.h>
+#include <vector>
+namespace octgb {
+cudaError_t launch_prec_split(const SpectralArgs& a, int dtype, double* apod64, __half* hi, __half* lo,
+                              float* mline, cudaStream_t st);
+cudaError_t launch_prec_sinc(const CUtensorMap& tm_hi, const CUtensorMap& tm_lo, const uint8_t* wtiles,
+                             const int* kb, const float* mline, float* X, int64_t n_ascans, int* status, int num_sms,
+                             cudaStream_t st);
+bool encode_prec_map(CUtensorMap* map, const void* base, int64_t n_ascans);
+// W tiles (per output block: hi then lo, canonical K-major no-swizzle, W x 64)
+// and window starts kb; false when a block's band exceeds the window
+bool build_prec_tiles(const int* start, const int* len, const float* wt, std::vector<uint16_t>& tiles,
+                      std::vector<int>& kb);
+size_t prec_smem_bytes();
+
 // learned beta/focus estimator (cnn.cu)
 cudaError_t launch_image_pool(const float* A, int n_probe, int nb, int nx, int z_keep, float* img, cudaStream_t st);
 cudaError_t launch_image_norm(float* img, int n_images, int64_t per_image, cudaStream_t st);

@@ -1,0 +1,400 @@
+// Precision form of the spectral stage: the banded sinc k-linearisation on
+// the 5th-generation tensor cores (tcgen05), split-FP16 with three products.
+//
+//   k_apod_mean64 + k_prec_split  the background in float64 (the float32 form
+//                 keeps the reference's float32 apodisation store, whose
+//                 rounding dominates its error against float64): d = raw -
+//                 apod, m = mean(d), d' = d - m (core/cpu_kernels.py:20-36),
+//                 split into fp16 hi = rn(d') and lo = rn(d' - hi) (22
+//                 significant bits together).
+//   k_prec_sinc   X[a][i] = sum_j W[i][j] d'[a][j] + m[a] (cpu_kernels.py:
+//                 37-41 without the window): a GEMM with M = 128 A-scans, N =
+//                 64 output samples, K = the 96-sample source window of the
+//                 output block (the band follows the chirp; the window start
+//                 kb is per block).  D = A_hi B_hi^T + A_hi B_lo^T + A_lo B_hi^T
+//                 accumulates in TMEM (float32).  W is pre-scaled by 64 (exact;
+//                 keeps the fp16 lo parts of small weights normal) and split on
+//                 the host into hi/lo tiles already in the canonical no-swizzle
+//                 K-major layout (core matrices of 8 rows x 16 bytes).
+//                 Warp roles, one CTA per SM, persistent over 128-A-scan tiles:
+//                   warp 4 lane 0  producer: per block, 12 + 12 two-dimensional
+//                                  TMA loads (cp.async.bulk.tensor, 8 samples x
+//                                  128 A-scans each) of d' hi/lo and two bulk
+//                                  copies of the W tiles, into one of 2 stages;
+//                   warp 5 lane 0  MMA issuer: 6 K-steps x 3 products of
+//                                  tcgen05.mma (M128 N64 K16), commit to the
+//                                  stage's empty barrier and the accumulator's
+//                                  full barrier; 2 accumulators of 64 TMEM
+//                                  columns alternate;
+//                   warps 0-3      epilogue: tcgen05.ld of their 32 TMEM lanes
+//                                  (A-scans) x 64 columns, X = D / 64 + m.
+//                 Every mbarrier wait is bounded (2 s); on expiry the CTA
+//                 records the status, drains its copies and MMAs, frees TMEM
+//                 and returns.
+// The FFT and |.| of the precision form are k_disp_mag's (estimate.cu) with
+// the geometry's window as the phase row.
+#include <cuda.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <cudaTypedefs.h>
+#include <stdint.h>
+
+#include <vector>
+
+#include "octgb_device.cuh"
+#include "octgb_internal.h"
+
+namespace octgb {
+namespace {
+
+constexpr uint32_t kAChunkBytes = kPM * 16;                  // 8 samples of 128 A-scans
+constexpr uint32_t kATileBytes = kPChunks * kAChunkBytes;    // 24576
+constexpr uint32_t kBChunkBytes = kPN * 16;                  // 8 samples of 64 outputs
+constexpr uint32_t kBTileBytes = kPChunks * kBChunkBytes;    // 12288
+constexpr uint32_t kStageBytes = 2 * kATileBytes + 2 * kBTileBytes;
+constexpr int kPStages = 2;
+constexpr int kPThreads = 192;
+
+struct PrecSmem {
+    alignas(1024) uint8_t stage[kPStages][kStageBytes];      // A_hi | A_lo | B_hi | B_lo
+    // every byte a descriptor of either operand layout could address stays
+    // inside the allocation
+    uint8_t slack[16384];
+    uint64_t full[kPStages], empty[kPStages], tfull[2], tempty[2], drain;
+    uint32_t tmem_base;
+    int abort;
+};
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+            smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// shared-memory matrix descriptor: no swizzle, K-major; lbo = byte stride
+// between core matrices along K, sbo = along M/N (8-row groups)
+__device__ __forceinline__ uint64_t smem_desc(const void* p, uint32_t lbo, uint32_t sbo) {
+    const uint64_t a = smem_u32(p);
+    return ((a >> 4) & 0x3fffull) | (static_cast<uint64_t>((lbo >> 4) & 0x3fff) << 16) |
+           (static_cast<uint64_t>((sbo >> 4) & 0x3fff) << 32) | (1ull << 46);
+}
+
+// kind::f16 instruction descriptor: f16 x f16 -> f32, K-major A and B, M = 128, N = 64
+constexpr uint32_t kIdesc = (1u << 4) | (static_cast<uint32_t>(kPN >> 3) << 17) | (static_cast<uint32_t>(kPM >> 4) << 24);
+
+__device__ __forceinline__ void mma_f16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate)
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// 32 consecutive TMEM columns of this warp's 32 lanes (one lane per thread)
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ bool wait_or_abort(uint64_t* bar, uint32_t parity, PrecSmem& S, int* status) {
+    if (*reinterpret_cast<volatile int*>(&S.abort)) return false;
+    if (mbar_wait_bounded(bar, parity, status)) return true;
+    atomicExch(&S.abort, 1);
+    return false;
+}
+
+__global__ void __launch_bounds__(kPThreads, 1)
+    k_prec_sinc(const __grid_constant__ CUtensorMap tm_hi, const __grid_constant__ CUtensorMap tm_lo,
+                const uint8_t* __restrict__ wtiles, const int* __restrict__ kb, const float* __restrict__ mline,
+                float* __restrict__ X, int64_t n_ascans, int* status) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    // tensor-copy destinations want 128-byte alignment: align the window by hand
+    PrecSmem& S = *reinterpret_cast<PrecSmem*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int64_t n_tiles = (n_ascans + kPM - 1) / kPM;
+    const int64_t my_tiles = blockIdx.x < n_tiles ? (n_tiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+    const int64_t n_q = my_tiles * kPBlocks;                   // (tile, block) steps of this CTA
+
+    if (tid == 0) {
+        for (int s = 0; s < kPStages; ++s) {
+            mbar_init(&S.full[s], 1);
+            mbar_init(&S.empty[s], 1);
+        }
+        for (int d = 0; d < 2; ++d) {
+            mbar_init(&S.tfull[d], 1);
+            mbar_init(&S.tempty[d], 4);
+        }
+        mbar_init(&S.drain, 1);
+        S.abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;" ::"r"(smem_u32(&S.tmem_base))
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = S.tmem_base;
+
+    if (warp == 4 && lane == 0) {
+        // ---------------- producer
+        int64_t q = 0;
+        for (; q < n_q; ++q) {
+            const int s = static_cast<int>(q % kPStages);
+            const uint32_t ph = static_cast<uint32_t>(q / kPStages) & 1u;
+            if (!wait_or_abort(&S.empty[s], ph ^ 1u, S, status)) break;
+            const int64_t tile = blockIdx.x + (q / kPBlocks) * gridDim.x;
+            const int b = static_cast<int>(q % kPBlocks);
+            uint8_t* st = S.stage[s];
+            mbar_expect_tx(&S.full[s], kStageBytes);
+            const int x0 = kb[b], y0 = static_cast<int>(tile * kPM);
+            for (int c = 0; c < kPChunks; ++c) {
+                tma_load_2d(st + c * kAChunkBytes, &tm_hi, x0 + 8 * c, y0, &S.full[s]);
+                tma_load_2d(st + kATileBytes + c * kAChunkBytes, &tm_lo, x0 + 8 * c, y0, &S.full[s]);
+            }
+            const uint8_t* wsrc = wtiles + static_cast<size_t>(b) * 2 * kBTileBytes;
+            tma_bulk_g2s(st + 2 * kATileBytes, wsrc, kBTileBytes, &S.full[s]);
+            tma_bulk_g2s(st + 2 * kATileBytes + kBTileBytes, wsrc + kBTileBytes, kBTileBytes, &S.full[s]);
+        }
+        // drain: copies still in flight land before the CTA's memory is released
+        for (int64_t r = q - kPStages; r < q; ++r) {
+            if (r < 0) continue;
+            mbar_wait_bounded(&S.full[r % kPStages], static_cast<uint32_t>(r / kPStages) & 1u, status);
+        }
+    } else if (warp == 5 && lane == 0) {
+        // ---------------- MMA issuer
+        for (int64_t q = 0; q < n_q; ++q) {
+            const int s = static_cast<int>(q % kPStages);
+            const uint32_t ph = static_cast<uint32_t>(q / kPStages) & 1u;
+            const int d = static_cast<int>(q & 1);
+            const uint32_t dph = static_cast<uint32_t>(q >> 1) & 1u;
+            if (!wait_or_abort(&S.full[s], ph, S, status)) break;
+            if (!wait_or_abort(&S.tempty[d], dph ^ 1u, S, status)) break;
+            tc_fence_after();
+            const uint32_t dt = tmem + static_cast<uint32_t>(d * kPN);
+            const uint8_t* st = S.stage[s];
+#pragma unroll
+            for (int k = 0; k < kPKW / 16; ++k) {
+                const uint64_t ah = smem_desc(st + k * 2 * kAChunkBytes, kAChunkBytes, 128);
+                const uint64_t al = smem_desc(st + kATileBytes + k * 2 * kAChunkBytes, kAChunkBytes, 128);
+                const uint64_t bh = smem_desc(st + 2 * kATileBytes + k * 2 * kBChunkBytes, kBChunkBytes, 128);
+                const uint64_t bl = smem_desc(st + 2 * kATileBytes + kBTileBytes + k * 2 * kBChunkBytes, kBChunkBytes,
+                                              128);
+                mma_f16(dt, ah, bh, k > 0 ? 1u : 0u);
+                mma_f16(dt, ah, bl, 1u);
+                mma_f16(dt, al, bh, 1u);
+            }
+            mma_commit(&S.empty[s]);
+            mma_commit(&S.tfull[d]);
+        }
+        // drain: every MMA issued has completed
+        mma_commit(&S.drain);
+        mbar_wait_bounded(&S.drain, 0, status);
+    } else if (warp < 4) {
+        // ---------------- epilogue
+        const uint32_t lane_base = static_cast<uint32_t>(32 * warp) << 16;
+        for (int64_t q = 0; q < n_q; ++q) {
+            const int d = static_cast<int>(q & 1);
+            const uint32_t dph = static_cast<uint32_t>(q >> 1) & 1u;
+            bool ok = true;
+            if (lane == 0) ok = wait_or_abort(&S.tfull[d], dph, S, status);
+            ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+            if (!ok) break;
+            tc_fence_after();
+            float v[2][32];
+            tmem_ld32(tmem + lane_base + static_cast<uint32_t>(d * kPN), v[0]);
+            tmem_ld32(tmem + lane_base + static_cast<uint32_t>(d * kPN + 32), v[1]);
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&S.tempty[d]);
+            const int64_t tile = blockIdx.x + (q / kPBlocks) * gridDim.x;
+            const int b = static_cast<int>(q % kPBlocks);
+            const int64_t a = tile * kPM + 32 * warp + lane;
+            if (a < n_ascans) {
+                const float m = mline[a];
+                float4* out = reinterpret_cast<float4*>(X + a * kN + b * kPN);
+#pragma unroll
+                for (int h = 0; h < 2; ++h)
+#pragma unroll
+                    for (int c = 0; c < 8; ++c)
+                        out[h * 8 + c] = make_float4(fmaf(v[h][4 * c], 1.0f / 64, m), fmaf(v[h][4 * c + 1], 1.0f / 64, m),
+                                                     fmaf(v[h][4 * c + 2], 1.0f / 64, m),
+                                                     fmaf(v[h][4 * c + 3], 1.0f / 64, m));
+            }
+        }
+    }
+    __syncwarp();                                       // role lanes rejoin their warps
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;" ::"r"(tmem) : "memory");
+}
+
+// float64 apodisation mean per (B-scan, sample): exact sum / apod
+template <typename RawT>
+__global__ void k_apod_mean64(const SpectralArgs a, double* __restrict__ out) {
+    const int b = blockIdx.y;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= kN) return;
+    const RawT* p = static_cast<const RawT*>(a.raw) + static_cast<int64_t>(b) * a.interf * kN + j;
+    double s = 0.0;
+    for (int k = 0; k < a.apod; ++k) s += static_cast<double>(p[static_cast<int64_t>(k) * kN]);
+    out[static_cast<int64_t>(b) * kN + j] = s / a.apod;
+}
+
+// One CTA (256 threads) per A-scan: the background in float64 (d = raw -
+// apod, m = mean(d), d' = d - m), then d' split to fp16 hi = rn(d') and
+// lo = rn(d' - hi), both roundings from float64.
+template <typename RawT>
+__global__ void __launch_bounds__(256) k_prec_split(const SpectralArgs a, const double* __restrict__ apod64,
+                                                    __half* __restrict__ hi, __half* __restrict__ lo,
+                                                    float* __restrict__ mline) {
+    __shared__ double red[8];
+    const int64_t as = blockIdx.x;                                // A-scan
+    const int64_t b = as / a.nx, x = as - b * a.nx;
+    const RawT* row = static_cast<const RawT*>(a.raw) + (b * a.interf + a.apod + x) * kN;
+    const double* ap = apod64 + b * kN;
+    double d[8];
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const int j = threadIdx.x + 256 * k;
+        d[k] = static_cast<double>(row[j]) - ap[j];
+        s += d[k];
+    }
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    double t = 0.0;
+#pragma unroll
+    for (int w = 0; w < 8; ++w) t += red[w];
+    const double m = t / kN;
+    if (threadIdx.x == 0) mline[as] = static_cast<float>(m);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const int j = threadIdx.x + 256 * k;
+        const double v = d[k] - m;
+        const __half h = __double2half(v);
+        hi[as * kN + j] = h;
+        lo[as * kN + j] = __double2half(v - static_cast<double>(__half2float(h)));
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_prec_split(const SpectralArgs& a, int dtype, double* apod64, __half* hi, __half* lo,
+                              float* mline, cudaStream_t st) {
+    const int64_t n = a.n_ascans;
+    if (n == 0) return cudaSuccess;
+    const dim3 ga(kN / 256, a.B);
+    const unsigned int g = static_cast<unsigned int>(n);
+    if (dtype == 0) {
+        k_apod_mean64<uint16_t><<<ga, 256, 0, st>>>(a, apod64);
+        k_prec_split<uint16_t><<<g, 256, 0, st>>>(a, apod64, hi, lo, mline);
+    } else if (dtype == 1) {
+        k_apod_mean64<int16_t><<<ga, 256, 0, st>>>(a, apod64);
+        k_prec_split<int16_t><<<g, 256, 0, st>>>(a, apod64, hi, lo, mline);
+    } else {
+        k_apod_mean64<float><<<ga, 256, 0, st>>>(a, apod64);
+        k_prec_split<float><<<g, 256, 0, st>>>(a, apod64, hi, lo, mline);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_prec_sinc(const CUtensorMap& tm_hi, const CUtensorMap& tm_lo, const uint8_t* wtiles,
+                             const int* kb, const float* mline, float* X, int64_t n_ascans, int* status, int num_sms,
+                             cudaStream_t st) {
+    const size_t smem = sizeof(PrecSmem) + 1024;                  // + alignment of the dynamic window
+    cudaError_t e = cudaFuncSetAttribute(k_prec_sinc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(smem));
+    if (e != cudaSuccess) return e;
+    const int64_t tiles = (n_ascans + kPM - 1) / kPM;
+    const int grid = static_cast<int>(tiles < num_sms ? tiles : num_sms);
+    if (grid < 1) return cudaSuccess;
+    k_prec_sinc<<<grid, kPThreads, smem, st>>>(tm_hi, tm_lo, wtiles, kb, mline, X, n_ascans, status);
+    return cudaGetLastError();
+}
+
+size_t prec_smem_bytes() { return sizeof(PrecSmem) + 1024; }
+
+bool encode_prec_map(CUtensorMap* map, const void* base, int64_t n_ascans) {
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    if (encode == nullptr) {
+        cudaDriverEntryPointQueryResult q;
+        void* fn = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess || fn == nullptr)
+            return false;
+        encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    }
+    const cuuint64_t dims[2] = {static_cast<cuuint64_t>(kN), static_cast<cuuint64_t>(n_ascans)};
+    const cuuint64_t strides[1] = {static_cast<cuuint64_t>(kN) * sizeof(__half)};
+    const cuuint32_t box[2] = {8, static_cast<cuuint32_t>(kPM)};
+    const cuuint32_t estr[2] = {1, 1};
+    return encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+bool build_prec_tiles(const int* start, const int* len, const float* wt, std::vector<uint16_t>& tiles,
+                      std::vector<int>& kb) {
+    tiles.assign(static_cast<size_t>(kPBlocks) * 2 * kBTileBytes / 2, 0);
+    kb.assign(kPBlocks, 0);
+    for (int b = 0; b < kPBlocks; ++b) {
+        int lo = kN, hi = 0;
+        for (int r = 0; r < kPN; ++r) {
+            const int i = b * kPN + r;
+            lo = lo < start[i] ? lo : start[i];
+            hi = hi > start[i] + len[i] ? hi : start[i] + len[i];
+        }
+        const int k0 = lo & ~7;
+        if (hi - k0 > kPKW) return false;
+        kb[b] = k0;
+        uint16_t* th = tiles.data() + static_cast<size_t>(b) * kBTileBytes;         // 2-byte units: hi then lo
+        uint16_t* tl = th + kBTileBytes / 2;
+        for (int r = 0; r < kPN; ++r) {
+            const int i = b * kPN + r;
+            for (int t = 0; t < len[i]; ++t) {
+                const int col = start[i] + t - k0;                                    // 0 .. kPKW-1
+                const float w = wt[static_cast<size_t>(t) * kN + i] * 64.0f;          // exact scaling
+                const __half h = __float2half_rn(w);
+                const __half l = __float2half_rn(w - __half2float(h));
+                const size_t off = static_cast<size_t>(col >> 3) * (kBChunkBytes / 2) + static_cast<size_t>(r) * 8 +
+                                   (col & 7);
+                th[off] = __half_as_ushort(h);
+                tl[off] = __half_as_ushort(l);
+            }
+        }
+    }
+    return true;
+}
+
+}  // namespace octgb

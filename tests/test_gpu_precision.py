@@ -1,0 +1,80 @@
+"""Precision form (tensor-core sinc) against the float64 oracle, stage by
+stage, beside the float32 form: (c) the linearised interferogram, (e) the
+magnitude, (f) the legacy codes at one shared clim (the parity criterion of
+the reconstruction)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from oracle import numerics as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def case():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import oct_recon_af_v1_gb300 as pkg
+    pkg.build()
+    from oct_recon_af_v1_gb300 import geometry as G
+    from oct_recon_af_v1_gb300 import synthetic as S
+    from oct_recon_af_v1_gb300._lib import Context
+    lam = S.lambda_nm()
+    beta = S.beta_ref_from_px(1e-5)
+    raw = S.generate_numpy(4, 300, 25, seed=17)           # 1200 A-scans: 9 tiles of 128, the last partial
+    og = O.spectral_geometry(lam, beta, 1.33)
+    sg = G.build_spectral_geometry(lam, beta, 1.33)
+    sg0 = G.build_spectral_geometry(lam, 0.0, 1.33)
+    ctx = Context(0)
+    yield dict(torch=torch, ctx=ctx, raw=raw, og=og, sg=sg, sg0=sg0)
+    ctx.close()
+
+
+def rel(a, b):
+    return float(np.abs(a - b).max() / np.abs(b).max())
+
+
+def test_stage_c_linearised(case):
+    ctx, raw, og, sg0 = case["ctx"], case["raw"], case["og"], case["sg0"]
+    ctx.set_geometry(sg0.sinc_idx, sg0.sinc_w, np.ones(len(sg0.lambda_nm), np.complex128))
+    x64 = O.linearise_numpy(raw, og, 25, np.float64)
+    xp = ctx.linearise_precision(raw, 25)
+    xf = np.real(ctx.fused_pre_fft(raw, 25))                 # the float32 form with a window of ones
+    e_p, e_f = rel(xp, x64), rel(xf, x64)
+    print(f"stage (c) max-norm relative error vs float64: precision {e_p:.2e}, float32 {e_f:.2e}")
+    assert e_p < 1e-5 and e_f < 1e-5
+    # background-free line: the float64 background makes the precision form's
+    # stage (c) closer to float64 than the float32 form's
+    assert e_p <= e_f
+
+
+def test_stage_e_and_codes(case):
+    ctx, raw, og, sg = case["ctx"], case["raw"], case["og"], case["sg"]
+    ctx.set_geometry(sg.sinc_idx, sg.sinc_w, sg.window)
+    m64 = O.magnitude_numpy(raw, og, 25, np.float64)
+    mp = ctx.magnitude_precision(raw, 25)
+    mf = ctx.magnitude(raw, 25)
+    e_p, e_f = rel(mp, m64), rel(mf, m64)
+    with np.errstate(divide="ignore"):
+        d64, dp, df = (20 * np.log10(m) for m in (m64, mp, mf))
+    fin = np.isfinite(d64)
+    clim = (float(d64[fin].min()), float(d64[fin].max()))
+    b64, bp, bf = (O.db_to_bits(d, clim).astype(np.int64) for d in (d64, dp, df))
+    lsb_p, lsb_f = np.abs(bp - b64), np.abs(bf - b64)
+    floor = np.median(d64[fin]) - 20
+    hi = d64 > floor
+    rows = [("precision", e_p, lsb_p), ("float32", e_f, lsb_f)]
+    for name, e, lsb in rows:
+        print(f"{name:9s} stage (e) rel {e:.2e}  codes: {100 * np.mean(lsb == 0):.2f}% exact, max {lsb.max()} LSB, "
+              f"max {lsb[hi].max()} LSB above median-20 dB")
+    assert e_p < 1e-5
+    # the float32 form (and the reference's float32 path) is ~90 % exact
+    # against float64 because of its float32 apodisation store; the precision
+    # form keeps the background in float64 (measured 99.69 %, max 9 LSB: the
+    # largest differences sit at deep noise-floor nulls, where the float32
+    # FFT's rounding dominates)
+    assert np.mean(lsb_p == 0) >= 0.995 and lsb_p.max() <= 12 and lsb_p[hi].max() <= 1
+    assert np.mean(lsb_p == 0) > np.mean(lsb_f == 0) and lsb_p.max() <= lsb_f.max()
