@@ -229,6 +229,8 @@ def gpu_arm(args, rank, world):
     ctx.set_stream(stream.cuda_stream)
     if args.config == 0:
         return gpu_arm_config0(args, rank, world, torch, ctx)
+    if args.config == 2:
+        return gpu_arm_config2(args, rank, world, torch, ctx, stream, dev)
     if args.config == 3:
         return gpu_arm_config3(args, rank, world, torch, ctx, stream, dev)
     if args.config == 4:
@@ -429,6 +431,75 @@ def gpu_arm_config3(args, rank, world, torch, ctx, stream, dev):
             "e2e": {"value": ascans / (ms_e2e * 1e-3), "unit": "A-scans/s", "ms_per_step": ms_e2e,
                     "h2d_bytes_per_step": raw_bytes, "d2h_bytes_per_step": out_bytes}}
     return line
+
+
+def gpu_arm_config2(args, rank, world, torch, ctx, stream, dev):
+    """Config 2: the config-1 tiles through the precision form of the spectral
+    stage (tensor-core sinc, float64 background), beside the float32 form."""
+    vol = Volume(ctx, torch, dev, host_copy=False, bscans=args.bscans)
+    tiles = list(vol.raw.values())
+    B, interf = tiles[0].shape[0], tiles[0].shape[1]
+    nxa = interf - APOD
+    mag = torch.empty((B, nxa, 1024), dtype=torch.float32, device=dev)
+    X = torch.empty((B, nxa, 2048), dtype=torch.float32, device=dev)
+    ascans = len(tiles) * B * nxa
+
+    def prec_step():
+        for t in tiles:
+            ctx.magnitude_precision(t, APOD, mag, raw_dtype=0)
+
+    def sinc_step():
+        for t in tiles:
+            ctx.linearise_precision(t, APOD, X, raw_dtype=0)
+
+    def f32_step():
+        for t in tiles:
+            ctx.magnitude(t, APOD, mag, raw_dtype=0)
+
+    def timed(fn, steps, warm):
+        for _ in range(warm):
+            fn()
+        torch.cuda.synchronize()
+        n0 = ctx.launches
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps, ctx.launches - n0
+
+    clocks = Clocks(int(os.environ.get("LOCAL_RANK", 0)))
+    clocks.start()
+    ms, launches = timed(prec_step, args.steps, args.warmup)
+    clk = clocks.stop()
+    ms_sinc, _ = timed(sinc_step, args.steps, 1)
+    ms_f32, _ = timed(f32_step, args.steps, 1)
+    hbm, src = peaks()
+    flops_per_ascan = 32 * 3 * 2 * 64 * 96                     # dense MMA tiles executed per A-scan
+    sinc_bytes = ascans * (interf / nxa * 2048 * 2 + 2048 * 4)   # raw in, X out
+    try:
+        tf_peak = float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text()).get("bf16_tflops"))
+    except Exception:
+        tf_peak = 1900.0
+    return {"metric": METRIC, "value": ascans / (ms * 1e-3), "unit": "A-scans/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (split-fp16 tensor-core sinc, uint16 in)",
+            "data": "synthetic (seeded, generated on device)",
+            "config": dict(config1_desc(args.bscans),
+                           workload="config2: config-1 tiles (12 x 270 B-scans x 1000 A-scans x 2048 uint16) through "
+                                    "the precision form of the spectral stage (float64 background, tcgen05 "
+                                    "split-FP16 sinc, FFT, |.|), magnitudes out"),
+            "gpu_launches": int(launches),
+            "roofline": {"bound": "hbm", "achieved": sinc_bytes / (ms_sinc * 1e-3) / 1e9, "peak": hbm, "unit": "GB/s",
+                         "frac": sinc_bytes / (ms_sinc * 1e-3) / 1e9 / hbm, "traffic": None,
+                         "kernel": "precision stage (c): float64 background + split + tcgen05 sinc, raw in / X out",
+                         "ms_per_step": ms_sinc, "peak_source": src + " (burst copy)",
+                         "tensor": {"achieved_tflops": ascans * flops_per_ascan / (ms_sinc * 1e-3) / 1e12,
+                                    "peak_tflops": tf_peak, "flops_per_ascan": flops_per_ascan,
+                                    "note": "dense 128x64x96 MMA tiles x 3 split products; time of the whole stage"}},
+            "clocks": clk,
+            "float32_form": {"value": ascans / (ms_f32 * 1e-3), "unit": "A-scans/s", "ms_per_step": ms_f32}}
 
 
 def config4_desc(n_train, n_base, epochs):
@@ -803,7 +874,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--config", type=int, default=1, choices=[0, 1, 3, 4])
+    ap.add_argument("--config", type=int, default=1, choices=[0, 1, 2, 3, 4])
     ap.add_argument("--train4", type=int, default=20000, help="training images of the learned estimator (config 4)")
     ap.add_argument("--epochs4", type=int, default=8, help="training epochs (config 4)")
     ap.add_argument("--tiles3", type=int, default=64, help="tiles of the batched workload (config 3)")

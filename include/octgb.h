@@ -110,16 +110,18 @@ int octgb_db(octgb_ctx *ctx, const void *raw, int raw_dtype, int raw_loc, int B,
  * GEMM on the tensor cores (tcgen05.mma, split-FP16 with three products,
  * float32 accumulation in TMEM; 128 A-scans x 64 output samples x a
  * 96-sample source window per block).  The background (apodisation mean, line
- * mean) is float64: this form is closer to the float64 path than the
- * reference's float32 path, which rounds the apodisation mean to float32
- * (core/cpu_kernels.py:20-25).  Requires every 64-output block's
+ * mean) is exact (integer sums; float64 for float32 raws): this form is
+ * closer to the float64 path than the reference's float32 path, which rounds
+ * the apodisation mean to float32 (core/cpu_kernels.py:20-25).  Requires
+ * every 64-output block's
  * sinc band to fit in 96 source samples (OCTGB_ERR_STATE otherwise) and
  * |raw - apod - mean| < 65504 (the fp16 range).
  * octgb_linearise_precision: stage (c) only, the linearised interferogram
  *   (B, interf-apod, n) float32 without the window (SpectralProcessor.linearise,
  *   core/spectral.py:118-134);
  * octgb_magnitude_precision: the magnitude of octgb_magnitude
- *   (core/spectral.py:136-153). */
+ *   (core/spectral.py:136-153).
+ * With device input and device output neither call synchronises. */
 int octgb_linearise_precision(octgb_ctx *ctx, const void *raw, int raw_dtype, int raw_loc, int B, int interf,
                               int apod_size, float *x, int x_loc);
 int octgb_magnitude_precision(octgb_ctx *ctx, const void *raw, int raw_dtype, int raw_loc, int B, int interf,

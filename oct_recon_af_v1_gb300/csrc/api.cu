@@ -1382,7 +1382,8 @@ int octgb_xmean(octgb_ctx* c, const float* mag, int mag_loc, int n_frames, int n
 
 namespace {
 // X (B * nx lines of kN float32, device) = linearised interferogram of a raw batch
-float* precision_linearise(octgb_ctx* c, const void* raw, int dtype, int loc, int B, int interf, int apod) {
+float* precision_linearise(octgb_ctx* c, const void* raw, int dtype, int loc, int B, int interf, int apod,
+                           float* x_dev = nullptr) {
     if (!c->has_geom) throw Error(OCTGB_ERR_STATE, "octgb_set_geometry has not been called");
     if (!c->prec_ok)
         throw Error(OCTGB_ERR_STATE, "the precision form needs every 64-output block's sinc band within 96 samples");
@@ -1404,18 +1405,22 @@ float* precision_linearise(octgb_ctx* c, const void* raw, int dtype, int loc, in
     ck(c->prec_hi.ensure(static_cast<size_t>(n) * kN * sizeof(__half)), "cudaMalloc(d hi)");
     ck(c->prec_lo.ensure(static_cast<size_t>(n) * kN * sizeof(__half)), "cudaMalloc(d lo)");
     ck(c->prec_m.ensure(static_cast<size_t>(n) * sizeof(float)), "cudaMalloc(line means)");
-    ck(c->prec_x.ensure(static_cast<size_t>(n) * kN * sizeof(float)), "cudaMalloc(X)");
-    ck(launch_prec_split(a, dtype, c->apod.as<double>(), c->prec_hi.as<__half>(), c->prec_lo.as<__half>(),
-                         c->prec_m.as<float>(), c->stream),
+    float* X = x_dev;
+    if (X == nullptr) {
+        ck(c->prec_x.ensure(static_cast<size_t>(n) * kN * sizeof(float)), "cudaMalloc(X)");
+        X = c->prec_x.as<float>();
+    }
+    ck(launch_prec_split(a, dtype, c->apod.p, c->prec_hi.as<__half>(), c->prec_lo.as<__half>(),
+                         c->prec_m.as<float>(), c->num_sms, c->stream),
        "background / split kernels");
     CUtensorMap mh, ml;
     if (!encode_prec_map(&mh, c->prec_hi.p, n) || !encode_prec_map(&ml, c->prec_lo.p, n))
         throw Error(OCTGB_ERR_CUDA, "cuTensorMapEncodeTiled failed");
-    ck(launch_prec_sinc(mh, ml, c->prec_w.as<uint8_t>(), c->prec_kb.as<int>(), c->prec_m.as<float>(),
-                        c->prec_x.as<float>(), n, c->status_dev, c->num_sms, c->stream),
+    ck(launch_prec_sinc(mh, ml, c->prec_w.as<uint8_t>(), c->prec_kb.as<int>(), c->prec_m.as<float>(), X, n,
+                        c->status_dev, c->num_sms, c->stream),
        "tensor-core sinc kernel");
     c->launches += 3;
-    return c->prec_x.as<float>();
+    return X;
 }
 }  // namespace
 
@@ -1425,6 +1430,12 @@ int octgb_linearise_precision(octgb_ctx* c, const void* raw, int dtype, int loc,
         validate_raw(raw, dtype, loc, B, interf, apod);
         require(x != nullptr, "x is NULL");
         if (B == 0) return;
+        if (x_loc == OCTGB_DEVICE) {
+            require((reinterpret_cast<uintptr_t>(x) & 15u) == 0, "device x must be 16-byte aligned");
+            precision_linearise(c, raw, dtype, loc, B, interf, apod, x);
+            if (loc != OCTGB_DEVICE) check_status(c);
+            return;
+        }
         const float* X = precision_linearise(c, raw, dtype, loc, B, interf, apod);
         copy_out(c, x, x_loc, X, static_cast<size_t>(B) * (interf - apod) * kN * sizeof(float));
         check_status(c);
@@ -1458,7 +1469,7 @@ int octgb_magnitude_precision(octgb_ctx* c, const void* raw, int dtype, int loc,
         ck(launch_disp_mag(a, c->num_sms, c->stream), "FFT kernel");
         c->launches++;
         if (mag_loc != OCTGB_DEVICE) copy_out(c, mag, OCTGB_HOST, dst, ob);
-        check_status(c);
+        if (mag_loc != OCTGB_DEVICE || loc != OCTGB_DEVICE) check_status(c);
     });
 }
 

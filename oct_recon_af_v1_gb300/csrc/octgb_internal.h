@@ -167,8 +167,9 @@ constexpr int kPBlocks = kN / kPN;       // output blocks per A-scan
 #include <cuda_fp16.h>
 #include <vector>
 namespace octgb {
-cudaError_t launch_prec_split(const SpectralArgs& a, int dtype, double* apod64, __half* hi, __half* lo,
-                              float* mline, cudaStream_t st);
+// apod_scratch: B x kN int32 (integer raws) or float64 (float32 raws)
+cudaError_t launch_prec_split(const SpectralArgs& a, int dtype, void* apod_scratch, __half* hi, __half* lo,
+                              float* mline, int num_sms, cudaStream_t st);
 cudaError_t launch_prec_sinc(const CUtensorMap& tm_hi, const CUtensorMap& tm_lo, const uint8_t* wtiles,
                              const int* kb, const float* mline, float* X, int64_t n_ascans, int* status, int num_sms,
                              cudaStream_t st);

@@ -1,12 +1,14 @@
 // Precision form of the spectral stage: the banded sinc k-linearisation on
 // the 5th-generation tensor cores (tcgen05), split-FP16 with three products.
 //
-//   k_apod_mean64 + k_prec_split  the background in float64 (the float32 form
+//   k_apod_sum + k_prec_split_int  the background exactly (the float32 form
 //                 keeps the reference's float32 apodisation store, whose
-//                 rounding dominates its error against float64): d = raw -
-//                 apod, m = mean(d), d' = d - m (core/cpu_kernels.py:20-36),
-//                 split into fp16 hi = rn(d') and lo = rn(d' - hi) (22
-//                 significant bits together).
+//                 rounding dominates its error against float64): for integer
+//                 raws d' = raw - apod - m (core/cpu_kernels.py:20-36) is an
+//                 exact int64 ratio rounded twice in float32 (float64 for
+//                 float32 raws, k_apod_mean64 + k_prec_split_f32), then split
+//                 into fp16 hi = rn(d') and lo = rn(d' - hi) (22 significant
+//                 bits together).
 //   k_prec_sinc   X[a][i] = sum_j W[i][j] d'[a][j] + m[a] (cpu_kernels.py:
 //                 37-41 without the window): a GEMM with M = 128 A-scans, N =
 //                 64 output samples, K = the 96-sample source window of the
@@ -257,73 +259,128 @@ __global__ void __launch_bounds__(kPThreads, 1)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;" ::"r"(tmem) : "memory");
 }
 
-// float64 apodisation mean per (B-scan, sample): exact sum / apod
+// Integer raws: exact apodisation sums S[b][j] (int32).
 template <typename RawT>
-__global__ void k_apod_mean64(const SpectralArgs a, double* __restrict__ out) {
+__global__ void k_apod_sum(const SpectralArgs a, int* __restrict__ out) {
     const int b = blockIdx.y;
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= kN) return;
     const RawT* p = static_cast<const RawT*>(a.raw) + static_cast<int64_t>(b) * a.interf * kN + j;
+    int s = 0;
+    for (int k = 0; k < a.apod; ++k) s += static_cast<int>(p[static_cast<int64_t>(k) * kN]);
+    out[static_cast<int64_t>(b) * kN + j] = s;
+}
+
+__device__ __forceinline__ void store_split(float v, __half* hi, __half* lo) {
+    const __half h = __float2half_rn(v);
+    *hi = h;
+    *lo = __float2half_rn(v - __half2float(h));            // exact difference in float32
+}
+
+// Integer raws, 256 threads, persistent over A-scans.  With N_j = apod*raw_j
+// - S_j (exact) the background-free line is d'_j = (2048 N_j - sum N) /
+// (2048 apod): an exact int64 numerator and two float32 roundings, each
+// relative to d'_j itself (the float32 form's apodisation store instead
+// errs by ~1e-7 of the ~2e4-count background).  m = sum N / (2048 apod).
+template <typename RawT>
+__global__ void __launch_bounds__(256) k_prec_split_int(const SpectralArgs a, const int* __restrict__ apod_sum,
+                                                        __half* __restrict__ hi, __half* __restrict__ lo,
+                                                        float* __restrict__ mline) {
+    __shared__ long long red[8];
+    const float den = static_cast<float>(kN) * static_cast<float>(a.apod);   // exact
+    for (int64_t as = blockIdx.x; as < a.n_ascans; as += gridDim.x) {
+        const int64_t b = as / a.nx, x = as - b * a.nx;
+        const RawT* row = static_cast<const RawT*>(a.raw) + (b * a.interf + a.apod + x) * kN;
+        const int* S = apod_sum + b * kN;
+        int n[8];
+        long long s = 0;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const int j = threadIdx.x + 256 * k;
+            n[k] = a.apod * static_cast<int>(row[j]) - S[j];
+            s += n[k];
+        }
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+        __syncthreads();
+        long long t = 0;
+#pragma unroll
+        for (int w = 0; w < 8; ++w) t += red[w];
+        __syncthreads();
+        if (threadIdx.x == 0) mline[as] = static_cast<float>(t) / den;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const int j = threadIdx.x + 256 * k;
+            const long long q = static_cast<long long>(kN) * n[k] - t;
+            store_split(static_cast<float>(q) / den, hi + as * kN + j, lo + as * kN + j);
+        }
+    }
+}
+
+// float32 raws: the background in float64 (apodisation mean, line mean).
+__global__ void k_apod_mean64(const SpectralArgs a, double* __restrict__ out) {
+    const int b = blockIdx.y;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= kN) return;
+    const float* p = static_cast<const float*>(a.raw) + static_cast<int64_t>(b) * a.interf * kN + j;
     double s = 0.0;
     for (int k = 0; k < a.apod; ++k) s += static_cast<double>(p[static_cast<int64_t>(k) * kN]);
     out[static_cast<int64_t>(b) * kN + j] = s / a.apod;
 }
 
-// One CTA (256 threads) per A-scan: the background in float64 (d = raw -
-// apod, m = mean(d), d' = d - m), then d' split to fp16 hi = rn(d') and
-// lo = rn(d' - hi), both roundings from float64.
-template <typename RawT>
-__global__ void __launch_bounds__(256) k_prec_split(const SpectralArgs a, const double* __restrict__ apod64,
-                                                    __half* __restrict__ hi, __half* __restrict__ lo,
-                                                    float* __restrict__ mline) {
+__global__ void __launch_bounds__(256) k_prec_split_f32(const SpectralArgs a, const double* __restrict__ apod64,
+                                                        __half* __restrict__ hi, __half* __restrict__ lo,
+                                                        float* __restrict__ mline) {
     __shared__ double red[8];
-    const int64_t as = blockIdx.x;                                // A-scan
-    const int64_t b = as / a.nx, x = as - b * a.nx;
-    const RawT* row = static_cast<const RawT*>(a.raw) + (b * a.interf + a.apod + x) * kN;
-    const double* ap = apod64 + b * kN;
-    double d[8];
-    double s = 0.0;
+    for (int64_t as = blockIdx.x; as < a.n_ascans; as += gridDim.x) {
+        const int64_t b = as / a.nx, x = as - b * a.nx;
+        const float* row = static_cast<const float*>(a.raw) + (b * a.interf + a.apod + x) * kN;
+        const double* ap = apod64 + b * kN;
+        double d[8];
+        double s = 0.0;
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
-        const int j = threadIdx.x + 256 * k;
-        d[k] = static_cast<double>(row[j]) - ap[j];
-        s += d[k];
-    }
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
-    __syncthreads();
-    double t = 0.0;
+        for (int k = 0; k < 8; ++k) {
+            const int j = threadIdx.x + 256 * k;
+            d[k] = static_cast<double>(row[j]) - ap[j];
+            s += d[k];
+        }
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+        __syncthreads();
+        double t = 0.0;
 #pragma unroll
-    for (int w = 0; w < 8; ++w) t += red[w];
-    const double m = t / kN;
-    if (threadIdx.x == 0) mline[as] = static_cast<float>(m);
+        for (int w = 0; w < 8; ++w) t += red[w];
+        __syncthreads();
+        const double m = t / kN;
+        if (threadIdx.x == 0) mline[as] = static_cast<float>(m);
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
-        const int j = threadIdx.x + 256 * k;
-        const double v = d[k] - m;
-        const __half h = __double2half(v);
-        hi[as * kN + j] = h;
-        lo[as * kN + j] = __double2half(v - static_cast<double>(__half2float(h)));
+        for (int k = 0; k < 8; ++k) {
+            const int j = threadIdx.x + 256 * k;
+            store_split(static_cast<float>(d[k] - m), hi + as * kN + j, lo + as * kN + j);
+        }
     }
 }
 
 }  // namespace
 
-cudaError_t launch_prec_split(const SpectralArgs& a, int dtype, double* apod64, __half* hi, __half* lo,
-                              float* mline, cudaStream_t st) {
+cudaError_t launch_prec_split(const SpectralArgs& a, int dtype, void* apod_scratch, __half* hi, __half* lo,
+                              float* mline, int num_sms, cudaStream_t st) {
     const int64_t n = a.n_ascans;
     if (n == 0) return cudaSuccess;
     const dim3 ga(kN / 256, a.B);
-    const unsigned int g = static_cast<unsigned int>(n);
+    const int64_t g64 = n < static_cast<int64_t>(num_sms) * 8 ? n : static_cast<int64_t>(num_sms) * 8;
+    const unsigned int g = static_cast<unsigned int>(g64);
+    int* isum = static_cast<int*>(apod_scratch);
     if (dtype == 0) {
-        k_apod_mean64<uint16_t><<<ga, 256, 0, st>>>(a, apod64);
-        k_prec_split<uint16_t><<<g, 256, 0, st>>>(a, apod64, hi, lo, mline);
+        k_apod_sum<uint16_t><<<ga, 256, 0, st>>>(a, isum);
+        k_prec_split_int<uint16_t><<<g, 256, 0, st>>>(a, isum, hi, lo, mline);
     } else if (dtype == 1) {
-        k_apod_mean64<int16_t><<<ga, 256, 0, st>>>(a, apod64);
-        k_prec_split<int16_t><<<g, 256, 0, st>>>(a, apod64, hi, lo, mline);
+        k_apod_sum<int16_t><<<ga, 256, 0, st>>>(a, isum);
+        k_prec_split_int<int16_t><<<g, 256, 0, st>>>(a, isum, hi, lo, mline);
     } else {
-        k_apod_mean64<float><<<ga, 256, 0, st>>>(a, apod64);
-        k_prec_split<float><<<g, 256, 0, st>>>(a, apod64, hi, lo, mline);
+        double* a64 = static_cast<double*>(apod_scratch);
+        k_apod_mean64<<<ga, 256, 0, st>>>(a, a64);
+        k_prec_split_f32<<<g, 256, 0, st>>>(a, a64, hi, lo, mline);
     }
     return cudaGetLastError();
 }
