@@ -154,6 +154,24 @@ int octgb_stitch_plan(octgb_ctx *ctx, int n_rows, int r0, int r1, int c0, int c1
                       const double *Wz, const double *WxT, const double *fz, const int64_t *shift,
                       const double *pdz, int n_y, int *plan_id);
 
+/* ---------------------------------------------------------------- rare raw formats */
+
+/* prepare_raw (octrecon/core/spectral.py:48-68): raw (B, n_lines, n) ->
+ * float32 (B, *out_lines, n): apod_mode 0 keeps the first apod_size lines as
+ * the apodisation, apod_mode 1 (Wasatch, no apodisation lines) prepends the
+ * frame mean (mean over a file's lines, then over the apod_group files of its
+ * frame, :59-63); the scan lines are AScanBinning-averaged (filter2 'same',
+ * zero padded, decimated from max(1, binning/2) - 1, :20-45) when binning > 1.
+ * Same float32 operation order as the reference, so equal to its arrays. */
+int octgb_prepare_raw(octgb_ctx *ctx, const void *raw, int raw_dtype, int raw_loc, int B, int n_lines,
+                      int apod_size, int binning, int apod_mode, int apod_group, float *out, int out_loc,
+                      int *out_lines);
+/* average_repeats (core/spectral.py:168-177): mag (n_frames * bscan_avg,
+ * size_x * ascan_avg, nz) -> (n_frames, size_x, nz), mean over B-scan repeats
+ * then A-scan repeats, float32 as the reference. */
+int octgb_average_repeats(octgb_ctx *ctx, const float *mag, int mag_loc, int n_frames, int bscan_avg, int size_x,
+                          int ascan_avg, int nz, float *out, int out_loc);
+
 /* Start a y-tile row (Reconstructor.process_row, octrecon/pipeline.py:230-232):
  * zero the device accumulators num/den of shape (n_frames, n_out_z, n_out_x). */
 int octgb_row_begin(octgb_ctx *ctx, int n_frames, int n_out_z, int n_out_x);
@@ -165,6 +183,16 @@ int octgb_row_begin(octgb_ctx *ctx, int n_frames, int n_out_z, int n_out_x);
  * optical-path shift row). */
 int octgb_row_add_batch(octgb_ctx *ctx, int plan_id, const void *raw, int raw_dtype, int raw_loc, int B,
                         int interf, int apod_size, const int64_t *frame_idx, int frame_offset);
+
+/* octgb_row_add_batch for the rare formats (pipeline.py:274-285 with
+ * hdr.spectra_avg, apod_mode, bscan_avg, ascan_avg): n_files = n_frames x
+ * bscan_avg raw files (B-scan repeats consecutive, Reconstructor.frame_files,
+ * pipeline.py:217-220) are prepared (octgb_prepare_raw with apod_group =
+ * bscan_avg), reconstructed, averaged over repeats (octgb_average_repeats) and
+ * stitched for frames frame_idx[0 .. n_frames-1]. */
+int octgb_row_add_batch_ex(octgb_ctx *ctx, int plan_id, const void *raw, int raw_dtype, int raw_loc, int n_files,
+                           int n_lines, int apod_size, int binning, int apod_mode, int bscan_avg, int ascan_avg,
+                           const int64_t *frame_idx, int n_frames, int frame_offset);
 
 /* Finalise the row (pipeline.py:296-300): den < threshold -> NaN, db =
  * 20*log10(num/den) as float32 (n_frames, n_out_z, n_out_x) into db (host or

@@ -57,6 +57,12 @@ SIGNATURES = {
                                 c_void_p, c_int]),
     "octgb_xmedian": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_int, c_void_p]),
     "octgb_xmean": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_void_p]),
+    "octgb_prepare_raw": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_int, c_int, c_int, c_int,
+                                  c_void_p, c_int, c_void_p]),
+    "octgb_average_repeats": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_int, c_int, c_void_p,
+                                      c_int]),
+    "octgb_row_add_batch_ex": (c_int, [c_void_p, c_int, c_void_p, c_int, c_int, c_int, c_int, c_int, c_int, c_int,
+                                       c_int, c_int, c_void_p, c_int, c_int]),
     "octgb_linearise_precision": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_int, c_void_p, c_int]),
     "octgb_magnitude_precision": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_int, c_void_p, c_int]),
     "octgb_cnn_images": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_int]),
@@ -226,6 +232,35 @@ class Context:
         self._check(self.lib.octgb_magnitude(self.h, p, dt, loc, B, interf, apod_size, op, oloc))
         return out
 
+    def prepare_raw(self, raw, apod_size: int, binning: int = 1, apod_mode: int = 0, apod_group: int = 1,
+                    out=None, raw_dtype=None):
+        """prepare_raw on the device: (B, lines, N) -> float32 (B, a + kept, N)
+        (numpy result for numpy input unless `out` is given)."""
+        raw, p, loc, dt, B, n_lines = self._raw_args(raw, apod_size, raw_dtype)
+        n_out = ctypes.c_int(0)
+        if out is None:
+            # shape first (no work when B = 0), then the call
+            self._check(self.lib.octgb_prepare_raw(self.h, p, dt, loc, 0, n_lines, apod_size, binning, apod_mode,
+                                                   apod_group, ctypes.c_void_p(16), HOST, ctypes.byref(n_out)))
+            out = np.empty((B, n_out.value, self.n), np.float32)
+        op, oloc = _ptr(out)
+        self._check(self.lib.octgb_prepare_raw(self.h, p, dt, loc, B, n_lines, apod_size, binning, apod_mode,
+                                               apod_group, op, oloc, ctypes.byref(n_out)))
+        return out
+
+    def average_repeats(self, mag, n_frames: int, bscan_avg: int, ascan_avg: int, out=None):
+        F, L, nz = mag.shape
+        size_x = L // ascan_avg
+        if out is None:
+            out = np.empty((n_frames, size_x, nz), np.float32)
+        if isinstance(mag, np.ndarray):
+            mag = np.ascontiguousarray(mag, dtype=np.float32)
+        p, loc = _ptr(mag)
+        op, oloc = _ptr(out)
+        self._check(self.lib.octgb_average_repeats(self.h, p, loc, n_frames, bscan_avg, size_x, ascan_avg, nz, op,
+                                                   oloc))
+        return out
+
     def linearise_precision(self, raw, apod_size: int, out=None, raw_dtype=None):
         """Precision form, stage (c): the linearised interferogram (B, nX, N)
         float32 from the tensor-core sinc (no window)."""
@@ -347,6 +382,15 @@ class Context:
             raise ValueError("frame_idx must have one entry per B-scan")
         self._check(self.lib.octgb_row_add_batch(self.h, int(plan_id), p, dt, loc, B, interf, int(apod_size),
                                                  fi.ctypes.data, int(frame_offset)))
+
+    def row_add_batch_ex(self, plan_id: int, raw, apod_size: int, frame_idx, frame_offset: int, binning: int = 1,
+                         apod_mode: int = 0, bscan_avg: int = 1, ascan_avg: int = 1, raw_dtype=None):
+        """One batch of a rare-format scan: len(frame_idx) frames x bscan_avg raw files."""
+        raw, p, loc, dt, n_files, n_lines = self._raw_args(raw, apod_size if apod_mode == 0 else 1, raw_dtype)
+        fi = np.ascontiguousarray(np.asarray(frame_idx).reshape(-1), dtype=np.int64)
+        self._check(self.lib.octgb_row_add_batch_ex(self.h, int(plan_id), p, dt, loc, n_files, n_lines,
+                                                    int(apod_size), int(binning), int(apod_mode), int(bscan_avg),
+                                                    int(ascan_avg), fi.ctypes.data, len(fi), int(frame_offset)))
 
     def row_finalise(self, threshold: float, shape, out=None, plane_minmax: bool = False):
         if out is None:

@@ -154,6 +154,8 @@ struct octgb_ctx {
     int64_t capture_launch0 = 0;
     DevBuf magbuf, dbbuf, planemm, segs, qtable;
     DevBuf qcounter;                         // batched form: queue head
+    // rare raw formats: prepared batch, frame-mean lines, per-file magnitudes
+    DevBuf prep, prep_apod, magrep;
     // precision form (tensor-core sinc)
     bool prec_ok = false;
     DevBuf prec_w, prec_kb, prec_hi, prec_lo, prec_m, prec_x;
@@ -467,7 +469,8 @@ int octgb_destroy(octgb_ctx* c) {
     for (DevBuf* b : {&c->w, &c->start, &c->win, &c->tw, &c->wsh, &c->s0, &c->raw, &c->apod, &c->out, &c->mm, &c->frames, &c->num,
                       &c->den, &c->plan_table, &c->run_mm, &c->magbuf, &c->dbbuf, &c->planemm, &c->segs, &c->qtable,
                       &c->qcounter, &c->disp_x, &c->disp_hann, &c->disp_phase, &c->disp_a, &c->disp_score, &c->xmed,
-                      &c->prec_w, &c->prec_kb, &c->prec_hi, &c->prec_lo, &c->prec_m, &c->prec_x})
+                      &c->prec_w, &c->prec_kb, &c->prec_hi, &c->prec_lo, &c->prec_m, &c->prec_x, &c->prep,
+                      &c->prep_apod, &c->magrep})
         b->release();
     for (QTable* t : c->qtables) {
         t->buf.release();
@@ -906,6 +909,66 @@ int octgb_row_begin(octgb_ctx* c, int n_frames, int n_out_z, int n_out_x) {
     });
 }
 
+}  // extern "C"
+
+namespace {
+// TileStitcher.contribute of B frames of magnitudes (device, (B, n_tile_x,
+// N/2)) into the row accumulators (pipeline.py:283-285)
+void stitch_row(octgb_ctx* c, const Plan& p, const float* mag, const std::vector<int>& fy, bool contiguous, int B,
+                int frame_offset) {
+    const int* fdev = nullptr;
+    if (!contiguous) {
+        // pageable copy: returns once staged, so `fy` may go out of scope
+        ck(c->frames.ensure(fy.size() * sizeof(int)), "cudaMalloc(frames)");
+        ck(cudaMemcpyAsync(c->frames.p, fy.data(), fy.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream),
+           "H2D frames");
+        fdev = c->frames.as<int>();
+    }
+    ck(launch_stitch(p.dev(), mag, fdev, fy[0], B, c->num.as<float>(), c->den.as<float>(), frame_offset, c->row_nx,
+                     p.xs_max, p.rs_max, c->stream),
+       "stitch kernel");
+    c->launches++;
+}
+
+// PrepArgs of a raw batch (prepare_raw, core/spectral.py:48-68); false when
+// the batch needs no preparation (apodisation lines, no binning)
+bool prep_args(PrepArgs& a, const void* raw, int B, int n_lines, int apod, int binning, int mode, int group) {
+    require(binning >= 1 && binning <= 64, "AScanBinning must be in [1, 64]");
+    require(mode == 0 || mode == 1, "apod_mode must be 0 (lines) or 1 (frame mean)");
+    require(group >= 1 && B % group == 0, "the batch is not a whole number of frames (apod_group)");
+    if (mode == 0) require(apod >= 1 && apod < n_lines, "apod_size must be in [1, lines)");
+    a.raw = raw;
+    a.B = B;
+    a.n_lines = n_lines;
+    a.mode = mode;
+    a.group = group;
+    a.binning = binning;
+    a.a_out = mode == 0 ? apod : 1;
+    a.scan0 = mode == 0 ? apod : 0;
+    a.n_scan = n_lines - a.scan0;
+    a.s0 = std::max(1, binning / 2) - 1;
+    a.left = (binning + 1) / 2 - 1;
+    a.n_kept = binning == 1 ? a.n_scan : (a.n_scan - a.s0 + binning - 1) / binning;
+    require(a.n_kept >= 1, "no A-lines left after AScanBinning");
+    return binning > 1 || mode == 1;
+}
+
+// prepared batch on the device (c->prep, float32 (B, a_out + n_kept, N))
+void run_prepare(octgb_ctx* c, const PrepArgs& a0, int dtype, int loc) {
+    PrepArgs a = a0;
+    const size_t bytes = static_cast<size_t>(a.B) * a.n_lines * kN * raw_elem(dtype);
+    a.raw = stage_raw(c, a.raw, dtype, loc, bytes);
+    ck(c->prep.ensure(static_cast<size_t>(a.B) * (a.a_out + a.n_kept) * kN * sizeof(float) + 16),
+       "cudaMalloc(prepared)");
+    if (a.mode == 1)
+        ck(c->prep_apod.ensure(static_cast<size_t>(a.B / a.group) * kN * sizeof(float)), "cudaMalloc(frame mean)");
+    ck(launch_prepare(a, dtype, c->prep_apod.as<float>(), c->prep.as<float>(), c->stream), "prepare kernel");
+    c->launches += a.mode == 1 ? 2 : 1;
+}
+}  // namespace
+
+extern "C" {
+
 int octgb_row_add_batch(octgb_ctx* c, int plan_id, const void* raw, int dtype, int loc, int B, int interf, int apod,
                         const int64_t* frame_idx, int frame_offset) {
     return guarded(c, [&] {
@@ -927,19 +990,8 @@ int octgb_row_add_batch(octgb_ctx* c, int plan_id, const void* raw, int dtype, i
         if (B == 0) return;
         const size_t mb = static_cast<size_t>(B) * p.n_tile_x * kHalf * sizeof(float);
         ck(c->magbuf.ensure(mb), "cudaMalloc(mag)");
-        const int* fdev = nullptr;
-        if (!contiguous) {
-            // pageable copy: returns once staged, so `fy` may go out of scope
-            ck(c->frames.ensure(fy.size() * sizeof(int)), "cudaMalloc(frames)");
-            ck(cudaMemcpyAsync(c->frames.p, fy.data(), fy.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream),
-               "H2D frames");
-            fdev = c->frames.as<int>();
-        }
         run_spectral(c, raw, dtype, loc, B, interf, apod, kModeMag, c->magbuf.as<float>(), 0, 0, nullptr);
-        ck(launch_stitch(p.dev(), c->magbuf.as<float>(), fdev, fy[0], B, c->num.as<float>(), c->den.as<float>(),
-                         frame_offset, c->row_nx, p.xs_max, p.rs_max, c->stream),
-           "stitch kernel");
-        c->launches++;
+        stitch_row(c, p, c->magbuf.as<float>(), fy, contiguous, B, frame_offset);
     });
 }
 
@@ -1134,7 +1186,8 @@ int octgb_graph_end(octgb_ctx* c, int* graph_id) {
         for (DevBuf* b : {&c->raw, &c->apod, &c->out, &c->mm, &c->frames, &c->num, &c->den, &c->plan_table,
                           &c->run_mm, &c->magbuf, &c->dbbuf, &c->planemm, &c->segs, &c->qtable, &c->qcounter,
                           &c->disp_x, &c->disp_hann, &c->disp_phase, &c->disp_a, &c->disp_score, &c->xmed,
-                          &c->prec_hi, &c->prec_lo, &c->prec_m, &c->prec_x})
+                          &c->prec_hi, &c->prec_lo, &c->prec_m, &c->prec_x, &c->prep, &c->prep_apod,
+                          &c->magrep})
             b->keep_old = true;
         for (int k = 0; k < octgb_ctx::kRing; ++k) c->ring[k].keep_old = true;
         c->launches.store(c->capture_launch0);
@@ -1375,6 +1428,106 @@ int octgb_xmedian(octgb_ctx* c, const float* mag, int mag_loc, int n_frames, int
 
 int octgb_xmean(octgb_ctx* c, const float* mag, int mag_loc, int n_frames, int nx, int nz, double* out) {
     return guarded(c, [&] { xprofile(c, mag, mag_loc, n_frames, nx, nz, 1, 1, out); });
+}
+
+// ---------------------------------------------------------------------------
+// Rare raw formats (core/spectral.py:20-82,168-177; pipeline.py:274-285).
+
+int octgb_prepare_raw(octgb_ctx* c, const void* raw, int dtype, int loc, int B, int n_lines, int apod, int binning,
+                      int apod_mode, int apod_group, float* out, int out_loc, int* out_lines) {
+    return guarded(c, [&] {
+        validate_raw(raw, dtype, loc, B, n_lines, apod_mode == 1 ? 1 : apod);
+        require(out != nullptr && out_lines != nullptr, "NULL output");
+        PrepArgs a{};
+        prep_args(a, raw, B, n_lines, apod, binning, apod_mode, apod_group);
+        *out_lines = a.a_out + a.n_kept;
+        if (B == 0) return;
+        run_prepare(c, a, dtype, loc);
+        copy_out(c, out, out_loc, c->prep.p, static_cast<size_t>(B) * (a.a_out + a.n_kept) * kN * sizeof(float));
+        check_status(c);
+    });
+}
+
+int octgb_average_repeats(octgb_ctx* c, const float* mag, int mag_loc, int n_frames, int bscan_avg, int size_x,
+                          int ascan_avg, int nz, float* out, int out_loc) {
+    return guarded(c, [&] {
+        require(mag && out, "NULL buffer");
+        require(n_frames >= 0 && bscan_avg >= 1 && ascan_avg >= 1 && size_x >= 1 && nz >= 1, "bad repeat shape");
+        if (n_frames == 0) return;
+        const size_t in_n = static_cast<size_t>(n_frames) * bscan_avg * size_x * ascan_avg * nz;
+        const size_t out_n = static_cast<size_t>(n_frames) * size_x * nz;
+        const float* src = mag;
+        if (mag_loc != OCTGB_DEVICE) {
+            ck(c->magrep.ensure(in_n * sizeof(float)), "cudaMalloc(mag)");
+            ck(cudaMemcpyAsync(c->magrep.p, mag, in_n * sizeof(float), cudaMemcpyHostToDevice, c->stream), "H2D mag");
+            src = c->magrep.as<float>();
+        }
+        float* dst = out;
+        if (out_loc != OCTGB_DEVICE) {
+            ck(c->magbuf.ensure(out_n * sizeof(float)), "cudaMalloc(out)");
+            dst = c->magbuf.as<float>();
+        }
+        ck(launch_avg_repeats(src, n_frames, bscan_avg, size_x, ascan_avg, nz, dst, c->stream), "repeat kernel");
+        c->launches++;
+        if (out_loc != OCTGB_DEVICE) copy_out(c, out, OCTGB_HOST, dst, out_n * sizeof(float));
+        check_status(c);
+    });
+}
+
+int octgb_row_add_batch_ex(octgb_ctx* c, int plan_id, const void* raw, int dtype, int loc, int n_files, int n_lines,
+                           int apod, int binning, int apod_mode, int bscan_avg, int ascan_avg, const int64_t* frame_idx,
+                           int n_frames, int frame_offset) {
+    return guarded(c, [&] {
+        if (!c->row_open) throw Error(OCTGB_ERR_STATE, "octgb_row_begin has not been called");
+        if (!c->has_geom) throw Error(OCTGB_ERR_STATE, "octgb_set_geometry has not been called");
+        if (c->cancel.load()) throw Error(OCTGB_ERR_CANCELLED, "cancelled");
+        require(plan_id >= 0 && plan_id < static_cast<int>(c->plans.size()), "bad plan id");
+        const Plan& p = *c->plans[plan_id];
+        validate_raw(raw, dtype, loc, n_files, n_lines, apod_mode == 1 ? 1 : apod);
+        require(bscan_avg >= 1 && ascan_avg >= 1, "repeat counts must be >= 1");
+        require(n_files == n_frames * bscan_avg, "n_files must be n_frames x bscan_avg (repeats consecutive)");
+        require(frame_offset >= 0 && frame_offset + n_frames <= c->row_nf, "frames outside the row");
+        require(frame_idx != nullptr, "frame_idx is NULL");
+        PrepArgs a{};
+        const bool prep = prep_args(a, raw, n_files, n_lines, apod, binning, apod_mode, bscan_avg);
+        require(a.n_kept % ascan_avg == 0, "A-lines are not a whole number of A-scan repeats");
+        const int size_x = a.n_kept / ascan_avg;
+        require(size_x == p.n_tile_x, "A-scans per B-scan differ from the plan's tile width");
+        require(p.n_out_z == c->row_nz && p.c0 + p.C <= c->row_nx, "plan does not fit the row");
+        std::vector<int> fy(n_frames > 0 ? n_frames : 1);
+        bool contiguous = true;
+        for (int f = 0; f < n_frames; ++f) {
+            require(!p.opc || (frame_idx[f] >= 0 && frame_idx[f] < p.n_y), "frame index outside the scan");
+            fy[f] = static_cast<int>(frame_idx[f]);
+            contiguous = contiguous && frame_idx[f] == frame_idx[0] + f;
+        }
+        if (n_frames == 0) return;
+        // spectral input: the prepared float32 batch, or the raw batch itself
+        const void* src = raw;
+        int sdt = dtype, sloc = loc, s_lines = n_lines, s_apod = apod;
+        if (prep) {
+            run_prepare(c, a, dtype, loc);
+            src = c->prep.p;
+            sdt = OCTGB_F32;
+            sloc = OCTGB_DEVICE;
+            s_lines = a.a_out + a.n_kept;
+            s_apod = a.a_out;
+        }
+        const bool rep = bscan_avg > 1 || ascan_avg > 1;
+        ck(c->magbuf.ensure(static_cast<size_t>(n_frames) * size_x * kHalf * sizeof(float)), "cudaMalloc(mag)");
+        float* m = c->magbuf.as<float>();
+        if (rep) {
+            ck(c->magrep.ensure(static_cast<size_t>(n_files) * a.n_kept * kHalf * sizeof(float)), "cudaMalloc(mag)");
+            m = c->magrep.as<float>();
+        }
+        run_spectral(c, src, sdt, sloc, n_files, s_lines, s_apod, kModeMag, m, 0, 0, nullptr);
+        if (rep) {
+            ck(launch_avg_repeats(m, n_frames, bscan_avg, size_x, ascan_avg, kHalf, c->magbuf.as<float>(), c->stream),
+               "repeat kernel");
+            c->launches++;
+        }
+        stitch_row(c, p, c->magbuf.as<float>(), fy, contiguous, n_frames, frame_offset);
+    });
 }
 
 // ---------------------------------------------------------------------------

@@ -156,6 +156,20 @@ cudaError_t launch_disp_metric(const float* A, int n_seg, int nx, int z_min, int
 cudaError_t launch_xmedian(const float* mag, int n_frames, int nx, int nz, int ignore_nan, int mean_mode,
                            double* out, cudaStream_t st);
 
+// rare raw formats (prepare.cu): AScanBinning, frame-mean apodisation, repeats
+struct PrepArgs {
+    const void* raw;      // (B, n_lines, kN)
+    int B, n_lines;
+    int a_out;            // apodisation lines of the output (apod_size, or 1 for frame mean)
+    int n_kept;           // scan lines of the output
+    int n_scan, scan0;    // scan lines of a file and the first one
+    int s0, left;         // AScanBinning: first kept column, window lines before the column
+    int binning, mode, group;   // mode 0: apodisation lines, 1: frame mean over `group` files
+};
+cudaError_t launch_prepare(const PrepArgs& p, int dtype, float* frame_apod, float* out, cudaStream_t st);
+cudaError_t launch_avg_repeats(const float* mag, int n_frames, int nb, int size_x, int na, int nz, float* out,
+                               cudaStream_t st);
+
 // precision form (precision.cu): tensor-core sinc
 constexpr int kPM = 128;                 // A-scans per tile (MMA M)
 constexpr int kPN = 64;                  // output samples per block (MMA N)

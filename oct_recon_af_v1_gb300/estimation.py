@@ -82,11 +82,20 @@ class DispersionScorer:
 
     @classmethod
     def from_context(cls, ctx, raw_list, metric: str, device: int = 0):
-        """Build from the reference's VolumeContext (estimation/_common.py:38-118)."""
+        """Build from the reference's VolumeContext (estimation/_common.py:38-118);
+        rare formats are prepared on the device first (SpectralProcessor.prepare,
+        core/spectral.py:112-116)."""
         h = ctx.hdr
-        if max(1, h.spectra_avg) != 1 or h.apod_mode != "lines":
-            raise NotImplementedError("gb300 scorer: AScanBinning / frame-mean apodisation are not supported")
-        return cls(ctx.lambda_nm, raw_list, metric, h.apod_size, device)
+        binning, frame_mean = max(1, int(h.spectra_avg)), h.apod_mode == "frame_mean"
+        if binning == 1 and not frame_mean:
+            return cls(ctx.lambda_nm, raw_list, metric, h.apod_size, device)
+        prep = Context(device)
+        try:
+            raws = [prep.prepare_raw(np.asarray(r), h.apod_size, binning, 1 if frame_mean else 0,
+                                     max(1, int(h.bscan_avg))) for r in raw_list]
+        finally:
+            prep.close()
+        return cls(ctx.lambda_nm, raws, metric, 1 if frame_mean else h.apod_size, device)
 
     def close(self):
         self.ctx.close()

@@ -115,16 +115,26 @@ class _GB300Processor:
     geometry on the GB300 kernels; host arrays in and out, as the estimators'
     CPU path."""
 
-    def __init__(self, sg, apod_size: int, device_index: int):
+    def __init__(self, sg, apod_size: int, device_index: int, binning: int = 1, apod_mode: int = 0,
+                 apod_group: int = 1):
         from ._lib import Context
         self.ctx = Context(device_index)
         self.ctx.set_geometry(sg.sinc_idx, sg.sinc_w, sg.window)
         self.apod_size = int(apod_size)
+        self.binning, self.apod_mode, self.apod_group = int(binning), int(apod_mode), int(apod_group)
         self.n = len(sg.lambda_nm)
         self.nz = self.n // 2
 
+    def prepare(self, raw):
+        """prepare_raw (core/spectral.py:48-68) on the device; raw itself when nothing applies."""
+        if self.binning == 1 and self.apod_mode == 0:
+            return np.asarray(raw)
+        return self.ctx.prepare_raw(np.asarray(raw), self.apod_size, self.binning, self.apod_mode, self.apod_group)
+
     def magnitude(self, raw):
-        return self.ctx.magnitude(np.asarray(raw), self.apod_size)
+        x = self.prepare(raw)
+        a = 1 if self.apod_mode == 1 else self.apod_size
+        return self.ctx.magnitude(x, a)
 
 
 def _register_estimators(get_xp, device_index: int) -> None:
@@ -146,10 +156,6 @@ def _register_estimators(get_xp, device_index: int) -> None:
         orig_ctx_init(self, volume_folder, "cpu" if gb else device, dtype)
         self._gb300 = {} if gb else None
         if gb:
-            h = self.hdr
-            if max(1, h.spectra_avg) != 1 or h.apod_mode != "lines":
-                raise NotImplementedError("gb300: AScanBinning / frame-mean apodisation are not supported by the "
-                                          "GB300 kernels")
             self.device = DEVICE
 
     def processor(self, dispersion, n_medium=None):
@@ -159,8 +165,10 @@ def _register_estimators(get_xp, device_index: int) -> None:
         key = (float(dispersion), self.si.tissue_ri if n_medium is None else float(n_medium))
         sp = cache.get(key)
         if sp is None:
-            sp = cache[key] = _GB300Processor(self.geometry(dispersion, n_medium), self.hdr.apod_size,
-                                              device_index)
+            h = self.hdr
+            sp = cache[key] = _GB300Processor(self.geometry(dispersion, n_medium), h.apod_size, device_index,
+                                              max(1, h.spectra_avg), 1 if h.apod_mode == "frame_mean" else 0,
+                                              max(1, h.bscan_avg))
         return sp
 
     VC.__init__ = ctx_init
@@ -181,13 +189,14 @@ class _RowEngine:
     def __init__(self, R, device_index: int):
         from ._lib import Context
         hdr = R.hdr
-        if max(1, hdr.bscan_avg) != 1 or max(1, hdr.ascan_avg) != 1:
-            raise NotImplementedError("gb300: B-/A-scan repeat averaging is not supported by the GB300 kernels")
-        if hdr.spectra_avg > 1 or hdr.apod_mode != "lines":
-            raise NotImplementedError("gb300: AScanBinning / frame-mean apodisation are not supported by the GB300 "
-                                      "kernels")
         self.ctx = Context(device_index)
         self.ctx.set_geometry(R.sg.sinc_idx, R.sg.sinc_w, R.sg.window)
+        # rare formats (core/spectral.py:20-82,168-177): prepared and averaged on the device
+        self.binning = max(1, int(hdr.spectra_avg))
+        self.apod_mode = 1 if hdr.apod_mode == "frame_mean" else 0
+        self.bscan_avg = max(1, int(hdr.bscan_avg))
+        self.ascan_avg = max(1, int(hdr.ascan_avg))
+        self.rare = self.binning > 1 or self.apod_mode == 1 or self.bscan_avg > 1 or self.ascan_avg > 1
         self.plans = {}
         for key, st in R.stitchers.items():
             if st.empty:
@@ -257,7 +266,11 @@ def _process_row(self, yi: int, frames=None, pool=None, on_batch=None):
                 pending.append((nxt, pool.submit(read_job, nxt)))
             t, s, fr = job
             # spectral stage + stitching + accumulation of this batch on the device
-            ctx.row_add_batch(eng.plans[(t.xi, t.zi)], raw, hdr.apod_size, fr, s)
+            if eng.rare:
+                ctx.row_add_batch_ex(eng.plans[(t.xi, t.zi)], raw, hdr.apod_size, fr, s, eng.binning, eng.apod_mode,
+                                     eng.bscan_avg, eng.ascan_avg)
+            else:
+                ctx.row_add_batch(eng.plans[(t.xi, t.zi)], raw, hdr.apod_size, fr, s)
             t2 = time.perf_counter()
             self.timers["spectral"] += t2 - t1
             n_done += 1

@@ -435,3 +435,56 @@ class DispScorer:
 
     def scores(self, beta, idx=None):
         return disp_metric(self.magnitude(beta, idx), self.metric)
+
+
+# ----------------------------------------------------------------------------- rare raw formats
+def bin_ascans(x, binning):
+    """core/spectral.py:27-45 AScanBinning: filter2 'same' (zero padded) average
+    of `binning` consecutive A-lines, decimated from max(1, B//2) - 1; the
+    window of kept column c is lines c - ceil(B/2) + 1 .. c + floor(B/2); sum
+    acc = x0*h, acc = acc + xt*h in the array's dtype, h = 1/B."""
+    x = np.asarray(x)
+    n = x.shape[-2]
+    s0 = max(1, binning // 2) - 1
+    cols = np.arange(s0, n, binning)
+    left = (binning + 1) // 2 - 1
+    h = x.dtype.type(1.0 / binning)
+    out = None
+    for t in range(binning):
+        lines = cols + t - left
+        ok = (lines >= 0) & (lines < n)
+        sl = np.zeros(x.shape[:-2] + (len(cols), x.shape[-1]), x.dtype)
+        sl[..., ok, :] = x[..., lines[ok], :]
+        term = sl * h
+        out = term if out is None else out + term
+    return out
+
+
+def prepare_raw(raw, apod_size, binning=1, apod_mode="lines", apod_group=1, dtype=np.float32):
+    """core/spectral.py:48-68: float array whose first lines are the
+    apodisation (apod_size lines, or the frame mean for apod_mode 'frame_mean':
+    mean over a file's lines, then over its frame's apod_group files), then the
+    (binned) scan lines; `raw` itself when nothing applies."""
+    if apod_mode == "frame_mean":
+        x = np.asarray(raw).astype(dtype)
+        B, nL, N = x.shape
+        g = max(1, int(apod_group))
+        apod = x.reshape(B // g, g, nL, N).mean(axis=2).mean(axis=1)
+        apod = np.repeat(apod, g, axis=0)[:, None, :]
+        if binning > 1:
+            x = bin_ascans(x, binning)
+        return np.concatenate([apod, x], axis=1)
+    if binning > 1:
+        x = np.asarray(raw).astype(dtype)
+        return np.concatenate([x[:, :apod_size, :], bin_ascans(x[:, apod_size:, :], binning)], axis=1)
+    return raw
+
+
+def average_repeats(mag, n_frames, bscan_avg, size_x, ascan_avg):
+    """core/spectral.py:168-177: mean over B-scan repeats, then A-scan repeats."""
+    nb, na = max(1, bscan_avg), max(1, ascan_avg)
+    if nb == 1 and na == 1:
+        return mag
+    m5 = np.asarray(mag).reshape(n_frames, nb, size_x, na, mag.shape[-1])
+    m4 = m5.mean(1) if nb > 1 else m5[:, 0]
+    return m4.mean(2) if na > 1 else m4[:, :, 0]
