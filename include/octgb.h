@@ -135,6 +135,21 @@ int octgb_magnitude_precision(octgb_ctx *ctx, const void *raw, int raw_dtype, in
  * or here).  Evaluated in float64 as write_legacy_tiff does (:62). */
 int octgb_quantise(octgb_ctx *ctx, const float *db, int64_t n, int db_loc, double c1, double c2,
                    uint16_t *bits, int bits_loc);
+/* Legacy double quantisation (write_legacy_tiff with
+ * legacy_double_quantization, tiff_writer.py:62-64): bits =
+ * db_to_bits(bits_to_db(db_to_bits(db, pc), pc), clim), pc = [p1, p2] the
+ * plane's clim, clim = [c1, c2] the volume's; float64 like the reference
+ * (the second pass is an exact 65 536-entry table of the first code).  A
+ * plane whose clim is not finite takes the single quantisation. */
+int octgb_quantise_double(octgb_ctx *ctx, const float *db, int64_t n, int db_loc, double p1, double p2, double c1,
+                          double c2, uint16_t *bits, int bits_loc);
+/* PackBits (TIFF compression 32773) of a (rows, cols) uint16 image, every row
+ * packed on its own from its little-endian bytes: out (host, `capacity`
+ * bytes) receives the rows' packets back to back, row_sizes (host, rows
+ * ints) each row's byte count, *total their sum.  A row never exceeds
+ * 2 cols + ceil(2 cols / 128) bytes.  Synchronises. */
+int octgb_packbits(octgb_ctx *ctx, const uint16_t *img, int img_loc, int rows, int cols, uint8_t *out,
+                   int64_t capacity, int *row_sizes, int64_t *total);
 /* [min, max] of the finite values of db (plane_clim, tiff_writer.py:48-50);
  * NaN pair when none is finite. */
 int octgb_minmax(octgb_ctx *ctx, const float *db, int64_t n, int db_loc, double *minmax);

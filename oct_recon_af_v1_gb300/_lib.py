@@ -57,6 +57,9 @@ SIGNATURES = {
                                 c_void_p, c_int]),
     "octgb_xmedian": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_int, c_void_p]),
     "octgb_xmean": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_void_p]),
+    "octgb_quantise_double": (c_int, [c_void_p, c_void_p, c_int64, c_int, c_double, c_double, c_double, c_double,
+                                      c_void_p, c_int]),
+    "octgb_packbits": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_void_p, c_int64, c_void_p, c_void_p]),
     "octgb_prepare_raw": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_int, c_int, c_int, c_int,
                                   c_void_p, c_int, c_void_p]),
     "octgb_average_repeats": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_int, c_int, c_void_p,
@@ -350,6 +353,32 @@ class Context:
         c1, c2 = sorted(float(c) for c in clim)
         self._check(self.lib.octgb_quantise(self.h, p, n, loc, c1, c2, op, oloc))
         return out
+
+    def quantise_double(self, db, plane_clim, clim, out=None):
+        """Legacy double quantisation (tiff_writer.py:62-64) of one plane."""
+        p, loc = _ptr(db)
+        n = int(np.prod(db.shape))
+        if out is None:
+            out = np.empty(db.shape, np.uint16)
+        op, oloc = _ptr(out)
+        p1, p2 = (float(v) for v in plane_clim)
+        c1, c2 = sorted(float(v) for v in clim)
+        self._check(self.lib.octgb_quantise_double(self.h, p, n, loc, p1, p2, c1, c2, op, oloc))
+        return out
+
+    def packbits(self, img):
+        """PackBits of every row of a (rows, cols) uint16 image -> (bytes, row sizes)."""
+        rows, cols = img.shape
+        if isinstance(img, np.ndarray):
+            img = np.ascontiguousarray(img, dtype=np.uint16)
+        p, loc = _ptr(img)
+        cap = rows * (2 * cols + (2 * cols + 127) // 128 + 1)
+        out = np.empty(max(cap, 1), np.uint8)
+        sizes = np.empty(max(rows, 1), np.int32)
+        total = ctypes.c_int64(0)
+        self._check(self.lib.octgb_packbits(self.h, p, loc, rows, cols, out.ctypes.data, cap, sizes.ctypes.data,
+                                            ctypes.byref(total)))
+        return out[:total.value].tobytes(), sizes[:rows]
 
     def minmax(self, db):
         p, loc = _ptr(db)

@@ -154,6 +154,8 @@ struct octgb_ctx {
     int64_t capture_launch0 = 0;
     DevBuf magbuf, dbbuf, planemm, segs, qtable;
     DevBuf qcounter;                         // batched form: queue head
+    // legacy TIFF encoding
+    DevBuf enc_bits, enc_lut, enc_slots, enc_sizes;
     // rare raw formats: prepared batch, frame-mean lines, per-file magnitudes
     DevBuf prep, prep_apod, magrep;
     // precision form (tensor-core sinc)
@@ -470,7 +472,7 @@ int octgb_destroy(octgb_ctx* c) {
                       &c->den, &c->plan_table, &c->run_mm, &c->magbuf, &c->dbbuf, &c->planemm, &c->segs, &c->qtable,
                       &c->qcounter, &c->disp_x, &c->disp_hann, &c->disp_phase, &c->disp_a, &c->disp_score, &c->xmed,
                       &c->prec_w, &c->prec_kb, &c->prec_hi, &c->prec_lo, &c->prec_m, &c->prec_x, &c->prep,
-                      &c->prep_apod, &c->magrep})
+                      &c->prep_apod, &c->magrep, &c->enc_bits, &c->enc_lut, &c->enc_slots, &c->enc_sizes})
         b->release();
     for (QTable* t : c->qtables) {
         t->buf.release();
@@ -1187,7 +1189,7 @@ int octgb_graph_end(octgb_ctx* c, int* graph_id) {
                           &c->run_mm, &c->magbuf, &c->dbbuf, &c->planemm, &c->segs, &c->qtable, &c->qcounter,
                           &c->disp_x, &c->disp_hann, &c->disp_phase, &c->disp_a, &c->disp_score, &c->xmed,
                           &c->prec_hi, &c->prec_lo, &c->prec_m, &c->prec_x, &c->prep, &c->prep_apod,
-                          &c->magrep})
+                          &c->magrep, &c->enc_bits, &c->enc_lut, &c->enc_slots, &c->enc_sizes})
             b->keep_old = true;
         for (int k = 0; k < octgb_ctx::kRing; ++k) c->ring[k].keep_old = true;
         c->launches.store(c->capture_launch0);
@@ -1428,6 +1430,84 @@ int octgb_xmedian(octgb_ctx* c, const float* mag, int mag_loc, int n_frames, int
 
 int octgb_xmean(octgb_ctx* c, const float* mag, int mag_loc, int n_frames, int nx, int nz, double* out) {
     return guarded(c, [&] { xprofile(c, mag, mag_loc, n_frames, nx, nz, 1, 1, out); });
+}
+
+// ---------------------------------------------------------------------------
+// Legacy TIFF encoding (io/tiff_writer.py:53-71).
+
+int octgb_quantise_double(octgb_ctx* c, const float* db, int64_t n, int db_loc, double p1, double p2, double c1,
+                          double c2, uint16_t* bits, int bits_loc) {
+    return guarded(c, [&] {
+        require(db != nullptr && bits != nullptr && n >= 0, "bad quantisation arguments");
+        if (p1 > p2) std::swap(p1, p2);
+        if (c1 > c2) std::swap(c1, c2);
+        require(c2 > c1, "clim must have c1 < c2");
+        if (n == 0) return;
+        const float* src = db;
+        if (db_loc != OCTGB_DEVICE) {
+            ck(c->dbbuf.ensure(n * sizeof(float)), "cudaMalloc(db)");
+            ck(cudaMemcpyAsync(c->dbbuf.p, db, n * sizeof(float), cudaMemcpyHostToDevice, c->stream), "H2D db");
+            src = c->dbbuf.as<float>();
+        }
+        uint16_t* dst = bits;
+        if (bits_loc != OCTGB_DEVICE) {
+            ck(c->enc_bits.ensure(n * sizeof(uint16_t)), "cudaMalloc(bits)");
+            dst = c->enc_bits.as<uint16_t>();
+        }
+        ck(c->qtable.ensure(kQuantTable * sizeof(float)), "cudaMalloc(table)");
+        // a plane without finite values has NaN plane clim: all its codes are 0
+        // either way, so it takes the single quantisation
+        const bool twice = std::isfinite(p1) && std::isfinite(p2) && p2 > p1;
+        ck(launch_quantise(src, n, twice ? p1 : c1, twice ? p2 : c2, c->qtable.as<float>(), dst, c->stream),
+           "quantise kernels");
+        c->launches += 2;
+        if (twice) {
+            ck(c->enc_lut.ensure(65536 * sizeof(uint16_t)), "cudaMalloc(lut)");
+            ck(launch_requant(dst, n, p1, p2, c1, c2, c->enc_lut.as<uint16_t>(), c->stream), "re-quantise kernels");
+            c->launches += 2;
+        }
+        if (bits_loc != OCTGB_DEVICE) copy_out(c, bits, OCTGB_HOST, dst, n * sizeof(uint16_t));
+        check_status(c);
+    });
+}
+
+int octgb_packbits(octgb_ctx* c, const uint16_t* img, int img_loc, int rows, int cols, uint8_t* out,
+                   int64_t capacity, int* row_sizes, int64_t* total) {
+    return guarded(c, [&] {
+        require(img && out && row_sizes && total, "NULL buffer");
+        require(rows >= 0 && cols >= 1, "bad image shape");
+        *total = 0;
+        if (rows == 0) return;
+        const size_t n = static_cast<size_t>(rows) * cols;
+        const uint16_t* src = img;
+        if (img_loc != OCTGB_DEVICE) {
+            ck(c->enc_bits.ensure(n * sizeof(uint16_t)), "cudaMalloc(image)");
+            ck(cudaMemcpyAsync(c->enc_bits.p, img, n * sizeof(uint16_t), cudaMemcpyHostToDevice, c->stream),
+               "H2D image");
+            src = c->enc_bits.as<uint16_t>();
+        }
+        const int slot = packbits_slot(cols);
+        ck(c->enc_slots.ensure(static_cast<size_t>(rows) * slot), "cudaMalloc(slots)");
+        ck(c->enc_sizes.ensure(static_cast<size_t>(rows) * sizeof(int)), "cudaMalloc(sizes)");
+        ck(launch_packbits(src, rows, cols, c->enc_slots.as<uint8_t>(), c->enc_sizes.as<int>(), c->stream),
+           "packbits kernel");
+        c->launches++;
+        std::vector<uint8_t> h(static_cast<size_t>(rows) * slot);
+        ck(cudaMemcpyAsync(row_sizes, c->enc_sizes.p, static_cast<size_t>(rows) * sizeof(int), cudaMemcpyDeviceToHost,
+                           c->stream),
+           "D2H sizes");
+        ck(cudaMemcpyAsync(h.data(), c->enc_slots.p, h.size(), cudaMemcpyDeviceToHost, c->stream), "D2H slots");
+        check_status(c);
+        int64_t off = 0;
+        for (int r = 0; r < rows; ++r) off += row_sizes[r];
+        require(off <= capacity, "output capacity too small for the packed image");
+        off = 0;
+        for (int r = 0; r < rows; ++r) {
+            memcpy(out + off, h.data() + static_cast<size_t>(r) * slot, row_sizes[r]);
+            off += row_sizes[r];
+        }
+        *total = off;
+    });
 }
 
 // ---------------------------------------------------------------------------

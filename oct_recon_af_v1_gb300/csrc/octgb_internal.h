@@ -170,6 +170,12 @@ cudaError_t launch_prepare(const PrepArgs& p, int dtype, float* frame_apod, floa
 cudaError_t launch_avg_repeats(const float* mag, int n_frames, int nb, int size_x, int na, int nz, float* out,
                                cudaStream_t st);
 
+// legacy TIFF encoding (encode.cu)
+cudaError_t launch_requant(uint16_t* bits, int64_t n, double p1, double p2, double c1, double c2, uint16_t* lut,
+                           cudaStream_t st);
+int packbits_slot(int cols);
+cudaError_t launch_packbits(const uint16_t* img, int rows, int cols, uint8_t* out, int* sizes, cudaStream_t st);
+
 // precision form (precision.cu): tensor-core sinc
 constexpr int kPM = 128;                 // A-scans per tile (MMA M)
 constexpr int kPN = 64;                  // output samples per block (MMA N)

@@ -24,6 +24,9 @@ files, so `Reconstructor`, the CLI (`--set device=gb300`) and the web app
 * Estimators asked for device gb300 (estimate_dispersion, detect_focus,
   octrecon/estimation) keep their host logic; their spectral processors and
   the DispersionScorer run on the GB300 kernels (`_register_estimators`).
+* The legacy TIFF writer (io/tiff_writer.py:53-71, called by
+  Reconstructor.run) is replaced by `tiff.write_legacy_tiff`: same file
+  layout, codes and PackBits packets computed on the GPU.
 * The web app's GPU card only lights up when CuPy imports
   (webapp/server.py:74-85); `register()` patches its `system_info` to report
   the gb300 device.
@@ -89,6 +92,23 @@ def register(device_index: int = 0) -> None:
             _attach(self, device_index)
 
     pipeline.Reconstructor.__init__ = init
+
+    try:
+        # the legacy TIFF (tiff_writer.py:53-71) written from the GPU codes and
+        # PackBits packets; needs neither tifffile nor imagecodecs
+        import octrecon.io.tiff_writer as tiff_writer
+
+        from .tiff import write_legacy_tiff as gb300_write
+
+        def write_legacy_tiff(path, db_volume, clim, metadata, legacy_double_quantization=False, plane_clims=None,
+                              progress=None):
+            return gb300_write(path, db_volume, clim, metadata, legacy_double_quantization, plane_clims, progress,
+                               device=device_index)
+
+        write_legacy_tiff.__doc__ = tiff_writer.write_legacy_tiff.__doc__
+        tiff_writer.write_legacy_tiff = write_legacy_tiff
+    except ImportError:
+        pass
 
     try:
         import octrecon.webapp.server as server

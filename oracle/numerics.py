@@ -488,3 +488,33 @@ def average_repeats(mag, n_frames, bscan_avg, size_x, ascan_avg):
     m5 = np.asarray(mag).reshape(n_frames, nb, size_x, na, mag.shape[-1])
     m4 = m5.mean(1) if nb > 1 else m5[:, 0]
     return m4.mean(2) if na > 1 else m4[:, :, 0]
+
+
+# ----------------------------------------------------------------------------- legacy TIFF encoding
+def legacy_double_bits(plane, plane_clim_, clim):
+    """io/tiff_writer.py:62-64: the legacy double quantisation of one plane."""
+    p = np.asarray(plane, np.float64)
+    return db_to_bits(bits_to_db(db_to_bits(p, plane_clim_), plane_clim_), clim)
+
+
+def packbits_encode_row(row_bytes: bytes) -> bytes:
+    """PackBits of one row (TIFF compression 32773, rows packed separately):
+    runs of >= 3 equal bytes (up to 128) as repeat packets, the rest as
+    literal packets of up to 128 bytes."""
+    b, n, i, out = row_bytes, len(row_bytes), 0, bytearray()
+    while i < n:
+        run = 1
+        while i + run < n and run < 128 and b[i + run] == b[i]:
+            run += 1
+        if run >= 3:
+            out += bytes([(257 - run) & 0xff, b[i]])
+            i += run
+            continue
+        j = i
+        while j < n and j - i < 128:
+            if j + 2 < n and b[j] == b[j + 1] == b[j + 2]:
+                break
+            j += 1
+        out += bytes([j - i - 1]) + b[i:j]
+        i = j
+    return bytes(out)
