@@ -184,6 +184,15 @@ class Context:
     def set_stream(self, stream_handle: int | None):
         self._check(self.lib.octgb_set_stream(self.h, c_void_p(stream_handle or None)))
 
+    def follow_torch_stream(self):
+        """Launch on torch's current CUDA stream; torch's default stream (handle
+        0) maps to the legacy default stream (cudaStreamLegacy), so the
+        context's work is ordered with torch's and with every other context
+        that follows the same stream."""
+        import torch
+        h = torch.cuda.current_stream().cuda_stream
+        self.set_stream(h if h else 1)                       # 1 == cudaStreamLegacy
+
     def synchronize(self):
         self._check(self.lib.octgb_synchronize(self.h))
 

@@ -14,7 +14,7 @@ image are standardised together.  The magnitude of one reconstruction does
 not reveal the sign of the residual dispersion; the +-p probes do.
 
 Network (NCHW float32): 4 x [conv 3x3 (pad 1) -> ReLU -> 2x2 mean pool]
-with 16, 32, 32, 32 channels, then dense 8192 -> 64 -> ReLU -> 2.  Outputs:
+of 32 channels each, then dense 8192 -> 64 -> ReLU -> 2.  Outputs:
 beta / BETA_SCALE and (focus - 500) / 400.  Every layer, its gradients, the
 loss and Adam run in hand-written kernels (csrc/cnn.cu) through the C ABI;
 torch only allocates the tensors.
@@ -73,8 +73,7 @@ class ImageMaker:
     def load(self, raw, raw_dtype=None):
         """Linearise and window raw B-scans once: device tensor (B, interf, N)
         (int16 holding uint16 bits with raw_dtype U16, or int16/float32)."""
-        torch = self.torch
-        self.ctx.set_stream(torch.cuda.current_stream().cuda_stream)
+        self.ctx.follow_torch_stream()
         self.B, interf, _ = raw.shape
         self.nx = interf - self.apod
         self.device = raw.device
@@ -85,6 +84,7 @@ class ImageMaker:
         b renders the probes at beta - b, i.e. the B-scans as if their spectra
         carried a compensating dispersion b (the scorer's phase trick)."""
         torch = self.torch
+        self.ctx.follow_torch_stream()
         P = len(self.probes)
         mag = torch.empty((P, self.B, self.nx, self.n // 2), dtype=torch.float32, device=self.device)
         self.ctx.disp_eval(self.probes - float(beta_shift), 0, self.B, 0, mag=mag)
@@ -102,7 +102,7 @@ class BetaFocusNet:
     """The CNN (see the module docstring); parameters and Adam state are torch
     CUDA tensors, every computation a C-ABI call on the context's stream."""
 
-    def __init__(self, ctx: Context, in_ch: int = 3, widths=(16, 32, 32, 32), img: int = IMG, hidden: int = 64,
+    def __init__(self, ctx: Context, in_ch: int = 3, widths=(32, 32, 32, 32), img: int = IMG, hidden: int = 64,
                  seed: int = 0, device="cuda"):
         import torch
         self.torch = torch
@@ -156,7 +156,10 @@ class BetaFocusNet:
 
     def forward(self, x):
         """x: (n, in_ch, img, img) float32 CUDA tensor -> (n, 2) predictions (a
-        view of an internal buffer, valid until the next call)."""
+        view of an internal buffer, valid until the next call).  Runs on
+        torch's current stream (see Context.follow_torch_stream), after the
+        work that produced x."""
+        self.ctx.follow_torch_stream()
         n = x.shape[0]
         b = self._buffers(n)
         self._x = x
