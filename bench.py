@@ -12,13 +12,22 @@ legacy uint16 quantisation of the volume.
 
 `--config 0`: one tile, 50 B-scans x (25 + 500) A-scans, z-crop 1000 px:
 spectral stage to dB, global clim, quantisation.
+`--config 2`: the config-1 tiles through the precision form of the spectral
+stage (exact background, tcgen05 split-FP16 sinc), beside the float32 form.
+`--config 3`: 64 tiles of uneven size in one persistent launch (device work
+queue, CUDA graph, autotuned grab / order), beside per-tile launches.
+`--config 4`: the learned beta/focus estimator trained on the device (20 k
+probe images), timed on 500 held-out B-scans against the GPU plain search.
 
 `value` is measured with inputs resident in HBM (inputs are larger than L2, so
 no flush is needed); `e2e` repeats the step through the same API with the raw
 spectra in pinned host memory (H2D inside the timed region) and reads the
-uint16 volume back (D2H).  `--impl reference` times the reference algorithm's
-CPU restatement (the oracle: Numba kernel restated in C/OpenMP + pocketfft +
-NumPy stitching) on the host cores over bounded samples.
+uint16 volume back (D2H).  Volumes are processed back to back: a volume's
+codes need its global clim, so their read-back overlaps the next volume's
+upload and reconstruction (second stream, double-buffered codes); the timed
+region ends after the last read-back.  `--impl reference` times the reference
+algorithm's CPU restatement (the oracle: Numba kernel restated in C/OpenMP +
+pocketfft + NumPy stitching) on the host cores over bounded samples.
 
 Run:  python bench.py [--gpus N --steps K --warmup W] [--impl reference]
 """
@@ -249,26 +258,48 @@ def gpu_arm(args, rank, world):
         run_step(ctx, vol, vol.raw, db_vol, bits, args.batch)
         graph = ctx.graph_end()
 
-    def step(src, e2e=False, host_bits=None):
+    # end to end, volumes back to back: the codes of a volume need its global
+    # clim, so their read-back cannot overlap the volume's own reconstruction;
+    # it runs on a second stream (the other link direction) while the next
+    # volume's raws stream in and reconstruct, from a double-buffered code volume
+    e2e_bits = [bits, torch.empty_like(bits)] if not args.no_e2e else [bits]
+    d2h = torch.cuda.Stream()
+    d2h_done = [torch.cuda.Event(), torch.cuda.Event()]
+    for ev in d2h_done:
+        ev.record(d2h)
+
+    def step(src, e2e=False, host_bits=None, k=0):
         if graph is not None and not e2e:
             ctx.graph_launch(graph)
-        else:
+            return
+        if not e2e:
             run_step(ctx, vol, src, db_vol, bits, args.batch)
-        if e2e:
-            host_bits.copy_(bits, non_blocking=True)
+            return
+        b = k % 2
+        stream.wait_event(d2h_done[b])                  # the copy of two volumes ago has left this buffer
+        run_step(ctx, vol, src, db_vol, e2e_bits[b], args.batch)
+        end = torch.cuda.Event()
+        end.record(stream)
+        d2h.wait_event(end)
+        with torch.cuda.stream(d2h):
+            host_bits[b].copy_(e2e_bits[b], non_blocking=True)
+        d2h_done[b].record(d2h)
 
     def timed(src, steps, warm, e2e=False):
-        host_bits = torch.empty(n_out, dtype=torch.int16, pin_memory=True) if e2e else None
-        for _ in range(warm):
-            step(src, e2e, host_bits)
+        host_bits = [torch.empty(n_out, dtype=torch.int16, pin_memory=True) for _ in range(2)] if e2e else None
+        for k in range(warm):
+            step(src, e2e, host_bits, k)
         torch.cuda.synchronize()
         if world > 1:
             torch.distributed.barrier()
         n0 = ctx.launches
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        for _ in range(steps):
-            step(src, e2e, host_bits)
+        for k in range(steps):
+            step(src, e2e, host_bits, k)
+        if e2e:                                          # every read-back is inside the timed region
+            stream.wait_event(d2h_done[0])
+            stream.wait_event(d2h_done[1])
         e1.record(stream)
         torch.cuda.synchronize()
         if world > 1:
@@ -281,7 +312,7 @@ def gpu_arm(args, rank, world):
     clk = clocks.stop()
     e2e_ms = None
     if not args.no_e2e:
-        e2e_ms, _ = timed(vol.host, max(1, args.steps // 2), 1, e2e=True)
+        e2e_ms, _ = timed(vol.host, max(2, args.steps), 1, e2e=True)
     # roofline of the dominant kernel, measured live on a 30-B-scan slab of one tile
     kms, kbytes, kascans = time_spectral_kernel(ctx, torch, vol.raw[(0, 0, 0)][:30], stream)
     ms_all = reduce_max(ms, world)
