@@ -1635,14 +1635,26 @@ float* precision_linearise(octgb_ctx* c, const void* raw, int dtype, int loc, in
     a.apod = apod;
     a.nx = nx;
     a.n_ascans = n;
-    ck(c->prec_hi.ensure(static_cast<size_t>(n) * kN * sizeof(__half)), "cudaMalloc(d hi)");
-    ck(c->prec_lo.ensure(static_cast<size_t>(n) * kN * sizeof(__half)), "cudaMalloc(d lo)");
-    ck(c->prec_m.ensure(static_cast<size_t>(n) * sizeof(float)), "cudaMalloc(line means)");
     float* X = x_dev;
     if (X == nullptr) {
         ck(c->prec_x.ensure(static_cast<size_t>(n) * kN * sizeof(float)), "cudaMalloc(X)");
         X = c->prec_x.as<float>();
     }
+    ck(c->prec_m.ensure(static_cast<size_t>(n) * sizeof(float)), "cudaMalloc(line means)");
+    if (dtype != OCTGB_F32) {
+        // integer raws: the sinc kernel reads the raw window itself (no d' in memory)
+        ck(c->prec_hi.ensure(static_cast<size_t>(n) * sizeof(long long)), "cudaMalloc(line sums)");
+        CUtensorMap mr;
+        if (!encode_raw_map(&mr, rd, B, interf, apod)) throw Error(OCTGB_ERR_CUDA, "cuTensorMapEncodeTiled failed");
+        ck(launch_prec_sinc_raw(a, dtype, mr, c->prec_w.as<uint8_t>(), c->prec_kb.as<int>(), c->apod.as<int>(),
+                                c->prec_hi.as<long long>(), c->prec_m.as<float>(), X, c->status_dev, c->num_sms,
+                                c->stream),
+           "tensor-core sinc kernels");
+        c->launches += 3;
+        return X;
+    }
+    ck(c->prec_hi.ensure(static_cast<size_t>(n) * kN * sizeof(__half)), "cudaMalloc(d hi)");
+    ck(c->prec_lo.ensure(static_cast<size_t>(n) * kN * sizeof(__half)), "cudaMalloc(d lo)");
     ck(launch_prec_split(a, dtype, c->apod.p, c->prec_hi.as<__half>(), c->prec_lo.as<__half>(),
                          c->prec_m.as<float>(), c->num_sms, c->stream),
        "background / split kernels");

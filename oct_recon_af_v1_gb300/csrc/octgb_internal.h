@@ -194,6 +194,12 @@ cudaError_t launch_prec_sinc(const CUtensorMap& tm_hi, const CUtensorMap& tm_lo,
                              const int* kb, const float* mline, float* X, int64_t n_ascans, int* status, int num_sms,
                              cudaStream_t st);
 bool encode_prec_map(CUtensorMap* map, const void* base, int64_t n_ascans);
+// integer raws, fused: apodisation sums, line sums, then the tensor-core sinc
+// reading the raw window directly (apod_sum: B x kN ints; sum_n, mline: per A-scan)
+cudaError_t launch_prec_sinc_raw(const SpectralArgs& a, int dtype, const CUtensorMap& tm_raw, const uint8_t* wtiles,
+                                 const int* kb, int* apod_sum, long long* sum_n, float* mline, float* X, int* status,
+                                 int num_sms, cudaStream_t st);
+bool encode_raw_map(CUtensorMap* map, const void* raw, int B, int interf, int apod);
 // W tiles (per output block: hi then lo, canonical K-major no-swizzle, W x 64)
 // and window starts kb; false when a block's band exceeds the window
 bool build_prec_tiles(const int* start, const int* len, const float* wt, std::vector<uint16_t>& tiles,

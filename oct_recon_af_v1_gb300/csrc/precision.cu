@@ -259,6 +259,255 @@ __global__ void __launch_bounds__(kPThreads, 1)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;" ::"r"(tmem) : "memory");
 }
 
+// ---------------------------------------------------------------------------
+// Fused variant for integer raws (k_prec_sinc_raw): the raw uint16/int16
+// window of each block arrives by three-dimensional tensor copies (samples x
+// A-scans x B-scans, tiles of 128 A-scans inside one B-scan, rows past the
+// B-scan zero-filled) and twelve converter warps form d' in shared memory
+// from it: n = apod * raw - S is an exact integer below 2^24, so
+// d' = fma(n, 1/apod, -m) takes one float32 rounding relative to
+// max(|d|, |m|) (m from k_prec_rowsum); they write the fp16 hi/lo operand
+// tiles in the canonical layout, so d' never reaches global memory.  Roles:
+// warps 0-3 epilogue, 4-15 converters, warp 16 lane 0 copies, warp 17 lane 0
+// MMAs.
+constexpr int kRConvWarps = 12;
+constexpr int kRThreads = (4 + kRConvWarps + 2) * 32;
+constexpr uint32_t kRawTileBytes = kPChunks * kAChunkBytes;            // 12 chunks of 8 samples x 128 rows, 2 B
+constexpr uint32_t kRStageBytes = kRawTileBytes + 2 * kATileBytes + 2 * kBTileBytes;
+constexpr uint32_t kRLoadBytes = kRawTileBytes + 2 * kBTileBytes;       // bytes the copies deliver per block
+
+struct RawSmem {
+    alignas(1024) uint8_t stage[kPStages][kRStageBytes];   // raw | A_hi | A_lo | B_hi | B_lo
+    uint64_t full[kPStages], conv[kPStages], empty[kPStages], tfull[2], tempty[2], drain;
+    uint32_t tmem_base;
+    int abort;
+};
+
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ bool wait_or_abort_r(uint64_t* bar, uint32_t parity, RawSmem& S, int* status) {
+    if (*reinterpret_cast<volatile int*>(&S.abort)) return false;
+    if (mbar_wait_bounded(bar, parity, status)) return true;
+    atomicExch(&S.abort, 1);
+    return false;
+}
+
+template <typename RawT>
+__global__ void __launch_bounds__(kRThreads, 1)
+    k_prec_sinc_raw(const __grid_constant__ CUtensorMap tm_raw, const uint8_t* __restrict__ wtiles,
+                    const int* __restrict__ kb, const int* __restrict__ apod_sum,
+                    const long long* __restrict__ sum_n, const float* __restrict__ mline, float* __restrict__ X,
+                    int B, int nx, int apod, int* status) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    RawSmem& S = *reinterpret_cast<RawSmem*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int xtiles = (nx + kPM - 1) / kPM;
+    const int64_t n_tiles = static_cast<int64_t>(B) * xtiles;
+    const int64_t my_tiles = blockIdx.x < n_tiles ? (n_tiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+    const int64_t n_q = my_tiles * kPBlocks;
+    const float inv_apod = 1.0f / static_cast<float>(apod);
+
+    if (tid == 0) {
+        for (int s = 0; s < kPStages; ++s) {
+            mbar_init(&S.full[s], 1);
+            mbar_init(&S.conv[s], kRConvWarps);
+            mbar_init(&S.empty[s], 1);
+        }
+        for (int d = 0; d < 2; ++d) {
+            mbar_init(&S.tfull[d], 1);
+            mbar_init(&S.tempty[d], 4);
+        }
+        mbar_init(&S.drain, 1);
+        S.abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;" ::"r"(smem_u32(&S.tmem_base))
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = S.tmem_base;
+
+    if (warp == 4 + kRConvWarps && lane == 0) {
+        // ---------------- copies
+        int64_t q = 0;
+        for (; q < n_q; ++q) {
+            const int s = static_cast<int>(q % kPStages);
+            const uint32_t ph = static_cast<uint32_t>(q / kPStages) & 1u;
+            if (!wait_or_abort_r(&S.empty[s], ph ^ 1u, S, status)) break;
+            const int64_t tile = blockIdx.x + (q / kPBlocks) * gridDim.x;
+            const int b = static_cast<int>(q % kPBlocks);
+            const int bs = static_cast<int>(tile / xtiles), xt = static_cast<int>(tile % xtiles);
+            uint8_t* st = S.stage[s];
+            mbar_expect_tx(&S.full[s], kRLoadBytes);
+            for (int c = 0; c < kPChunks; ++c)
+                tma_load_3d(st + c * kAChunkBytes, &tm_raw, kb[b] + 8 * c, xt * kPM, bs, &S.full[s]);
+            const uint8_t* wsrc = wtiles + static_cast<size_t>(b) * 2 * kBTileBytes;
+            uint8_t* bdst = st + kRawTileBytes + 2 * kATileBytes;
+            tma_bulk_g2s(bdst, wsrc, kBTileBytes, &S.full[s]);
+            tma_bulk_g2s(bdst + kBTileBytes, wsrc + kBTileBytes, kBTileBytes, &S.full[s]);
+        }
+        for (int64_t r = q - kPStages; r < q; ++r) {
+            if (r < 0) continue;
+            mbar_wait_bounded(&S.full[r % kPStages], static_cast<uint32_t>(r / kPStages) & 1u, status);
+        }
+    } else if (warp >= 4 && warp < 4 + kRConvWarps) {
+        // ---------------- converters: raw window -> d' hi/lo operand tiles
+        const int ct = tid - 128;
+        for (int64_t q = 0; q < n_q; ++q) {
+            const int s = static_cast<int>(q % kPStages);
+            const uint32_t ph = static_cast<uint32_t>(q / kPStages) & 1u;
+            bool ok = true;
+            if (lane == 0) ok = wait_or_abort_r(&S.full[s], ph, S, status);
+            ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+            if (!ok) break;
+            const int64_t tile = blockIdx.x + (q / kPBlocks) * gridDim.x;
+            const int b = static_cast<int>(q % kPBlocks);
+            const int bs = static_cast<int>(tile / xtiles), xt = static_cast<int>(tile % xtiles);
+            const int j0 = kb[b];
+            uint8_t* st = S.stage[s];
+            const int* Sb = apod_sum + static_cast<int64_t>(bs) * kN;
+            for (int i = ct; i < kPChunks * kPM; i += kRConvWarps * 32) {
+                const int row = i % kPM, c = i / kPM;
+                const int x = xt * kPM + row;
+                const float m = x < nx ? mline[static_cast<int64_t>(bs) * nx + x] : 0.f;
+                const uint4 rv = *reinterpret_cast<const uint4*>(st + c * kAChunkBytes + row * 16);
+                const uint32_t words[4] = {rv.x, rv.y, rv.z, rv.w};
+                uint32_t hw[4], lw[4];
+#pragma unroll
+                for (int e2 = 0; e2 < 4; ++e2) {
+                    uint32_t h2 = 0, l2 = 0;
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const int j = j0 + 8 * c + 2 * e2 + h;
+                        const uint32_t u = (words[e2] >> (16 * h)) & 0xffffu;
+                        const int rawv = sizeof(RawT) == 2 && static_cast<RawT>(-1) < 0
+                                             ? static_cast<int>(static_cast<int16_t>(u))
+                                             : static_cast<int>(u);
+                        // n = apod (raw - apod mean), an exact integer below 2^24: exact in
+                        // float32, so d' = n / apod - m takes one rounding (fma)
+                        const int n = j < kN ? apod * rawv - Sb[j] : 0;
+                        const float v = fmaf(static_cast<float>(n), inv_apod, -m);
+                        const __half hv = __float2half_rn(v);
+                        const __half lv = __float2half_rn(v - __half2float(hv));
+                        h2 |= static_cast<uint32_t>(__half_as_ushort(hv)) << (16 * h);
+                        l2 |= static_cast<uint32_t>(__half_as_ushort(lv)) << (16 * h);
+                    }
+                    hw[e2] = h2;
+                    lw[e2] = l2;
+                }
+                *reinterpret_cast<uint4*>(st + kRawTileBytes + c * kAChunkBytes + row * 16) =
+                    make_uint4(hw[0], hw[1], hw[2], hw[3]);
+                *reinterpret_cast<uint4*>(st + kRawTileBytes + kATileBytes + c * kAChunkBytes + row * 16) =
+                    make_uint4(lw[0], lw[1], lw[2], lw[3]);
+            }
+            // generic-proxy writes become visible to the tensor cores' (async) reads
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&S.conv[s]);
+        }
+    } else if (warp == 5 + kRConvWarps && lane == 0) {
+        // ---------------- MMA issuer
+        for (int64_t q = 0; q < n_q; ++q) {
+            const int s = static_cast<int>(q % kPStages);
+            const uint32_t ph = static_cast<uint32_t>(q / kPStages) & 1u;
+            const int d = static_cast<int>(q & 1);
+            const uint32_t dph = static_cast<uint32_t>(q >> 1) & 1u;
+            if (!wait_or_abort_r(&S.conv[s], ph, S, status)) break;
+            if (!wait_or_abort_r(&S.tempty[d], dph ^ 1u, S, status)) break;
+            tc_fence_after();
+            const uint32_t dt = tmem + static_cast<uint32_t>(d * kPN);
+            const uint8_t* A = S.stage[s] + kRawTileBytes;
+            const uint8_t* Bw = A + 2 * kATileBytes;
+#pragma unroll
+            for (int k = 0; k < kPKW / 16; ++k) {
+                const uint64_t ah = smem_desc(A + k * 2 * kAChunkBytes, kAChunkBytes, 128);
+                const uint64_t al = smem_desc(A + kATileBytes + k * 2 * kAChunkBytes, kAChunkBytes, 128);
+                const uint64_t bh = smem_desc(Bw + k * 2 * kBChunkBytes, kBChunkBytes, 128);
+                const uint64_t bl = smem_desc(Bw + kBTileBytes + k * 2 * kBChunkBytes, kBChunkBytes, 128);
+                mma_f16(dt, ah, bh, k > 0 ? 1u : 0u);
+                mma_f16(dt, ah, bl, 1u);
+                mma_f16(dt, al, bh, 1u);
+            }
+            mma_commit(&S.empty[s]);
+            mma_commit(&S.tfull[d]);
+        }
+        mma_commit(&S.drain);
+        mbar_wait_bounded(&S.drain, 0, status);
+    } else if (warp < 4) {
+        // ---------------- epilogue
+        const uint32_t lane_base = static_cast<uint32_t>(32 * warp) << 16;
+        for (int64_t q = 0; q < n_q; ++q) {
+            const int d = static_cast<int>(q & 1);
+            const uint32_t dph = static_cast<uint32_t>(q >> 1) & 1u;
+            bool ok = true;
+            if (lane == 0) ok = wait_or_abort_r(&S.tfull[d], dph, S, status);
+            ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+            if (!ok) break;
+            tc_fence_after();
+            float v[2][32];
+            tmem_ld32(tmem + lane_base + static_cast<uint32_t>(d * kPN), v[0]);
+            tmem_ld32(tmem + lane_base + static_cast<uint32_t>(d * kPN + 32), v[1]);
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&S.tempty[d]);
+            const int64_t tile = blockIdx.x + (q / kPBlocks) * gridDim.x;
+            const int b = static_cast<int>(q % kPBlocks);
+            const int bs = static_cast<int>(tile / xtiles), xt = static_cast<int>(tile % xtiles);
+            const int x = xt * kPM + 32 * warp + lane;
+            if (x < nx) {
+                const int64_t a = static_cast<int64_t>(bs) * nx + x;
+                const float m = mline[a];
+                float4* out = reinterpret_cast<float4*>(X + a * kN + b * kPN);
+#pragma unroll
+                for (int h = 0; h < 2; ++h)
+#pragma unroll
+                    for (int c = 0; c < 8; ++c)
+                        out[h * 8 + c] = make_float4(fmaf(v[h][4 * c], 1.0f / 64, m), fmaf(v[h][4 * c + 1], 1.0f / 64, m),
+                                                     fmaf(v[h][4 * c + 2], 1.0f / 64, m),
+                                                     fmaf(v[h][4 * c + 3], 1.0f / 64, m));
+            }
+        }
+    }
+    __syncwarp();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;" ::"r"(tmem) : "memory");
+}
+
+// Line sums of the integer numerators: sum_n[a] = sum_j (apod raw_j - S_j),
+// mline[a] = sum_n / (2048 apod) (the line mean of d).  One warp per A-scan.
+template <typename RawT>
+__global__ void __launch_bounds__(256) k_prec_rowsum(const SpectralArgs a, const int* __restrict__ apod_sum,
+                                                     long long* __restrict__ sum_n, float* __restrict__ mline) {
+    const int lane = threadIdx.x & 31;
+    const float den = static_cast<float>(kN) * static_cast<float>(a.apod);
+    for (int64_t as = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5; as < a.n_ascans;
+         as += (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5) {
+        const int64_t b = as / a.nx, x = as - b * a.nx;
+        const RawT* row = static_cast<const RawT*>(a.raw) + (b * a.interf + a.apod + x) * kN;
+        const int* Sb = apod_sum + b * kN;
+        long long s = 0;
+        for (int j = lane; j < kN; j += 32) s += a.apod * static_cast<int>(row[j]) - Sb[j];
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) {
+            sum_n[as] = s;
+            mline[as] = static_cast<float>(s) / den;
+        }
+    }
+}
+
 // Integer raws: exact apodisation sums S[b][j] (int32).
 template <typename RawT>
 __global__ void k_apod_sum(const SpectralArgs a, int* __restrict__ out) {
@@ -400,6 +649,64 @@ cudaError_t launch_prec_sinc(const CUtensorMap& tm_hi, const CUtensorMap& tm_lo,
 }
 
 size_t prec_smem_bytes() { return sizeof(PrecSmem) + 1024; }
+
+cudaError_t launch_prec_sinc_raw(const SpectralArgs& a, int dtype, const CUtensorMap& tm_raw, const uint8_t* wtiles,
+                                 const int* kb, int* apod_sum, long long* sum_n, float* mline, float* X, int* status,
+                                 int num_sms, cudaStream_t st) {
+    if (a.n_ascans == 0) return cudaSuccess;
+    const dim3 ga(kN / 256, a.B);
+    const int64_t warps = a.n_ascans;
+    int64_t g = (warps * 32 + 255) / 256;
+    if (g > static_cast<int64_t>(num_sms) * 16) g = static_cast<int64_t>(num_sms) * 16;
+    const size_t smem = sizeof(RawSmem) + 1024;
+    const int xtiles = (a.nx + kPM - 1) / kPM;
+    const int64_t tiles = static_cast<int64_t>(a.B) * xtiles;
+    const int grid = static_cast<int>(tiles < num_sms ? tiles : num_sms);
+    cudaError_t e;
+    if (dtype == 0) {
+        k_apod_sum<uint16_t><<<ga, 256, 0, st>>>(a, apod_sum);
+        k_prec_rowsum<uint16_t><<<static_cast<unsigned int>(g), 256, 0, st>>>(a, apod_sum, sum_n, mline);
+        e = cudaFuncSetAttribute(k_prec_sinc_raw<uint16_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(smem));
+        if (e != cudaSuccess) return e;
+        k_prec_sinc_raw<uint16_t><<<grid, kRThreads, smem, st>>>(tm_raw, wtiles, kb, apod_sum, sum_n, mline, X,
+                                                                 a.B, a.nx, a.apod, status);
+    } else {
+        k_apod_sum<int16_t><<<ga, 256, 0, st>>>(a, apod_sum);
+        k_prec_rowsum<int16_t><<<static_cast<unsigned int>(g), 256, 0, st>>>(a, apod_sum, sum_n, mline);
+        e = cudaFuncSetAttribute(k_prec_sinc_raw<int16_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 static_cast<int>(smem));
+        if (e != cudaSuccess) return e;
+        k_prec_sinc_raw<int16_t><<<grid, kRThreads, smem, st>>>(tm_raw, wtiles, kb, apod_sum, sum_n, mline, X,
+                                                                a.B, a.nx, a.apod, status);
+    }
+    return cudaGetLastError();
+}
+
+// 3-D map of the scan lines of a raw batch: samples x A-scans x B-scans
+// (uint16/int16 elements, rows of one B-scan consecutive, B-scans `interf`
+// rows apart), boxes of 8 samples x 128 A-scans x 1 B-scan
+bool encode_raw_map(CUtensorMap* map, const void* raw, int B, int interf, int apod) {
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    if (encode == nullptr) {
+        cudaDriverEntryPointQueryResult q;
+        void* fn = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess || fn == nullptr)
+            return false;
+        encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    }
+    const void* base = static_cast<const uint16_t*>(raw) + static_cast<size_t>(apod) * kN;
+    const cuuint64_t dims[3] = {static_cast<cuuint64_t>(kN), static_cast<cuuint64_t>(interf - apod),
+                                static_cast<cuuint64_t>(B)};
+    const cuuint64_t strides[2] = {static_cast<cuuint64_t>(kN) * 2, static_cast<cuuint64_t>(interf) * kN * 2};
+    const cuuint32_t box[3] = {8, static_cast<cuuint32_t>(kPM), 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    return encode(map, CU_TENSOR_MAP_DATA_TYPE_UINT16, 3, const_cast<void*>(base), dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
 
 bool encode_prec_map(CUtensorMap* map, const void* base, int64_t n_ascans) {
     static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;

@@ -78,3 +78,17 @@ def test_stage_e_and_codes(case):
     # FFT's rounding dominates)
     assert np.mean(lsb_p == 0) >= 0.995 and lsb_p.max() <= 12 and lsb_p[hi].max() <= 1
     assert np.mean(lsb_p == 0) > np.mean(lsb_f == 0) and lsb_p.max() <= lsb_f.max()
+
+
+def test_raw_dtypes_agree(case):
+    """uint16 and int16 raws take the fused kernel (the raw window converted in
+    shared memory) and must agree bit for bit; float32 raws take the split +
+    tensor-copy path and agree to rounding."""
+    ctx, raw, sg0 = case["ctx"], case["raw"], case["sg0"]
+    ctx.set_geometry(sg0.sinc_idx, sg0.sinc_w, np.ones(len(sg0.lambda_nm), np.complex128))
+    assert raw.max() < 32768
+    xu = ctx.linearise_precision(raw, 25)
+    xi = ctx.linearise_precision(raw.astype(np.int16), 25)
+    xf = ctx.linearise_precision(raw.astype(np.float32), 25)
+    np.testing.assert_array_equal(xu, xi)
+    assert np.abs(xf - xu).max() <= 1e-6 * np.abs(xu).max()
