@@ -1625,7 +1625,8 @@ float* precision_linearise(octgb_ctx* c, const void* raw, int dtype, int loc, in
     const int64_t n = static_cast<int64_t>(B) * nx;
     const size_t bytes = static_cast<size_t>(B) * interf * kN * raw_elem(dtype);
     const void* rd = stage_raw(c, raw, dtype, loc, bytes);
-    ck(c->apod.ensure(static_cast<size_t>(B) * kN * sizeof(double) + 16), "cudaMalloc(apod)");
+    // (+ one window of padding: the sinc kernel copies whole 96-sample windows of the sums)
+    ck(c->apod.ensure(static_cast<size_t>(B) * kN * sizeof(double) + kPKW * sizeof(int) + 16), "cudaMalloc(apod)");
     SpectralArgs a{};
     a.raw = rd;
     a.seg[0] = rd;

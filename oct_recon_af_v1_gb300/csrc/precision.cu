@@ -274,10 +274,13 @@ constexpr int kRConvWarps = 12;
 constexpr int kRThreads = (4 + kRConvWarps + 2) * 32;
 constexpr uint32_t kRawTileBytes = kPChunks * kAChunkBytes;            // 12 chunks of 8 samples x 128 rows, 2 B
 constexpr uint32_t kRStageBytes = kRawTileBytes + 2 * kATileBytes + 2 * kBTileBytes;
-constexpr uint32_t kRLoadBytes = kRawTileBytes + 2 * kBTileBytes;       // bytes the copies deliver per block
+constexpr uint32_t kRLoadBytes = kRawTileBytes + 2 * kBTileBytes + kPKW * 4;   // bytes the copies deliver per block
+
+constexpr uint32_t kRSBytes = kPKW * 4;                                // apodisation sums of one window
 
 struct RawSmem {
     alignas(1024) uint8_t stage[kPStages][kRStageBytes];   // raw | A_hi | A_lo | B_hi | B_lo
+    alignas(16) int sw[kPStages][kPKW];                     // S[b][kb .. kb + 96) of the block
     uint64_t full[kPStages], conv[kPStages], empty[kPStages], tfull[2], tempty[2], drain;
     uint32_t tmem_base;
     int abort;
@@ -355,6 +358,8 @@ __global__ void __launch_bounds__(kRThreads, 1)
             uint8_t* bdst = st + kRawTileBytes + 2 * kATileBytes;
             tma_bulk_g2s(bdst, wsrc, kBTileBytes, &S.full[s]);
             tma_bulk_g2s(bdst + kBTileBytes, wsrc + kBTileBytes, kBTileBytes, &S.full[s]);
+            // the window's apodisation sums (the buffer is padded past the last B-scan)
+            tma_bulk_g2s(S.sw[s], apod_sum + static_cast<int64_t>(bs) * kN + kb[b], kPKW * 4, &S.full[s]);
         }
         for (int64_t r = q - kPStages; r < q; ++r) {
             if (r < 0) continue;
@@ -375,35 +380,38 @@ __global__ void __launch_bounds__(kRThreads, 1)
             const int bs = static_cast<int>(tile / xtiles), xt = static_cast<int>(tile % xtiles);
             const int j0 = kb[b];
             uint8_t* st = S.stage[s];
-            const int* Sb = apod_sum + static_cast<int64_t>(bs) * kN;
+            const int* sw = S.sw[s];
+            // a thread's items all lie in one row (the stride is a multiple of 128)
+            const int row = ct % kPM;
+            const int x = xt * kPM + row;
+            const float m = x < nx ? mline[static_cast<int64_t>(bs) * nx + x] : 0.f;
             for (int i = ct; i < kPChunks * kPM; i += kRConvWarps * 32) {
-                const int row = i % kPM, c = i / kPM;
-                const int x = xt * kPM + row;
-                const float m = x < nx ? mline[static_cast<int64_t>(bs) * nx + x] : 0.f;
+                const int c = i / kPM;
                 const uint4 rv = *reinterpret_cast<const uint4*>(st + c * kAChunkBytes + row * 16);
+                const int4 sa = *reinterpret_cast<const int4*>(sw + 8 * c);
+                const int4 sb = *reinterpret_cast<const int4*>(sw + 8 * c + 4);
+                const int sv[8] = {sa.x, sa.y, sa.z, sa.w, sb.x, sb.y, sb.z, sb.w};
                 const uint32_t words[4] = {rv.x, rv.y, rv.z, rv.w};
+                const bool in_row = j0 + 8 * c + 8 <= kN;         // samples past N are never used
                 uint32_t hw[4], lw[4];
 #pragma unroll
                 for (int e2 = 0; e2 < 4; ++e2) {
-                    uint32_t h2 = 0, l2 = 0;
+                    float v[2];
 #pragma unroll
                     for (int h = 0; h < 2; ++h) {
-                        const int j = j0 + 8 * c + 2 * e2 + h;
                         const uint32_t u = (words[e2] >> (16 * h)) & 0xffffu;
-                        const int rawv = sizeof(RawT) == 2 && static_cast<RawT>(-1) < 0
-                                             ? static_cast<int>(static_cast<int16_t>(u))
-                                             : static_cast<int>(u);
+                        const int rawv = static_cast<RawT>(-1) < 0 ? static_cast<int>(static_cast<int16_t>(u))
+                                                                   : static_cast<int>(u);
                         // n = apod (raw - apod mean), an exact integer below 2^24: exact in
                         // float32, so d' = n / apod - m takes one rounding (fma)
-                        const int n = j < kN ? apod * rawv - Sb[j] : 0;
-                        const float v = fmaf(static_cast<float>(n), inv_apod, -m);
-                        const __half hv = __float2half_rn(v);
-                        const __half lv = __float2half_rn(v - __half2float(hv));
-                        h2 |= static_cast<uint32_t>(__half_as_ushort(hv)) << (16 * h);
-                        l2 |= static_cast<uint32_t>(__half_as_ushort(lv)) << (16 * h);
+                        const int n = in_row ? apod * rawv - sv[2 * e2 + h] : 0;
+                        v[h] = fmaf(static_cast<float>(n), inv_apod, -m);
                     }
-                    hw[e2] = h2;
-                    lw[e2] = l2;
+                    const __half2 hv = __floats2half2_rn(v[0], v[1]);
+                    const float2 hf = __half22float2(hv);
+                    const __half2 lv = __floats2half2_rn(v[0] - hf.x, v[1] - hf.y);
+                    hw[e2] = *reinterpret_cast<const uint32_t*>(&hv);
+                    lw[e2] = *reinterpret_cast<const uint32_t*>(&lv);
                 }
                 *reinterpret_cast<uint4*>(st + kRawTileBytes + c * kAChunkBytes + row * 16) =
                     make_uint4(hw[0], hw[1], hw[2], hw[3]);
