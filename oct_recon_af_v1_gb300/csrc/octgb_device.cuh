@@ -114,16 +114,29 @@ __device__ __forceinline__ uint64_t globaltimer_ns() {
     return t;
 }
 
+// try_wait suspends the thread in hardware until the phase completes or the
+// hint (ns) runs out, so waiting warps issue (almost) no instructions
+__device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(smem_u32(bar)), "r"(parity), "r"(100000u)
+        : "memory");
+    return done != 0;
+}
+
 // Bounded wait on an mbarrier phase: gives up after ~2 s of wall time and
-// reports it through the status word (the copy it waits for is 4 KiB and
-// normally lands within microseconds).
+// reports it through the status word (the copies and MMAs waited for
+// normally complete within microseconds).
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int* status) {
     if (mbar_test(bar, parity)) return true;
     const uint64_t t0 = globaltimer_ns();
     for (uint32_t it = 0; it < (1u << 30); ++it) {
-        if (mbar_test(bar, parity)) return true;
-        __nanosleep(64);
-        if ((it & 255u) == 255u && globaltimer_ns() - t0 > 2000000000ull) break;
+        if (mbar_try(bar, parity)) return true;
+        if (globaltimer_ns() - t0 > 2000000000ull) break;
     }
     atomicExch(status, kStatusTimeout);
     return false;
