@@ -232,26 +232,29 @@ __global__ void __launch_bounds__(kStThreads) k_stitch_frames(const StitchDev* _
         float* pa = sm + s.off;
         float* pf = pa + s.xs * s.rs;
         const int fy = f0 + f;
-        // 64 consecutive threads read 64 consecutive rows of one A-scan, four A-scans per pass
+        // the patch is copied as is (asynchronous 4-byte copies, every slot's
+        // in flight at once); the focus weight multiplies it when it is read,
+        // the same single product a * F.  64 consecutive threads copy 64
+        // consecutive rows of one A-scan, four A-scans per pass
         for (int rr = tid & 63; rr < s.rs; rr += 64)
-#pragma unroll 4
-        for (int xx = tid >> 6; xx < s.xs; xx += kStThreads / 64) {
-            const int i = xx * s.rs + rr;
-            const int x = s.x_lo + xx;
-            const int r = s.r_lo + rr;
-            const int ra = p.r0 + r;
-            int src = ra;
-            float F = p.fz[r];
-            if (p.shift != nullptr) {
-                const int64_t o = static_cast<int64_t>(fy) * p.n_tile_x + x;
-                if (ra < p.lo[o] || ra > p.hi[o]) F = 0.f;
-                src = ra + p.shift[o];
-                src = src < 0 ? 0 : (src > p.n_rows - 1 ? p.n_rows - 1 : src);
-                pf[i] = F;
+            for (int xx = tid >> 6; xx < s.xs; xx += kStThreads / 64) {
+                const int i = xx * s.rs + rr;
+                const int x = s.x_lo + xx;
+                const int ra = p.r0 + s.r_lo + rr;
+                int src = ra;
+                if (p.shift != nullptr) {
+                    const int64_t o = static_cast<int64_t>(fy) * p.n_tile_x + x;
+                    pf[i] = (ra < p.lo[o] || ra > p.hi[o]) ? 0.f : p.fz[s.r_lo + rr];
+                    src = ra + p.shift[o];
+                    src = src < 0 ? 0 : (src > p.n_rows - 1 ? p.n_rows - 1 : src);
+                }
+                asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(
+                                 static_cast<uint32_t>(__cvta_generic_to_shared(pa + i))),
+                             "l"(mag_f + static_cast<int64_t>(x) * kHalf + src)
+                             : "memory");
             }
-            pa[i] = mag_f[static_cast<int64_t>(x) * kHalf + src] * F;
-        }
     }
+    asm volatile("cp.async.wait_all;" ::: "memory");
     __syncthreads();
 
     // 2. per voxel: tiles in order, depth (Wz) then lateral (WxT) interpolation
@@ -280,9 +283,6 @@ __global__ void __launch_bounds__(kStThreads) k_stitch_frames(const StitchDev* _
             const bool has_r1 = rr + 1 < s.rs;
             const float w0 = wz0_s[k * kFZ + z], w1 = wz1_s[k * kFZ + z];
             const float* a0p = pa + x0 * s.rs + rr;
-            const float a00 = a0p[0], a01 = has_r1 ? a0p[1] : 0.f;
-            const float a10 = has_x1 ? a0p[s.rs] : 0.f;
-            const float a11 = has_x1 && has_r1 ? a0p[s.rs + 1] : 0.f;
             float f00, f01, f10, f11;
             if (opc) {
                 const float* f0p = pf + x0 * s.rs + rr;
@@ -296,6 +296,10 @@ __global__ void __launch_bounds__(kStThreads) k_stitch_frames(const StitchDev* _
                 f10 = has_x1 ? f00 : 0.f;
                 f11 = has_x1 ? f01 : 0.f;
             }
+            // a = magnitude * F (TileStitcher.contribute, stitching.py:136)
+            const float a00 = a0p[0] * f00, a01 = has_r1 ? a0p[1] * f01 : 0.f;
+            const float a10 = has_x1 ? a0p[s.rs] * f10 : 0.f;
+            const float a11 = has_x1 && has_r1 ? a0p[s.rs + 1] * f11 : 0.f;
             const float u0 = fmaf(a01, w1, a00 * w0), u1 = fmaf(a11, w1, a10 * w0);
             const float d0 = fmaf(f01, w1, f00 * w0), d1 = fmaf(f11, w1, f10 * w0);
             an[q] += fmaf(u1, wx1, u0 * wx0);
