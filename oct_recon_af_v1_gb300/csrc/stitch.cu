@@ -68,7 +68,9 @@ __device__ bool block_contrib(const StitchDev& p, const float* __restrict__ mag_
     const int r_lo = zr_b.x, rs = zr_b.y - zr_b.x + 1;
     const int tid = threadIdx.x;
 
-    // 1. gather the patch: rows fastest (contiguous in the magnitude layout)
+    // 1. gather the patch: rows fastest (contiguous in the magnitude layout);
+    //    magnitudes by asynchronous 4-byte copies (all in flight at once), the
+    //    focus weight F beside them (a = magnitude * F is formed on read)
     for (int i = tid; i < xs * rs; i += kStThreads) {
         const int xx = i / rs, rr = i - xx * rs;
         const int x = x_lo + xx;
@@ -82,9 +84,13 @@ __device__ bool block_contrib(const StitchDev& p, const float* __restrict__ mag_
             src = ra + p.shift[o];
             src = src < 0 ? 0 : (src > p.n_rows - 1 ? p.n_rows - 1 : src);
         }
-        s.pa[xx * rs_max + rr] = mag_f[static_cast<int64_t>(x) * kHalf + src] * F;
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(
+                         static_cast<uint32_t>(__cvta_generic_to_shared(s.pa + xx * rs_max + rr))),
+                     "l"(mag_f + static_cast<int64_t>(x) * kHalf + src)
+                     : "memory");
         s.pf[xx * rs_max + rr] = F;
     }
+    asm volatile("cp.async.wait_all;" ::: "memory");
     __syncthreads();
 
     // 2. depth interpolation (Wz) for every A-scan of the patch and row of the block
@@ -97,11 +103,11 @@ __device__ bool block_contrib(const StitchDev& p, const float* __restrict__ mag_
             if (zr >= 0) {
                 const int rr = zr - r_lo;
                 const float w0 = p.wz0[zo], w1 = p.wz1[zo];
-                const float a0 = s.pa[xx * rs_max + rr], f0 = s.pf[xx * rs_max + rr];
+                const float f0 = s.pf[xx * rs_max + rr], a0 = s.pa[xx * rs_max + rr] * f0;
                 float a1 = 0.f, f1 = 0.f;
                 if (rr + 1 < rs) {
-                    a1 = s.pa[xx * rs_max + rr + 1];
                     f1 = s.pf[xx * rs_max + rr + 1];
+                    a1 = s.pa[xx * rs_max + rr + 1] * f1;
                 }
                 un = fmaf(a1, w1, a0 * w0);
                 ud = fmaf(f1, w1, f0 * w0);
