@@ -181,6 +181,16 @@ int octgb_stitch_plan(octgb_ctx *ctx, int n_rows, int r0, int r1, int c0, int c1
 int octgb_prepare_raw(octgb_ctx *ctx, const void *raw, int raw_dtype, int raw_loc, int B, int n_lines,
                       int apod_size, int binning, int apod_mode, int apod_group, float *out, int out_loc,
                       int *out_lines);
+/* Thorlabs SRR raw files on the device (octrecon/io/srr.py:108-125, the
+ * reader's read_file + read_bscans): words (n_files, file_lines, n) uint16 as
+ * stored after each file's header; only the low 12 bits are data (data %
+ * 4096).  Writes out (n_files, (apod_end - apod_start) + (scan_end -
+ * scan_start), n) int16: the apodisation lines [apod_start, apod_end) then the
+ * scan lines [scan_start, scan_end) of each file, decoded — the (B, interf, n)
+ * int16 layout every entry reads with raw_dtype OCTGB_I16.  From host words
+ * only the used lines are copied. */
+int octgb_srr_decode(octgb_ctx *ctx, const uint16_t *words, int words_loc, int n_files, int file_lines, int n,
+                     int apod_start, int apod_end, int scan_start, int scan_end, int16_t *out, int out_loc);
 /* average_repeats (core/spectral.py:168-177): mag (n_frames * bscan_avg,
  * size_x * ascan_avg, nz) -> (n_frames, size_x, nz), mean over B-scan repeats
  * then A-scan repeats, float32 as the reference. */

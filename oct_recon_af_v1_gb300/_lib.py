@@ -62,6 +62,8 @@ SIGNATURES = {
     "octgb_packbits": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_void_p, c_int64, c_void_p, c_void_p]),
     "octgb_prepare_raw": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_int, c_int, c_int, c_int,
                                   c_void_p, c_int, c_void_p]),
+    "octgb_srr_decode": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_int, c_int, c_int, c_int,
+                                 c_void_p, c_int]),
     "octgb_average_repeats": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_int, c_int, c_void_p,
                                       c_int]),
     "octgb_row_add_batch_ex": (c_int, [c_void_p, c_int, c_void_p, c_int, c_int, c_int, c_int, c_int, c_int, c_int,
@@ -244,6 +246,16 @@ class Context:
         self._check(self.lib.octgb_magnitude(self.h, p, dt, loc, B, interf, apod_size, op, oloc))
         return out
 
+    def prepared_lines(self, raw, apod_size: int, binning: int = 1, apod_mode: int = 0, apod_group: int = 1,
+                       raw_dtype=None) -> int:
+        """Lines per B-scan of prepare_raw's result (apodisation + kept scan
+        lines); a shape query, no device work."""
+        raw, p, loc, dt, B, n_lines = self._raw_args(raw, apod_size, raw_dtype)
+        n_out = ctypes.c_int(0)
+        self._check(self.lib.octgb_prepare_raw(self.h, p, dt, loc, 0, n_lines, apod_size, binning, apod_mode,
+                                               apod_group, ctypes.c_void_p(16), HOST, ctypes.byref(n_out)))
+        return n_out.value
+
     def prepare_raw(self, raw, apod_size: int, binning: int = 1, apod_mode: int = 0, apod_group: int = 1,
                     out=None, raw_dtype=None):
         """prepare_raw on the device: (B, lines, N) -> float32 (B, a + kept, N)
@@ -251,13 +263,32 @@ class Context:
         raw, p, loc, dt, B, n_lines = self._raw_args(raw, apod_size, raw_dtype)
         n_out = ctypes.c_int(0)
         if out is None:
-            # shape first (no work when B = 0), then the call
-            self._check(self.lib.octgb_prepare_raw(self.h, p, dt, loc, 0, n_lines, apod_size, binning, apod_mode,
-                                                   apod_group, ctypes.c_void_p(16), HOST, ctypes.byref(n_out)))
-            out = np.empty((B, n_out.value, self.n), np.float32)
+            out = np.empty((B, self.prepared_lines(raw, apod_size, binning, apod_mode, apod_group, raw_dtype),
+                            self.n), np.float32)
         op, oloc = _ptr(out)
         self._check(self.lib.octgb_prepare_raw(self.h, p, dt, loc, B, n_lines, apod_size, binning, apod_mode,
                                                apod_group, op, oloc, ctypes.byref(n_out)))
+        return out
+
+    def srr_decode(self, words, apod_range, scan_range, out=None):
+        """Thorlabs SRR words (n_files, file_lines, n) uint16 (host or device)
+        -> (n_files, apod + scan lines, n) int16, decoded on the device
+        (io/srr.py:108-125).  A numpy result for numpy input unless `out` (a
+        device or host array of that shape) is given."""
+        if isinstance(words, np.ndarray):
+            words = np.ascontiguousarray(words, dtype=np.uint16)
+        elif not words.is_contiguous():
+            words = words.contiguous()
+        if words.ndim != 3:
+            raise ValueError("words must be (n_files, file_lines, n)")
+        n_files, file_lines, n = (int(v) for v in words.shape)
+        a0, a1 = (int(v) for v in apod_range)
+        s0, s1 = (int(v) for v in scan_range)
+        if out is None:
+            out = np.empty((n_files, (a1 - a0) + (s1 - s0), n), np.int16)
+        p, loc = _ptr(words)
+        op, oloc = _ptr(out)
+        self._check(self.lib.octgb_srr_decode(self.h, p, loc, n_files, file_lines, n, a0, a1, s0, s1, op, oloc))
         return out
 
     def average_repeats(self, mag, n_frames: int, bscan_avg: int, ascan_avg: int, out=None):

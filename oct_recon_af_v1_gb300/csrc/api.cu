@@ -157,7 +157,7 @@ struct octgb_ctx {
     // legacy TIFF encoding
     DevBuf enc_bits, enc_lut, enc_slots, enc_sizes;
     // rare raw formats: prepared batch, frame-mean lines, per-file magnitudes
-    DevBuf prep, prep_apod, magrep;
+    DevBuf prep, prep_apod, magrep, srr;
     // precision form (tensor-core sinc)
     bool prec_ok = false;
     DevBuf prec_w, prec_kb, prec_hi, prec_lo, prec_m, prec_x;
@@ -472,7 +472,7 @@ int octgb_destroy(octgb_ctx* c) {
                       &c->den, &c->plan_table, &c->run_mm, &c->magbuf, &c->dbbuf, &c->planemm, &c->segs, &c->qtable,
                       &c->qcounter, &c->disp_x, &c->disp_hann, &c->disp_phase, &c->disp_a, &c->disp_score, &c->xmed,
                       &c->prec_w, &c->prec_kb, &c->prec_hi, &c->prec_lo, &c->prec_m, &c->prec_x, &c->prep,
-                      &c->prep_apod, &c->magrep, &c->enc_bits, &c->enc_lut, &c->enc_slots, &c->enc_sizes})
+                      &c->prep_apod, &c->magrep, &c->srr, &c->enc_bits, &c->enc_lut, &c->enc_slots, &c->enc_sizes})
         b->release();
     for (QTable* t : c->qtables) {
         t->buf.release();
@@ -1189,7 +1189,7 @@ int octgb_graph_end(octgb_ctx* c, int* graph_id) {
                           &c->run_mm, &c->magbuf, &c->dbbuf, &c->planemm, &c->segs, &c->qtable, &c->qcounter,
                           &c->disp_x, &c->disp_hann, &c->disp_phase, &c->disp_a, &c->disp_score, &c->xmed,
                           &c->prec_hi, &c->prec_lo, &c->prec_m, &c->prec_x, &c->prep, &c->prep_apod,
-                          &c->magrep, &c->enc_bits, &c->enc_lut, &c->enc_slots, &c->enc_sizes})
+                          &c->magrep, &c->srr, &c->enc_bits, &c->enc_lut, &c->enc_slots, &c->enc_sizes})
             b->keep_old = true;
         for (int k = 0; k < octgb_ctx::kRing; ++k) c->ring[k].keep_old = true;
         c->launches.store(c->capture_launch0);
@@ -1524,6 +1524,48 @@ int octgb_prepare_raw(octgb_ctx* c, const void* raw, int dtype, int loc, int B, 
         if (B == 0) return;
         run_prepare(c, a, dtype, loc);
         copy_out(c, out, out_loc, c->prep.p, static_cast<size_t>(B) * (a.a_out + a.n_kept) * kN * sizeof(float));
+        check_status(c);
+    });
+}
+
+int octgb_srr_decode(octgb_ctx* c, const uint16_t* words, int loc, int n_files, int file_lines, int n, int apod_start,
+                     int apod_end, int scan_start, int scan_end, int16_t* out, int out_loc) {
+    return guarded(c, [&] {
+        require(words != nullptr && out != nullptr, "NULL buffer");
+        require(n_files >= 0 && file_lines >= 1 && n >= 1, "bad SRR file shape");
+        require(apod_start >= 0 && apod_start < apod_end && apod_end <= file_lines,
+                "apodisation lines must be a non-empty range inside the file");
+        require(scan_start >= 0 && scan_start < scan_end && scan_end <= file_lines,
+                "scan lines must be a non-empty range inside the file");
+        const int na = apod_end - apod_start, lines_out = na + (scan_end - scan_start);
+        if (n_files == 0) return;
+        const size_t out_bytes = static_cast<size_t>(n_files) * lines_out * n * sizeof(int16_t);
+        int16_t* dst = out;
+        if (out_loc != OCTGB_DEVICE) {
+            ck(c->srr.ensure(out_bytes), "cudaMalloc(srr)");
+            dst = c->srr.as<int16_t>();
+        }
+        if (loc == OCTGB_DEVICE) {
+            ck(launch_srr_decode(words, static_cast<int64_t>(file_lines) * n, apod_start, na, scan_start, lines_out, n,
+                                 n_files, dst, c->stream),
+               "SRR decode kernel");
+        } else {
+            // only the used lines cross the link: two strided copies into the
+            // output layout, then the 12-bit decode in place
+            const size_t row = static_cast<size_t>(n) * sizeof(uint16_t);
+            const size_t sp = static_cast<size_t>(file_lines) * row, dp = static_cast<size_t>(lines_out) * row;
+            ck(cudaMemcpy2DAsync(dst, dp, words + static_cast<size_t>(apod_start) * n, sp, na * row, n_files,
+                                 cudaMemcpyHostToDevice, c->stream),
+               "H2D SRR apodisation lines");
+            ck(cudaMemcpy2DAsync(dst + static_cast<size_t>(na) * n, dp, words + static_cast<size_t>(scan_start) * n, sp,
+                                 (scan_end - scan_start) * row, n_files, cudaMemcpyHostToDevice, c->stream),
+               "H2D SRR scan lines");
+            ck(launch_srr_decode(reinterpret_cast<const uint16_t*>(dst), static_cast<int64_t>(lines_out) * n, 0, na, na,
+                                 lines_out, n, n_files, dst, c->stream),
+               "SRR decode kernel");
+        }
+        c->launches++;
+        if (out_loc != OCTGB_DEVICE) copy_out(c, out, OCTGB_HOST, dst, out_bytes);
         check_status(c);
     });
 }

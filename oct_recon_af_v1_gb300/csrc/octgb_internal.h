@@ -167,6 +167,8 @@ struct PrepArgs {
     int binning, mode, group;   // mode 0: apodisation lines, 1: frame mean over `group` files
 };
 cudaError_t launch_prepare(const PrepArgs& p, int dtype, float* frame_apod, float* out, cudaStream_t st);
+cudaError_t launch_srr_decode(const uint16_t* src, int64_t src_file, int a0, int na, int s0, int lines_out, int n,
+                              int n_files, int16_t* out, cudaStream_t st);
 cudaError_t launch_avg_repeats(const float* mag, int n_frames, int nb, int size_x, int na, int nz, float* out,
                                cudaStream_t st);
 

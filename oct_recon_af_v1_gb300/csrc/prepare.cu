@@ -17,6 +17,11 @@
 //   k_avg_repeats  (n_frames * nb, size_x * na, nz) -> (n_frames, size_x, nz):
 //                  mean over the nb B-scan repeats, then over the na A-scan
 //                  repeats (sequential float32 sums, then the division)
+//   k_srr_decode   Thorlabs SRR files (octrecon/io/srr.py:108-125): uint16
+//                  words whose low 12 bits are the sample (data % 4096, kept
+//                  as int16); each file's apodisation lines [a0, a0 + na) and
+//                  scan lines [s0, ...) gathered into the (files, na + scan, n)
+//                  int16 layout the spectral stage reads
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -103,6 +108,36 @@ __global__ void k_avg_repeats(const float* __restrict__ mag, int n_frames, int n
     }
 }
 
+// Vec: eight samples per thread with 16-byte accesses (n a multiple of 8,
+// both buffers 16-byte aligned).  src may equal out with the identity line map
+// (each thread reads its own words before writing them), so no __restrict__.
+template <bool Vec>
+__global__ void k_srr_decode(const uint16_t* src, int64_t src_file, int a0, int na, int s0, int lines_out, int n,
+                             int64_t total, int16_t* out) {
+    constexpr int kV = Vec ? 8 : 1;
+    const int nv = n / kV;
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < total;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const int jv = static_cast<int>(i % nv);
+        const int64_t fl = i / nv;                        // file * lines_out + line
+        const int l = static_cast<int>(fl % lines_out);
+        const int64_t f = fl / lines_out;
+        const int line = l < na ? a0 + l : s0 + (l - na);
+        const int64_t si = f * src_file + static_cast<int64_t>(line) * n + static_cast<int64_t>(jv) * kV;
+        const int64_t di = fl * n + static_cast<int64_t>(jv) * kV;
+        if (Vec) {
+            uint4 u = *reinterpret_cast<const uint4*>(src + si);
+            u.x &= 0x0fff0fffu;
+            u.y &= 0x0fff0fffu;
+            u.z &= 0x0fff0fffu;
+            u.w &= 0x0fff0fffu;
+            *reinterpret_cast<uint4*>(out + di) = u;
+        } else {
+            out[di] = static_cast<int16_t>(src[si] & 0x0fffu);
+        }
+    }
+}
+
 int grid_of(int64_t n) {
     int64_t g = (n + 255) / 256;
     return static_cast<int>(g > 65536 ? 65536 : (g < 1 ? 1 : g));
@@ -121,6 +156,19 @@ cudaError_t prepare_t(const PrepArgs& p, float* frame_apod, float* out, cudaStre
 }
 
 }  // namespace
+
+cudaError_t launch_srr_decode(const uint16_t* src, int64_t src_file, int a0, int na, int s0, int lines_out, int n,
+                              int n_files, int16_t* out, cudaStream_t st) {
+    const bool vec = n % 8 == 0 && (reinterpret_cast<uintptr_t>(src) & 15) == 0 &&
+                     (reinterpret_cast<uintptr_t>(out) & 15) == 0 && src_file % 8 == 0;
+    const int64_t total = static_cast<int64_t>(n_files) * lines_out * (vec ? n / 8 : n);
+    if (total == 0) return cudaSuccess;
+    if (vec)
+        k_srr_decode<true><<<grid_of(total), 256, 0, st>>>(src, src_file, a0, na, s0, lines_out, n, total, out);
+    else
+        k_srr_decode<false><<<grid_of(total), 256, 0, st>>>(src, src_file, a0, na, s0, lines_out, n, total, out);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_prepare(const PrepArgs& p, int dtype, float* frame_apod, float* out, cudaStream_t st) {
     if (dtype == 0) return prepare_t<uint16_t>(p, frame_apod, out, st);

@@ -24,6 +24,10 @@ files, so `Reconstructor`, the CLI (`--set device=gb300`) and the web app
 * Estimators asked for device gb300 (estimate_dispersion, detect_focus,
   octrecon/estimation) keep their host logic; their spectral processors and
   the DispersionScorer run on the GB300 kernels (`_register_estimators`).
+* Thorlabs SRR scans (io/srr.py): the read-ahead threads read each file's
+  words as stored and the 12-bit decode plus the apodisation / scan line
+  gather run on the device (`_srr_words`, octgb_srr_decode); only the used
+  lines cross the link.
 * The legacy TIFF writer (io/tiff_writer.py:53-71, called by
   Reconstructor.run) is replaced by `tiff.write_legacy_tiff`: same file
   layout, codes and PackBits packets computed on the GPU.
@@ -230,6 +234,48 @@ class _RowEngine:
                 None if oc is None else oc.shift, None if oc is None else oc.pdz)
         from .stitching import min_weight_threshold
         self.threshold = min_weight_threshold(np.float32)
+        self._srr_buf = None
+
+    def srr_raw(self, sw: _SrrWords):
+        """Device int16 (files, interf, n) of one batch of SRR words, in a
+        buffer reused batch after batch (every use is on the context's stream)."""
+        import torch
+        a0, a1 = sw.apod_range
+        s0, s1 = sw.scan_range
+        shape = (sw.words.shape[0], (a1 - a0) + (s1 - s0), sw.words.shape[2])
+        if self._srr_buf is None or tuple(self._srr_buf.shape) != shape:
+            self._srr_buf = torch.empty(shape, dtype=torch.int16, device=f"cuda:{self.ctx.device}")
+        return self.ctx.srr_decode(sw.words, sw.apod_range, sw.scan_range, out=self._srr_buf)
+
+
+class _SrrWords:
+    """The files of one batch as stored, (files, file_lines, n) uint16, and
+    the header's line ranges."""
+
+    def __init__(self, words, apod_range, scan_range):
+        self.words, self.apod_range, self.scan_range = words, apod_range, scan_range
+
+
+def _srr_words(reader, file_indices, n_lambda: int) -> _SrrWords:
+    """SRRTileReader.read_file without the decode (io/srr.py:108-118): each
+    file's words after its header, the same size check; the decode and the
+    line gather of read_bscans (:120-125) run on the device."""
+    from pathlib import Path
+    h = reader.srr
+    file_lines = int(reader.file_lines)
+    words = np.empty((len(file_indices), file_lines, n_lambda), np.uint16)
+    for k, fi in enumerate(file_indices):
+        p = Path(reader.dir) / reader.file_name(fi)
+        b = p.read_bytes()
+        data = np.frombuffer(b, dtype="<u2", offset=h["headerTotalBytes"], count=(len(b) - h["headerTotalBytes"]) // 2)
+        if data.size != n_lambda * file_lines:
+            raise IOError(f"{p}: expected {n_lambda * file_lines} samples, got {data.size}")
+        words[k] = data.reshape(file_lines, n_lambda)
+    return _SrrWords(words, (h["apodstart"], h["apodend"]), (h["scanstart"], h["scanend"]))
+
+
+def _is_srr(reader) -> bool:
+    return getattr(reader, "layout", None) == "srr" and hasattr(reader, "srr") and hasattr(reader, "file_lines")
 
 
 def _attach(R, device_index: int) -> None:
@@ -256,8 +302,11 @@ def _process_row(self, yi: int, frames=None, pool=None, on_batch=None):
     def read_job(job):
         t, s, fr = job
         files = [f for fr_ in fr for f in self.frame_files(int(fr_))]
+        rd = self.reader(t.folder)
+        if _is_srr(rd):
+            return _srr_words(rd, files, hdr.n_lambda)
         buf = np.empty((len(files), hdr.interf_size, hdr.n_lambda), np.dtype(hdr.raw_dtype))
-        self.reader(t.folder).read_bscans(files, buf)
+        rd.read_bscans(files, buf)
         return buf
 
     ctx = eng.ctx
@@ -285,6 +334,8 @@ def _process_row(self, yi: int, frames=None, pool=None, on_batch=None):
             if nxt is not None:
                 pending.append((nxt, pool.submit(read_job, nxt)))
             t, s, fr = job
+            if isinstance(raw, _SrrWords):
+                raw = eng.srr_raw(raw)
             # spectral stage + stitching + accumulation of this batch on the device
             if eng.rare:
                 ctx.row_add_batch_ex(eng.plans[(t.xi, t.zi)], raw, hdr.apod_size, fr, s, eng.binning, eng.apod_mode,

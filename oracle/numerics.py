@@ -480,6 +480,17 @@ def prepare_raw(raw, apod_size, binning=1, apod_mode="lines", apod_group=1, dtyp
     return raw
 
 
+def srr_decode(words, apod_range, scan_range):
+    """io/srr.py:108-125: SRR words (files, file_lines, n) uint16 -> int16
+    (files, apod + scan lines, n): every word modulo 4096 (only the low 12 bits
+    are data, :118), then each file's apodisation lines [apodstart, apodend)
+    followed by its scan lines [scanstart, scanend) (read_bscans, :120-125)."""
+    w = (np.asarray(words, dtype=np.uint16) % 4096).astype(np.int16)
+    a0, a1 = apod_range
+    s0, s1 = scan_range
+    return np.concatenate([w[:, a0:a1], w[:, s0:s1]], axis=1)
+
+
 def average_repeats(mag, n_frames, bscan_avg, size_x, ascan_avg):
     """core/spectral.py:168-177: mean over B-scan repeats, then A-scan repeats."""
     nb, na = max(1, bscan_avg), max(1, ascan_avg)

@@ -1,6 +1,7 @@
 """Rare raw formats on the host (no GPU): the oracle's prepare_raw,
-AScanBinning and average_repeats restatements against the reference's own
-outputs (tests/golden/formats_case.npz, make_golden_formats.py), bit for bit."""
+AScanBinning, average_repeats and SRR 12-bit decode restatements against the
+reference's own outputs (tests/golden/formats_case.npz, make_golden_formats.py;
+srr_case.npz, make_golden_srr.py), bit for bit."""
 from __future__ import annotations
 
 from pathlib import Path
@@ -39,3 +40,34 @@ def test_binning_edges():
     h = np.float32(1.0 / 3)
     np.testing.assert_array_equal(b3[:, 0], (x[:, 0] * h + x[:, 1] * h))
     np.testing.assert_array_equal(b3[:, 2], (x[:, 5] * h + x[:, 6] * h))
+
+
+def test_srr_decode_matches_reference_reader():
+    srr = np.load(GOLDEN / "srr_case.npz")
+    a0, a1, s0, s1 = (int(v) for v in srr["ranges"])
+    assert (srr["words"] >= 4096).any()                 # the upper bits are set in the files
+    got = O.srr_decode(srr["words"], (a0, a1), (s0, s1))
+    assert got.dtype == srr["decoded"].dtype
+    np.testing.assert_array_equal(got, srr["decoded"])
+
+
+def test_plugin_srr_words_match_reference_reader(tmp_path):
+    """The plug-in's read-ahead of SRR files (words as stored) followed by the
+    oracle's decode equals the reference reader's read_bscans."""
+    import tarfile
+
+    from octrecon_ref import import_octrecon
+    import_octrecon()
+    from octrecon.io.srr import SRRTileReader
+
+    from oct_recon_af_v1_gb300.plugin import _is_srr, _srr_words
+    with tarfile.open(GOLDEN / "srr_volume.tar.xz") as tf:
+        tf.extractall(tmp_path, filter="data")
+    tile = sorted(p for p in (tmp_path / "srr").rglob("*.srr"))[0].parent
+    rd = SRRTileReader(tile)
+    assert _is_srr(rd)
+    files = [0, 3, 1]
+    sw = _srr_words(rd, files, rd.header.n_lambda)
+    ref = np.empty((len(files), rd.header.interf_size, rd.header.n_lambda), np.int16)
+    rd.read_bscans(files, ref)
+    np.testing.assert_array_equal(O.srr_decode(sw.words, sw.apod_range, sw.scan_range), ref)
