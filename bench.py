@@ -188,11 +188,12 @@ class Volume:
         return sum(int(t.numel()) * 2 for t in self.raw.values())
 
 
-def run_step(ctx, vol, src, db_vol, bits, batch=6):
+def run_step(ctx, vol, src, db_vol, bits, batch=9):
     """One whole-volume reconstruction through the frame-batch API: for each
     y-row and each batch of `batch` frames, every tile's spectral stage and
     the stitched, finalised planes (num/den never leave the chip; the
-    magnitudes of a batch stay in L2); then the legacy quantisation with the
+    magnitudes of a batch are read back right after they are written, largely
+    from L2); then the legacy quantisation with the
     running (global) clim read on the device.  src maps tile keys to device or
     pinned-host int16 tensors holding uint16 spectra."""
     ids = [vol.st[k].plan for k in vol.order]
@@ -914,7 +915,7 @@ def main():
     ap.add_argument("--no-plain", action="store_true", help="skip timing the reference's plain float32 GPU path")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--ref-frames", type=int, default=4)
-    ap.add_argument("--batch", type=int, default=6, help="frames per frame batch")
+    ap.add_argument("--batch", type=int, default=9, help="frames per frame batch")
     ap.add_argument("--bscans", type=int, default=270, help="B-scans per tile (270 = the full workload)")
     ap.add_argument("--no-graph", action="store_true")
     args = ap.parse_args()
