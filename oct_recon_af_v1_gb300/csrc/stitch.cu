@@ -202,7 +202,10 @@ __global__ void __launch_bounds__(kStThreads) k_stitch_frames(const StitchDev* _
     int* zr_s = reinterpret_cast<int*>(smem_all);                  // [ns_max][kFZ]
     float* wz0_s = smem_all + ns_max * kFZ;
     float* wz1_s = wz0_s + ns_max * kFZ;
-    int* xr_s = reinterpret_cast<int*>(wz1_s + ns_max * kFZ);      // [ns_max][kBlk]
+    float* fz0_s = wz1_s + ns_max * kFZ;                          // F of the row's two taps
+    float* fz1_s = fz0_s + ns_max * kFZ;
+    float* dz_s = fz1_s + ns_max * kFZ;                           // depth-interpolated F
+    int* xr_s = reinterpret_cast<int*>(dz_s + ns_max * kFZ);      // [ns_max][kBlk]
     float* wx0_s = reinterpret_cast<float*>(xr_s + ns_max * kBlk);
     float* wx1_s = wx0_s + ns_max * kBlk;
     float* sm = wx1_s + ns_max * kBlk;
@@ -222,11 +225,19 @@ __global__ void __launch_bounds__(kStThreads) k_stitch_frames(const StitchDev* _
         const StitchSlot s = slot[k];
         const StitchDev& p = plans[tl.id[s.t]];
         if (tid < kFZ) {
+            // without the optical-path correction F depends on the row only:
+            // its two taps and the depth-interpolated F (the den term) per row
             const int zo = zb + tid;
             const int zr = zo < p.n_out_z ? p.zr[zo] : -1;
+            const float w0 = zr >= 0 ? p.wz0[zo] : 0.f, w1 = zr >= 0 ? p.wz1[zo] : 0.f;
+            const bool has_r1 = zr >= 0 && zr - s.r_lo + 1 < s.rs;
+            const float fa = zr >= 0 ? p.fz[zr] : 0.f, fb = has_r1 ? p.fz[zr + 1] : 0.f;
             zr_s[k * kFZ + tid] = zr;
-            wz0_s[k * kFZ + tid] = zr >= 0 ? p.wz0[zo] : 0.f;
-            wz1_s[k * kFZ + tid] = zr >= 0 ? p.wz1[zo] : 0.f;
+            wz0_s[k * kFZ + tid] = w0;
+            wz1_s[k * kFZ + tid] = w1;
+            fz0_s[k * kFZ + tid] = fa;
+            fz1_s[k * kFZ + tid] = fb;
+            dz_s[k * kFZ + tid] = fmaf(fb, w1, fa * w0);
         } else if (tid < kFZ + kBlk) {
             const int cc = cb + tid - kFZ - p.c0;
             const int xr = (cc >= 0 && cc < p.C) ? p.xr[cc] : -1;
@@ -276,7 +287,6 @@ __global__ void __launch_bounds__(kStThreads) k_stitch_frames(const StitchDev* _
         const float* pa = sm + s.off;
         const float* pf = pa + s.xs * s.rs;
         const bool opc = s.opc != 0;
-        const float* fz = plans[tl.id[s.t]].fz;
         const int x0 = xr - s.x_lo;
         const bool has_x1 = x0 + 1 < s.xs;
         const float wx0 = wx0_s[k * kBlk + tx], wx1 = wx1_s[k * kBlk + tx];
@@ -289,25 +299,29 @@ __global__ void __launch_bounds__(kStThreads) k_stitch_frames(const StitchDev* _
             const bool has_r1 = rr + 1 < s.rs;
             const float w0 = wz0_s[k * kFZ + z], w1 = wz1_s[k * kFZ + z];
             const float* a0p = pa + x0 * s.rs + rr;
-            float f00, f01, f10, f11;
+            float f00, f01, f10, f11, d0, d1;
             if (opc) {
                 const float* f0p = pf + x0 * s.rs + rr;
                 f00 = f0p[0];
                 f01 = has_r1 ? f0p[1] : 0.f;
                 f10 = has_x1 ? f0p[s.rs] : 0.f;
                 f11 = has_x1 && has_r1 ? f0p[s.rs + 1] : 0.f;
+                d0 = fmaf(f01, w1, f00 * w0);
+                d1 = fmaf(f11, w1, f10 * w0);
             } else {
-                f00 = fz[zr];
-                f01 = has_r1 ? fz[zr + 1] : 0.f;
+                // the same values as the general form with F10 = F00, F11 = F01
+                f00 = fz0_s[k * kFZ + z];
+                f01 = fz1_s[k * kFZ + z];
                 f10 = has_x1 ? f00 : 0.f;
                 f11 = has_x1 ? f01 : 0.f;
+                d0 = dz_s[k * kFZ + z];
+                d1 = has_x1 ? d0 : 0.f;
             }
             // a = magnitude * F (TileStitcher.contribute, stitching.py:136)
             const float a00 = a0p[0] * f00, a01 = has_r1 ? a0p[1] * f01 : 0.f;
             const float a10 = has_x1 ? a0p[s.rs] * f10 : 0.f;
             const float a11 = has_x1 && has_r1 ? a0p[s.rs + 1] * f11 : 0.f;
             const float u0 = fmaf(a01, w1, a00 * w0), u1 = fmaf(a11, w1, a10 * w0);
-            const float d0 = fmaf(f01, w1, f00 * w0), d1 = fmaf(f11, w1, f10 * w0);
             an[q] += fmaf(u1, wx1, u0 * wx0);
             ad[q] += fmaf(d1, wx1, d0 * wx0);
         }
@@ -553,7 +567,7 @@ cudaError_t launch_stitch_frames(const StitchDev* plans_dev, const TileList& til
                                  int64_t mag_tile_stride, int B, int n_tile_x, int f0, int n_out_z, int n_out_x,
                                  float thr, float* db, unsigned int* plane_mm, unsigned int* run_mm, cudaStream_t st) {
     if (B == 0) return cudaSuccess;
-    const size_t smem = patch_smem_bytes + sizeof(float) * static_cast<size_t>(ns_max) * 3 * (kFZ + kBlk) + 16;
+    const size_t smem = patch_smem_bytes + sizeof(float) * static_cast<size_t>(ns_max) * (6 * kFZ + 3 * kBlk) + 16;
     if (smem > 160 * 1024) return cudaErrorInvalidValue;
     cudaError_t e = cudaFuncSetAttribute(k_stitch_frames, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(smem));
