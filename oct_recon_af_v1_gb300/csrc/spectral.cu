@@ -7,7 +7,8 @@
 //       next quad's rows stream in while the current quad is computed;
 //   (b) d[j] = float(raw[j]) - apod[j] (float32 apodisation mean of the
 //       B-scan, rounded from an exact sum as core/cpu_kernels.py:20-25 does),
-//       line mean m removed (cpu_kernels.py:26-36);
+//       line mean m removed before d reaches shared memory (cpu_kernels.py:
+//       26-36);
 //   (c) banded sinc k-linearisation, sum_t w[t,i] * d[start_i + t]
 //       (cpu_kernels.py:37-40), float32 accumulation;
 //   (d) (acc + m) * window[i] (Hann/rms * dispersion phase, scaled by 1/N for
@@ -252,9 +253,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
         const SlotRef me = slot_ref<RawT, kQueue>(a, quad0_s, quad, g);
         const bool valid = me.valid;
         const float* apod = a.apod_mean + me.apod_row * kN;
-        // d = raw - apod goes to shared memory now; the line mean m is
-        // subtracted when the sinc loads its window (the same float32 value
-        // d - m the reference stores, cpu_kernels.py:35-36)
+        // d = raw - apod stays in registers until the line mean m is known;
+        // shared memory receives d - m (the float32 value the reference
+        // stores, cpu_kernels.py:35-36), so the sinc reads its window as is
+        float dv[16];
         float sum = 0.f;
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
@@ -262,18 +264,26 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
             float rv[4];
             RawLoad<RawT>::load4(&S.stage[buf][g][j], rv);
             const float4 ap = __ldg(reinterpret_cast<const float4*>(apod + j));
-            const float d0 = rv[0] - ap.x, d1 = rv[1] - ap.y, d2 = rv[2] - ap.z, d3 = rv[3] - ap.w;
-            S.d[g][skew(j)] = d0;
-            S.d[g][skew(j + 1)] = d1;
-            S.d[g][skew(j + 2)] = d2;
-            S.d[g][skew(j + 3)] = d3;
-            sum += (d0 + d1) + (d2 + d3);
+            dv[4 * q] = rv[0] - ap.x;
+            dv[4 * q + 1] = rv[1] - ap.y;
+            dv[4 * q + 2] = rv[2] - ap.z;
+            dv[4 * q + 3] = rv[3] - ap.w;
+            sum += (dv[4 * q] + dv[4 * q + 1]) + (dv[4 * q + 2] + dv[4 * q + 3]);
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
         if (lane == 0) S.red[g][warp & 3] = sum;
         group_sync(g);
-        if (lt == 0) S.mval[g] = ((S.red[g][0] + S.red[g][1]) + (S.red[g][2] + S.red[g][3])) * (1.0f / kN);
+        {
+            const float m = ((S.red[g][0] + S.red[g][1]) + (S.red[g][2] + S.red[g][3])) * (1.0f / kN);
+            if (lt == 0) S.mval[g] = m;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int j = 4 * lt + 512 * q;
+#pragma unroll
+                for (int i = 0; i < 4; ++i) S.d[g][skew(j + i)] = dv[4 * q + i] - m;
+            }
+        }
         __syncthreads();
 
         // ---- (c)+(d) sinc k-linearisation and window, four A-scans ----
@@ -288,7 +298,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
                 const float mk = S.mval[k];
                 float win[U];
 #pragma unroll
-                for (int u = 0; u < U; ++u) win[u] = S.d[k][skew(s0 + u)] - mk;
+                for (int u = 0; u < U; ++u) win[u] = S.d[k][skew(s0 + u)];
 #pragma unroll
                 for (int r = 0; r < 4; ++r) {
                     float acc = 0.f;
