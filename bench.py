@@ -610,7 +610,7 @@ def gpu_arm_config4(args, rank, world, torch, ctx, stream, dev):
 
     def learned_step(src):
         imgs = mk.images(src, out=img_buf, raw_dtype=U16)
-        pred = net.forward(imgs)
+        pred = net.predict(imgs)
         pred_host.copy_(pred, non_blocking=True)
 
     def timed(fn, steps, warm):
@@ -669,7 +669,7 @@ def gpu_arm_config4(args, rank, world, torch, ctx, stream, dev):
             "config": config4_desc(n_train, n_base, epochs), "gpu_launches": int(launches),
             "roofline": {"bound": "hbm", "achieved": raw_bytes / (ms_learned * 1e-3) / 1e9, "peak": hbm,
                          "unit": "GB/s", "frac": raw_bytes / (ms_learned * 1e-3) / 1e9 / hbm, "traffic": None,
-                         "kernel": "whole learned step (linearise, 3 probe FFT passes, pooling, CNN forward)",
+                         "kernel": "whole learned step (linearise, 3 probe FFT passes, pooling, CNN forward on the tensor cores)",
                          "bytes_per_launch": raw_bytes, "peak_source": src + " (burst copy)"},
             "clocks": clk,
             "search": {"value": v_s, "unit": "A-scans/s", "seconds": t_search, "evaluations": n_evals,

@@ -348,6 +348,20 @@ int octgb_cnn_images(octgb_ctx *ctx, const float *mag, int n_probe, int nb, int 
 /* y = conv3x3(x, w) + b, stride 1, zero padding 1: x (n, cin, h, w), w (cout, cin, 3, 3), b (cout) or NULL. */
 int octgb_cnn_conv3x3(octgb_ctx *ctx, const float *x, const float *w, const float *b, float *y, int n, int cin,
                       int cout, int h, int wd);
+/* octgb_cnn_conv3x3 on the tensor cores (tcgen05.mma, FP16 operands, float32
+ * accumulation in TMEM): the inference form of the learned estimator's
+ * convolutions.  Shapes: 1 <= cin <= 32, cout a multiple of 32 up to 128, wd
+ * a multiple of 128, or a divisor of 128 with h a multiple of 128 / wd.
+ * Asynchronous; a bounded device wait that expires is reported by the next
+ * synchronising call (OCTGB_ERR_TIMEOUT). */
+int octgb_cnn_conv3x3_tc(octgb_ctx *ctx, const float *x, const float *w, const float *b, float *y, int n, int cin,
+                         int cout, int h, int wd);
+/* octgb_cnn_conv3x3_tc followed by octgb_cnn_relu_pool in one kernel (the
+ * pre-activations never reach memory): p (n, cout, h/2, wd/2) = 0.25 *
+ * ((relu + relu) + (relu + relu)) of each 2x2 block.  wd a multiple of 128, h
+ * even. */
+int octgb_cnn_conv3x3_relu_pool_tc(octgb_ctx *ctx, const float *x, const float *w, const float *b, float *p, int n,
+                                   int cin, int cout, int h, int wd);
 /* Gradients of octgb_cnn_conv3x3: dw, db from dy and x; dx (optional) with
  * w_scratch (cout * cin * 9 floats) for the flipped kernel. */
 int octgb_cnn_conv3x3_bwd(octgb_ctx *ctx, const float *x, const float *w, const float *dy, float *dx, float *dw,

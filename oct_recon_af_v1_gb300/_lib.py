@@ -73,6 +73,10 @@ SIGNATURES = {
     "octgb_cnn_images": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_int]),
     "octgb_cnn_conv3x3": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_int,
                                   c_int]),
+    "octgb_cnn_conv3x3_tc": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_int,
+                                  c_int]),
+    "octgb_cnn_conv3x3_relu_pool_tc": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_int,
+                                  c_int]),
     "octgb_cnn_conv3x3_bwd": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                       c_void_p, c_int, c_int, c_int, c_int, c_int]),
     "octgb_cnn_relu_pool": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_int, c_int]),

@@ -1789,6 +1789,33 @@ int octgb_cnn_conv3x3(octgb_ctx* c, const float* x, const float* w, const float*
     });
 }
 
+int octgb_cnn_conv3x3_tc(octgb_ctx* c, const float* x, const float* w, const float* b, float* y, int n, int cin,
+                         int cout, int h, int wd) {
+    return guarded(c, [&] {
+        require(x && w && y, "NULL buffer");
+        require(n >= 1 && h >= 1 && wd >= 1, "bad convolution shape");
+        require(conv3x3_tc_supported(cin, cout, h, wd),
+                "tensor-core convolution: 1 <= cin <= 32, cout a multiple of 32 up to 128, and the width a "
+                "multiple of 128 or a divisor of 128 whose row count divides the height");
+        ck(launch_conv3x3_tc(x, w, b, y, n, cin, cout, h, wd, 0, c->status_dev, c->stream), "tensor-core conv kernel");
+        c->launches++;
+    });
+}
+
+int octgb_cnn_conv3x3_relu_pool_tc(octgb_ctx* c, const float* x, const float* w, const float* b, float* p, int n,
+                                   int cin, int cout, int h, int wd) {
+    return guarded(c, [&] {
+        require(x && w && p, "NULL buffer");
+        require(n >= 1 && h >= 1 && wd >= 1, "bad convolution shape");
+        require(conv3x3_tc_pool_supported(cin, cout, h, wd),
+                "fused tensor-core convolution + pool: 1 <= cin <= 32, cout a multiple of 32 up to 128, the width "
+                "a multiple of 128 and the height even");
+        ck(launch_conv3x3_tc(x, w, b, p, n, cin, cout, h, wd, 1, c->status_dev, c->stream),
+           "tensor-core conv + pool kernel");
+        c->launches++;
+    });
+}
+
 int octgb_cnn_conv3x3_bwd(octgb_ctx* c, const float* x, const float* w, const float* dy, float* dx, float* dw,
                           float* db, float* w_scratch, int n, int cin, int cout, int h, int wd) {
     return guarded(c, [&] {

@@ -1,0 +1,386 @@
+// Tensor-core 3x3 convolution of the learned estimator (the inference form of
+// cnn.cu's k_conv3x3): stride 1, zero padding 1, + bias, NCHW float32 in and
+// out, FP16 operands and float32 accumulation on the 5th-generation tensor
+// cores (tcgen05.mma kind::f16, accumulator in TMEM).
+//
+// Implicit GEMM without an im2col copy: M = 128 output pixels of one image (a
+// row segment when the width W >= 128, else 128 / W whole rows), N = the
+// output channels, K = 3 x 3 taps x the input channels (chunks of 8, an even
+// number of chunks).  The tile's input rows are staged once in shared memory
+// as fp16, eight channels per 16 bytes, pixel rows contiguous per chunk, so
+// the A operand of tap (dy, dx) is the staged block itself seen through a
+// shifted matrix descriptor (canonical no-swizzle K-major layout, rows 16
+// bytes apart):
+//   W >= 128  rows y0 - 1 .. y0 + 1 with a one-pixel halo (columns x0 - 1 ..
+//             x0 + 128, zero outside the image); tap (dy, dx) starts at pixel
+//             dy * 130 + dx;
+//   W < 128   rows y0 - 1 .. y0 + R without halo, in three copies shifted by
+//             dx - 1 columns with the wrapped column zeroed; tap (dy, dx)
+//             starts at pixel dy * W of copy dx.
+// Per tile one thread issues 9 taps x (chunks / 2) K16 MMAs; the staged block
+// and the accumulator (2 x N TMEM columns) are double-buffered, so tile j's
+// MMAs run while the CTA writes tile j - 1's pre-activations (every warp its
+// 32 TMEM lanes = pixels, + bias, coalesced along x) and stages tile j + 1.
+// Persistent over tiles.  Every mbarrier wait is bounded; on expiry the CTA
+// records the status, waits (bounded) for its MMAs, frees its TMEM and
+// returns.
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "octgb_device.cuh"
+#include "octgb_internal.h"
+
+namespace octgb {
+namespace {
+
+constexpr int kCM = 128;                    // output pixels per tile (MMA M)
+constexpr int kCThreads = 128;              // four warps = the 128 TMEM lanes
+constexpr int kCSlots = 4;                  // staged pixels per thread (a staged block holds <= 512)
+
+struct ConvGeom {
+    int n, cin, cout, H, W;
+    int cin8;          // channel chunks of 8, even (chunks past cin8r are zero)
+    int cin8r;         // chunks holding channels
+    int wseg, rows;    // tile: rows x wseg pixels
+    int halo;          // 1: one staged copy with halo columns (W >= 128); 0: three shifted copies
+    int cols_s;        // staged pixels per row
+    int pix_c;         // staged pixels per chunk (one copy)
+    int nbuf;          // staged buffers (2: the next tile stages while the MMAs read the other)
+    int pool;          // 1: ReLU + 2x2 mean fused into the epilogue (units = vertical tile pairs)
+    int tiles_img;     // tiles per image
+    int64_t n_units;   // tiles, or tile pairs with pool
+    uint32_t xbytes;   // one staged buffer
+    uint32_t off_b, smem;
+    int tmem_cols;
+};
+
+struct ConvBars {
+    uint64_t x[2], d[2], drain;
+    uint32_t tmem;
+    int abort;
+    float bias[128];
+};
+
+__device__ __forceinline__ uint32_t pack_h2(float a, float b) {
+    const __half2 h = __floats2half2_rn(a, b);
+    return *reinterpret_cast<const uint32_t*>(&h);
+}
+
+__device__ __forceinline__ bool conv_wait(uint64_t* bar, uint32_t parity, ConvBars& S, int* status) {
+    bool ok = true;
+    if (*reinterpret_cast<volatile int*>(&S.abort) == 0) {
+        ok = mbar_wait_bounded(bar, parity, status);
+        if (!ok) atomicExch(&S.abort, 1);
+    } else {
+        ok = false;
+    }
+    return __syncthreads_and(ok ? 1 : 0) != 0;
+}
+
+// image and origin of tile h (0, or 1 = the row below with pool) of unit u
+__device__ __forceinline__ void unit_tile(const ConvGeom& g, int64_t u, int h, int& img, int& y0, int& x0) {
+    if (g.pool) {                                 // W >= 128: pairs of row segments
+        const int per_row = g.W / kCM;
+        const int64_t pairs = static_cast<int64_t>(g.H / 2) * per_row;
+        img = static_cast<int>(u / pairs);
+        const int pi = static_cast<int>(u - static_cast<int64_t>(img) * pairs);
+        y0 = 2 * (pi / per_row) + h;
+        x0 = (pi % per_row) * kCM;
+        return;
+    }
+    img = static_cast<int>(u / g.tiles_img);
+    const int ti = static_cast<int>(u - static_cast<int64_t>(img) * g.tiles_img);
+    if (g.W >= kCM) {
+        const int per_row = g.W / kCM;
+        y0 = ti / per_row;
+        x0 = (ti - y0 * per_row) * kCM;
+    } else {
+        y0 = ti * g.rows;
+        x0 = 0;
+    }
+}
+
+__global__ void __launch_bounds__(kCThreads, 2)
+    k_conv3x3_tc(const float* __restrict__ x, const float* __restrict__ w, const float* __restrict__ bias,
+                 float* __restrict__ y, const ConvGeom g, int* status) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    __shared__ ConvBars S;
+    uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    uint8_t* B = base + g.off_b;                         // [9 taps][cin8][cout][16 B]
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const uint32_t b_chunk = static_cast<uint32_t>(g.cout) * 16;
+    const int64_t hw = static_cast<int64_t>(g.H) * g.W;
+    const int copies = g.halo ? 1 : 3;
+    const int U = g.pool ? 2 : 1;                        // tiles per unit
+
+    if (tid == 0) {
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&S.x[b], 1);
+            mbar_init(&S.d[b], 1);
+        }
+        mbar_init(&S.drain, 1);
+        S.abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&S.tmem)),
+                     "r"(g.tmem_cols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    for (int co = tid; co < g.cout; co += kCThreads) S.bias[co] = bias != nullptr ? bias[co] : 0.f;
+    // weights: B[tap][c8][co] = 8 fp16 of channels 8 c8 .. 8 c8 + 7 (zero past cin)
+    for (int i = tid; i < 9 * g.cin8 * g.cout; i += kCThreads) {
+        const int kb = i / g.cout, co = i - kb * g.cout;
+        const int tap = kb / g.cin8, c8 = kb - tap * g.cin8;
+        const int dy = tap / 3, dx = tap - 3 * dy;
+        float v[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) {
+            const int c = 8 * c8 + e;
+            v[e] = c < g.cin ? w[((static_cast<int64_t>(co) * g.cin + c) * 3 + dy) * 3 + dx] : 0.f;
+        }
+        *reinterpret_cast<uint4*>(B + static_cast<uint32_t>(kb) * b_chunk + co * 16) =
+            make_uint4(pack_h2(v[0], v[1]), pack_h2(v[2], v[3]), pack_h2(v[4], v[5]), pack_h2(v[6], v[7]));
+    }
+    // the padding chunks of every staged buffer (never rewritten)
+    {
+        const int npad = (g.cin8 - g.cin8r) * g.pix_c;
+        for (int i = tid; i < g.nbuf * copies * npad; i += kCThreads) {
+            const int bc = i / npad, r = i - bc * npad;                 // bc = buffer * copies + copy
+            uint4* X = reinterpret_cast<uint4*>(base + (bc / copies) * g.xbytes);
+            X[((bc % copies) * g.cin8 + g.cin8r) * g.pix_c + r] = make_uint4(0, 0, 0, 0);
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = S.tmem;
+    const uint32_t idesc = mma_idesc_f16(kCM, g.cout);
+    // the staged source pixels this thread loads: p = tid + 128 k (row, column), -1 past the block
+    int prs[kCSlots], pcs[kCSlots];
+#pragma unroll
+    for (int k = 0; k < kCSlots; ++k) {
+        const int p = tid + kCThreads * k;
+        prs[k] = p < g.pix_c ? p / g.cols_s : -1;
+        pcs[k] = p < g.pix_c ? p - prs[k] * g.cols_s : 0;
+    }
+
+    auto epilogue = [&](int64_t u, int ab) {
+        const int m = 32 * warp + lane;
+        int img, y0, x0;
+        unit_tile(g, u, 0, img, y0, x0);
+        const uint32_t taddr = tmem + (static_cast<uint32_t>(32 * warp) << 16) + static_cast<uint32_t>(ab * U * g.cout);
+        if (!g.pool) {
+            const int oy = y0 + m / g.wseg, ox = x0 + m % g.wseg;
+            float* yo = y + static_cast<int64_t>(img) * g.cout * hw + static_cast<int64_t>(oy) * g.W + ox;
+            for (int c0 = 0; c0 < g.cout; c0 += 32) {
+                float v[32];
+                tmem_ld32(taddr + static_cast<uint32_t>(c0), v);
+#pragma unroll
+                for (int i = 0; i < 32; ++i) {
+                    *yo = v[i] + S.bias[c0 + i];
+                    yo += hw;
+                }
+            }
+        } else {
+            // rows y0 (accumulator 0) and y0 + 1 (accumulator 1); lanes m, m + 1
+            // are the two columns: 0.25 ((relu + relu) + (relu + relu)) as k_relu_pool
+            const int Ho = g.H / 2, Wo = g.W / 2;
+            const int64_t pw = static_cast<int64_t>(Ho) * Wo;
+            float* po = y + static_cast<int64_t>(img) * g.cout * pw + static_cast<int64_t>(y0 / 2) * Wo + (x0 + m) / 2;
+            for (int c0 = 0; c0 < g.cout; c0 += 32) {
+                float v0[32], v1[32];
+                tmem_ld32(taddr + static_cast<uint32_t>(c0), v0);
+                tmem_ld32(taddr + static_cast<uint32_t>(g.cout + c0), v1);
+#pragma unroll
+                for (int i = 0; i < 32; ++i) {
+                    const float bb = S.bias[c0 + i];
+                    const float top = fmaxf(v0[i] + bb, 0.f), bot = fmaxf(v1[i] + bb, 0.f);
+                    const float tsum = top + __shfl_xor_sync(0xffffffffu, top, 1);
+                    const float bsum = bot + __shfl_xor_sync(0xffffffffu, bot, 1);
+                    if ((lane & 1) == 0) *po = 0.25f * (tsum + bsum);
+                    po += pw;
+                }
+            }
+        }
+        tc_fence_before();
+    };
+
+    uint32_t j = 0;            // tiles staged by this CTA so far
+    uint32_t ju = 0;           // units so far (accumulator set ju & 1)
+    int64_t prev = -1;
+    bool ok = true;
+    for (int64_t u = blockIdx.x; u < g.n_units && ok; u += gridDim.x, ++ju) {
+        const int ab = static_cast<int>(ju & 1);
+        for (int h = 0; h < U && ok; ++h, ++j) {
+            const int b = static_cast<int>(j % static_cast<uint32_t>(g.nbuf));
+            if (j >= static_cast<uint32_t>(g.nbuf)) {
+                // the MMAs of the tile staged nbuf tiles ago have read X[b]
+                ok = conv_wait(&S.x[b], ((j - g.nbuf) / g.nbuf) & 1u, S, status);
+                if (!ok) break;
+            }
+            int img, y0, x0;
+            unit_tile(g, u, h, img, y0, x0);
+            uint4* X = reinterpret_cast<uint4*>(base + b * g.xbytes);
+            const float* xi = x + static_cast<int64_t>(img) * g.cin * hw;
+            int off[kCSlots];
+#pragma unroll
+            for (int k = 0; k < kCSlots; ++k) {
+                const int iy = y0 - 1 + prs[k];
+                const int ix = g.halo ? x0 - 1 + pcs[k] : pcs[k];
+                off[k] = (prs[k] >= 0 && iy >= 0 && iy < g.H && ix >= 0 && ix < g.W) ? iy * g.W + ix : -1;
+            }
+            // each source pixel is loaded once (eight channels in flight) and
+            // stored into every copy that holds it: the halo block, or the
+            // three shifted copies (copy dx holds column c + dx - 1; the
+            // wrapped column is zero)
+            for (int c8 = 0; c8 < g.cin8r; ++c8) {
+                const float* xc = xi + static_cast<int64_t>(8 * c8) * hw;
+                const int ne = g.cin - 8 * c8;
+#pragma unroll
+                for (int k = 0; k < kCSlots; ++k) {
+                    if (prs[k] < 0) continue;
+                    float v[8];
+#pragma unroll
+                    for (int e = 0; e < 8; ++e)
+                        v[e] = (off[k] >= 0 && e < ne) ? __ldg(xc + static_cast<int64_t>(e) * hw + off[k]) : 0.f;
+                    const uint4 q = make_uint4(pack_h2(v[0], v[1]), pack_h2(v[2], v[3]), pack_h2(v[4], v[5]),
+                                               pack_h2(v[6], v[7]));
+                    const int p = tid + kCThreads * k;
+                    if (g.halo) {
+                        X[c8 * g.pix_c + p] = q;
+                    } else {
+                        const uint4 z = make_uint4(0, 0, 0, 0);
+                        X[(1 * g.cin8 + c8) * g.pix_c + p] = q;
+                        uint4* X0 = X + c8 * g.pix_c;
+                        uint4* X2 = X + (2 * g.cin8 + c8) * g.pix_c;
+                        if (pcs[k] + 1 < g.W) X0[p + 1] = q;
+                        if (pcs[k] == 0) X0[p] = z;
+                        if (pcs[k] >= 1) X2[p - 1] = q;
+                        if (pcs[k] == g.W - 1) X2[p] = z;
+                    }
+                }
+            }
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            tc_fence_before();
+            __syncthreads();
+            if (tid == 0) {
+                tc_fence_after();
+                const uint8_t* Xb = base + b * g.xbytes;
+                const uint32_t lbo = static_cast<uint32_t>(g.pix_c) * 16;
+                const uint32_t d_tmem = tmem + static_cast<uint32_t>((ab * U + h) * g.cout);
+                for (int tap = 0; tap < 9; ++tap) {
+                    const int dy = tap / 3, dx = tap - 3 * dy;
+                    const uint8_t* a0 = g.halo ? Xb + (dy * g.cols_s + dx) * 16
+                                               : Xb + static_cast<uint32_t>(dx * g.cin8) * lbo + dy * g.W * 16;
+                    for (int ks = 0; ks < g.cin8 / 2; ++ks) {
+                        const uint64_t da = smem_desc(a0 + 2 * ks * lbo, lbo, 128);
+                        const uint64_t db = smem_desc(B + static_cast<uint32_t>(tap * g.cin8 + 2 * ks) * b_chunk,
+                                                      b_chunk, 128);
+                        mma_f16_id(d_tmem, da, db, idesc, (tap > 0 || ks > 0) ? 1u : 0u);
+                    }
+                }
+                mma_commit(&S.x[b]);
+                if (h == U - 1) mma_commit(&S.d[ab]);
+            }
+        }
+        if (!ok) break;
+        if (prev >= 0) {
+            const int pab = static_cast<int>((ju - 1) & 1);
+            ok = conv_wait(&S.d[pab], ((ju - 1) >> 1) & 1u, S, status);
+            if (!ok) break;
+            tc_fence_after();
+            epilogue(prev, pab);
+        }
+        prev = u;
+    }
+    if (ok && prev >= 0) {
+        const int pab = static_cast<int>((ju - 1) & 1);
+        ok = conv_wait(&S.d[pab], ((ju - 1) >> 1) & 1u, S, status);
+        if (ok) {
+            tc_fence_after();
+            epilogue(prev, pab);
+        }
+    }
+    // every MMA this CTA issued has completed before its TMEM is released
+    __syncthreads();
+    if (tid == 0) {
+        mma_commit(&S.drain);
+        mbar_wait_bounded(&S.drain, 0, status);
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(g.tmem_cols)
+                     : "memory");
+}
+
+}  // namespace
+
+bool conv3x3_tc_supported(int cin, int cout, int H, int W) {
+    if (cin < 1 || cin > 32 || cout < 32 || cout > 128 || cout % 32 != 0) return false;
+    if (W >= kCM) return W % kCM == 0;
+    return W >= 1 && kCM % W == 0 && H % (kCM / W) == 0;
+}
+
+bool conv3x3_tc_pool_supported(int cin, int cout, int H, int W) {
+    return conv3x3_tc_supported(cin, cout, H, W) && W >= kCM && H % 2 == 0;
+}
+
+cudaError_t launch_conv3x3_tc(const float* x, const float* w, const float* b, float* y, int n, int cin, int cout,
+                              int H, int W, int pool, int* status, cudaStream_t st) {
+    if (!conv3x3_tc_supported(cin, cout, H, W)) return cudaErrorInvalidValue;
+    if (pool && !conv3x3_tc_pool_supported(cin, cout, H, W)) return cudaErrorInvalidValue;
+    ConvGeom g{};
+    g.n = n;
+    g.cin = cin;
+    g.cout = cout;
+    g.H = H;
+    g.W = W;
+    g.cin8r = (cin + 7) / 8;
+    g.cin8 = (g.cin8r + 1) / 2 * 2;
+    g.halo = W >= kCM ? 1 : 0;
+    g.wseg = W >= kCM ? kCM : W;
+    g.rows = kCM / g.wseg;
+    g.cols_s = g.halo ? g.wseg + 2 : g.wseg;
+    g.pix_c = (g.rows + 2) * g.cols_s;
+    g.nbuf = g.halo ? 2 : 1;
+    g.pool = pool ? 1 : 0;
+    g.tiles_img = static_cast<int>(static_cast<int64_t>(H) * W / kCM);
+    g.n_units = static_cast<int64_t>(n) * g.tiles_img / (pool ? 2 : 1);
+    g.xbytes = static_cast<uint32_t>((g.halo ? 1 : 3) * g.cin8 * g.pix_c) * 16u;
+    g.xbytes = (g.xbytes + 127u) & ~127u;
+    g.off_b = static_cast<uint32_t>(g.nbuf) * g.xbytes;
+    g.smem = g.off_b + 9u * static_cast<uint32_t>(g.cin8) * static_cast<uint32_t>(cout) * 16u + 1024u;
+    const int cols = 2 * (pool ? 2 : 1) * cout;                   // two units of accumulators
+    g.tmem_cols = cols <= 32 ? 32 : (cols <= 64 ? 64 : (cols <= 128 ? 128 : (cols <= 256 ? 256 : 512)));
+    if (g.n_units == 0) return cudaSuccess;
+    if (g.smem > 227u * 1024u || g.pix_c > kCSlots * kCThreads) return cudaErrorInvalidValue;
+    cudaError_t e = cudaFuncSetAttribute(k_conv3x3_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(g.smem));
+    if (e != cudaSuccess) return e;
+    // CTAs per SM: shared memory, registers and TMEM columns
+    int dev = 0, sms = 0, smem_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    cudaFuncAttributes fa{};
+    e = cudaFuncGetAttributes(&fa, k_conv3x3_tc);
+    if (e != cudaSuccess) return e;
+    const int by_smem = smem_sm / static_cast<int>(g.smem + fa.sharedSizeBytes + 1024);
+    const int regs = (fa.numRegs + 7) / 8 * 8;
+    const int by_regs = 65536 / (regs * kCThreads);
+    const int by_tmem = 512 / g.tmem_cols;
+    int per_sm = by_smem < by_regs ? by_smem : by_regs;
+    per_sm = per_sm < by_tmem ? per_sm : by_tmem;
+    per_sm = per_sm < 1 ? 1 : per_sm;
+    const int64_t slots = static_cast<int64_t>(per_sm) * sms;
+    const int64_t grid = g.n_units < slots ? g.n_units : slots;
+    k_conv3x3_tc<<<static_cast<unsigned int>(grid), kCThreads, g.smem, st>>>(x, w, b, y, g, status);
+    return cudaGetLastError();
+}
+
+}  // namespace octgb

@@ -211,6 +211,13 @@ size_t prec_smem_bytes();
 // learned beta/focus estimator (cnn.cu)
 cudaError_t launch_image_pool(const float* A, int n_probe, int nb, int nx, int z_keep, float* img, cudaStream_t st);
 cudaError_t launch_image_norm(float* img, int n_images, int64_t per_image, cudaStream_t st);
+// tensor-core 3x3 convolution (cnn_tc.cu): same contract as launch_conv3x3 for
+// the shapes conv3x3_tc_supported accepts; FP16 operands, float32 accumulation
+// (pool: ReLU + 2x2 mean fused, y is then (n, cout, H/2, W/2))
+bool conv3x3_tc_supported(int cin, int cout, int H, int W);
+bool conv3x3_tc_pool_supported(int cin, int cout, int H, int W);
+cudaError_t launch_conv3x3_tc(const float* x, const float* w, const float* b, float* y, int n, int cin, int cout,
+                              int H, int W, int pool, int* status, cudaStream_t st);
 cudaError_t launch_conv3x3(const float* x, const float* w, const float* b, float* y, int Nn, int C, int K, int H,
                            int W, cudaStream_t st);
 cudaError_t launch_flip_weights(const float* w, int K, int C, float* wf, cudaStream_t st);

@@ -154,11 +154,20 @@ class BetaFocusNet:
             self._acts[n] = b
         return b
 
-    def forward(self, x):
+    @staticmethod
+    def tc_supported(cin: int, cout: int, h: int, w: int) -> bool:
+        """Shapes octgb_cnn_conv3x3_tc accepts."""
+        if not (1 <= cin <= 32 and 32 <= cout <= 128 and cout % 32 == 0):
+            return False
+        return w % 128 == 0 if w >= 128 else (128 % w == 0 and h % (128 // w) == 0)
+
+    def forward(self, x, tensor_cores: bool = False):
         """x: (n, in_ch, img, img) float32 CUDA tensor -> (n, 2) predictions (a
         view of an internal buffer, valid until the next call).  Runs on
         torch's current stream (see Context.follow_torch_stream), after the
-        work that produced x."""
+        work that produced x.  tensor_cores: the convolutions on the tensor
+        cores (FP16 operands, float32 accumulation) where the shape allows;
+        training keeps the float32 form its gradients are checked against."""
         self.ctx.follow_torch_stream()
         n = x.shape[0]
         b = self._buffers(n)
@@ -167,9 +176,17 @@ class BetaFocusNet:
         h = self.img
         for i, (cin, cout) in enumerate(zip(self.chans[:-1], self.chans[1:])):
             w, bias = self.params[2 * i], self.params[2 * i + 1]
-            self._check(self.lib.octgb_cnn_conv3x3(self.ctx.h, _p(cur), _p(w), _p(bias), _p(b["pre"][i]), n, cin,
-                                                   cout, h, h))
-            self._check(self.lib.octgb_cnn_relu_pool(self.ctx.h, _p(b["pre"][i]), _p(b["pooled"][i]), n * cout, h, h))
+            if tensor_cores and self.tc_supported(cin, cout, h, h) and h >= 128 and h % 2 == 0:
+                # convolution, ReLU and pooling in one kernel (no pre-activations)
+                self._check(self.lib.octgb_cnn_conv3x3_relu_pool_tc(self.ctx.h, _p(cur), _p(w), _p(bias),
+                                                                    _p(b["pooled"][i]), n, cin, cout, h, h))
+            else:
+                conv = self.lib.octgb_cnn_conv3x3
+                if tensor_cores and self.tc_supported(cin, cout, h, h):
+                    conv = self.lib.octgb_cnn_conv3x3_tc
+                self._check(conv(self.ctx.h, _p(cur), _p(w), _p(bias), _p(b["pre"][i]), n, cin, cout, h, h))
+                self._check(self.lib.octgb_cnn_relu_pool(self.ctx.h, _p(b["pre"][i]), _p(b["pooled"][i]), n * cout,
+                                                         h, h))
             cur = b["pooled"][i]
             h //= 2
         w1, b1, w2, b2 = self.params[8:12]
@@ -178,6 +195,12 @@ class BetaFocusNet:
         self._check(self.lib.octgb_cnn_dense(self.ctx.h, _p(b["h"]), _p(w2), _p(b2), _p(b["out"]), None, n,
                                              self.hidden, 2))
         return b["out"]
+
+    def predict(self, x):
+        """Inference: forward with the convolutions on the tensor cores (layers
+        of width >= 128 fused with their ReLU + pooling, so their
+        pre-activations are not kept: no backward after predict)."""
+        return self.forward(x, tensor_cores=True)
 
     def backward(self, dout):
         """Gradients of all parameters (self.grads) from d loss / d output."""

@@ -44,6 +44,59 @@ def test_conv_forward_ragged_shapes(torch_ctx):
         np.testing.assert_allclose(y.cpu().numpy(), ref, rtol=1e-4, atol=1e-4 * np.abs(ref).max())
 
 
+def _fp16(a):
+    return np.asarray(a, np.float32).astype(np.float16).astype(np.float64)
+
+
+def test_conv_tensor_cores_match_fp16_operands(torch_ctx):
+    """The tcgen05 convolution equals the float64 convolution of the
+    FP16-rounded operands (float32 accumulation: relative 1e-5), and the
+    float32 kernel within the operands' rounding, on every shape the network
+    uses and on ragged ones (edges, multi-row tiles, partial channel chunks)."""
+    torch, ctx = torch_ctx
+    from oct_recon_af_v1_gb300.learned import BetaFocusNet, _p
+    rng = np.random.default_rng(5)
+    for n, cin, cout, h, w in ((2, 3, 32, 256, 256), (2, 32, 32, 128, 128), (3, 32, 32, 64, 64),
+                               (3, 32, 32, 32, 32), (1, 11, 64, 16, 16), (2, 32, 96, 8, 384), (1, 1, 32, 128, 1)):
+        assert BetaFocusNet.tc_supported(cin, cout, h, w)
+        x = rng.standard_normal((n, cin, h, w)).astype(np.float32)
+        wt = (rng.standard_normal((cout, cin, 3, 3)) * 0.3).astype(np.float32)
+        b = rng.standard_normal(cout).astype(np.float32)
+        ref16 = C.conv3x3(_fp16(x), _fp16(wt), b.astype(np.float64))
+        xd, wd, bd = (torch.tensor(a, device="cuda") for a in (x, wt, b))
+        y = torch.empty((n, cout, h, w), dtype=torch.float32, device="cuda")
+        ctx._check(ctx.lib.octgb_cnn_conv3x3_tc(ctx.h, _p(xd), _p(wd), _p(bd), _p(y), n, cin, cout, h, w))
+        y32 = torch.empty_like(y)
+        ctx._check(ctx.lib.octgb_cnn_conv3x3(ctx.h, _p(xd), _p(wd), _p(bd), _p(y32), n, cin, cout, h, w))
+        ctx.synchronize()
+        got = y.cpu().numpy()
+        scale = np.abs(ref16).max()
+        np.testing.assert_allclose(got, ref16, rtol=0, atol=1e-5 * scale * np.sqrt(cin * 9))
+        assert np.abs(got - y32.cpu().numpy()).max() < 2e-3 * scale, (cin, cout, h, w)
+    from oct_recon_af_v1_gb300._lib import OctgbError
+    with pytest.raises(OctgbError):
+        ctx._check(ctx.lib.octgb_cnn_conv3x3_tc(ctx.h, _p(xd), _p(wd), _p(bd), _p(y), 1, 33, 32, 32, 32))
+
+
+def test_conv_relu_pool_tensor_cores(torch_ctx):
+    """The fused tensor-core convolution + ReLU + 2x2 mean equals the oracle's
+    ReLU-pool of the float64 convolution of the FP16-rounded operands."""
+    torch, ctx = torch_ctx
+    from oct_recon_af_v1_gb300.learned import _p
+    rng = np.random.default_rng(6)
+    for n, cin, cout, h, w in ((2, 3, 32, 256, 256), (2, 32, 32, 128, 128), (1, 5, 64, 6, 256)):
+        x = rng.standard_normal((n, cin, h, w)).astype(np.float32)
+        wt = (rng.standard_normal((cout, cin, 3, 3)) * 0.3).astype(np.float32)
+        b = rng.standard_normal(cout).astype(np.float32)
+        pre = C.conv3x3(_fp16(x), _fp16(wt), b.astype(np.float64))
+        ref = np.maximum(pre, 0).reshape(n, cout, h // 2, 2, w // 2, 2).mean(axis=(3, 5))
+        xd, wd, bd = (torch.tensor(a, device="cuda") for a in (x, wt, b))
+        p = torch.empty((n, cout, h // 2, w // 2), dtype=torch.float32, device="cuda")
+        ctx._check(ctx.lib.octgb_cnn_conv3x3_relu_pool_tc(ctx.h, _p(xd), _p(wd), _p(bd), _p(p), n, cin, cout, h, w))
+        ctx.synchronize()
+        np.testing.assert_allclose(p.cpu().numpy(), ref, rtol=0, atol=1e-5 * np.abs(pre).max() * np.sqrt(cin * 9))
+
+
 def test_network_gradients_match_oracle(torch_ctx):
     torch, ctx = torch_ctx
     from oct_recon_af_v1_gb300.learned import BetaFocusNet
@@ -181,7 +234,12 @@ def test_trained_network_gains_over_no_estimator(torch_ctx):
         ft = rng.uniform(100, 900, n_test)
         raw_t = S.u16_bits(S.generate(n_test, nx, 25, seed=999, device="cuda", beta_px=bpx, focus_px=ft,
                                       chunk=n_test, precision="float32"))
-        beta_l, focus_l = L.decode(net.forward(mk.images(raw_t, raw_dtype=U16)).cpu().numpy())
+        imgs_t = mk.images(raw_t, raw_dtype=U16)
+        pred32 = net.forward(imgs_t).cpu().numpy()
+        pred_tc = net.predict(imgs_t).cpu().numpy()
+        # the tensor-core forward (FP16 operands) stays close to the float32 one
+        assert np.abs(pred_tc - pred32).max() < 0.02 * max(1.0, np.abs(pred32).max()), np.abs(pred_tc - pred32).max()
+        beta_l, focus_l = L.decode(pred_tc)
         sc = DispersionScorer(lam, raw_t, "top_percentile", 25, rep=1, raw_dtype=U16)
         try:
             beta_s, grid, Sg = L.search_per_bscan(sc, -1.2 * L.beta_scale(), 1.2 * L.beta_scale(), 41)
