@@ -306,6 +306,9 @@ int octgb_batch_process(octgb_ctx *ctx, int n_tiles, const octgb_tile *tiles, in
 int octgb_disp_load(octgb_ctx *ctx, const void *raw, int raw_dtype, int raw_loc, int n_bscans, int rep, int interf,
                     int apod_size, const double *hann);
 /* dk2[j] = (k_eq[j] - mean(k_eq))^2, n doubles (dispersion.py:78-79). */
+/* The lines octgb_disp_load prepared: (n_bscans * rep, nX, n) float32, each
+ * float32(float64(linearised sample) * hann[j]). */
+int octgb_disp_lines(octgb_ctx *ctx, float *out, int out_loc);
 int octgb_disp_set_dk2(octgb_ctx *ctx, const double *dk2);
 /* Score n_beta candidate betas on loaded B-scans b0 .. b0+nb-1 in one launch
  * (DispersionScorer.magnitude + _metric, dispersion.py:46-63,91-107): phase
@@ -345,6 +348,13 @@ int octgb_xmean(octgb_ctx *ctx, const float *mag, int mag_loc, int n_frames, int
  * image over all its probes and pixels. */
 int octgb_cnn_images(octgb_ctx *ctx, const float *mag, int n_probe, int nb, int nx, int z_keep, float *img,
                      int normalise);
+/* The probe images straight from the loaded B-scans (octgb_disp_load): for
+ * each of the n_beta probe betas the dispersion kernel's |X| is pooled over
+ * depth inside the kernel (the magnitudes never reach memory), then over the
+ * A-scans, as octgb_cnn_images of octgb_disp_eval's magnitudes; img is a
+ * device buffer (nb, n_beta, 256, 256).  Asynchronous. */
+int octgb_disp_images(octgb_ctx *ctx, int n_beta, const double *betas, int b0, int nb, int z_keep, float *img,
+                      int normalise);
 /* y = conv3x3(x, w) + b, stride 1, zero padding 1: x (n, cin, h, w), w (cout, cin, 3, 3), b (cout) or NULL. */
 int octgb_cnn_conv3x3(octgb_ctx *ctx, const float *x, const float *w, const float *b, float *y, int n, int cin,
                       int cout, int h, int wd);

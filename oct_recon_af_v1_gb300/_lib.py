@@ -52,6 +52,7 @@ SIGNATURES = {
     "octgb_magnitude_noalloc": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_void_p]),
     "octgb_batch_process": (c_int, [c_void_p, c_int, c_void_p, c_int, c_float, c_int]),
     "octgb_disp_load": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_int, c_int, c_void_p]),
+    "octgb_disp_lines": (c_int, [c_void_p, c_void_p, c_int]),
     "octgb_disp_set_dk2": (c_int, [c_void_p, c_void_p]),
     "octgb_disp_eval": (c_int, [c_void_p, c_int, c_void_p, c_int, c_int, c_int, c_int64, c_int, c_void_p,
                                 c_void_p, c_int]),
@@ -70,6 +71,7 @@ SIGNATURES = {
                                        c_int, c_int, c_void_p, c_int, c_int]),
     "octgb_linearise_precision": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_int, c_void_p, c_int]),
     "octgb_magnitude_precision": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_int, c_void_p, c_int]),
+    "octgb_disp_images": (c_int, [c_void_p, c_int, c_void_p, c_int, c_int, c_int, c_void_p, c_int]),
     "octgb_cnn_images": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_int]),
     "octgb_cnn_conv3x3": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_int,
                                   c_int]),
@@ -347,6 +349,15 @@ class Context:
         h = np.ascontiguousarray(hann, dtype=np.float64)
         self._check(self.lib.octgb_disp_load(self.h, p, dt, loc, int(n_bscans), int(rep), interf, int(apod_size),
                                              h.ctypes.data))
+        self._disp_lines_shape = (B, interf - int(apod_size), self.n)
+
+    def disp_lines(self, out=None):
+        """The loaded, linearised and windowed lines (n_bscans * rep, nX, N) float32."""
+        if out is None:
+            out = np.empty((self._disp_lines_shape), np.float32)
+        p, loc = _ptr(out)
+        self._check(self.lib.octgb_disp_lines(self.h, p, loc))
+        return out
 
     def disp_set_dk2(self, dk2: np.ndarray):
         d = np.ascontiguousarray(dk2, dtype=np.float64)

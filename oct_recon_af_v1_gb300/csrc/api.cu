@@ -247,7 +247,8 @@ void validate_raw(const void* raw, int dtype, int loc, int B, int interf, int ap
 
 // Launch apod mean + fused spectral kernel over n_seg device batches (same B, interf, apod).
 void launch_spectral_segs(octgb_ctx* c, const void* const* segs, int n_seg, int dtype, int B, int interf, int apod,
-                          int mode, float* out_dev, int z0, int nz, unsigned int* mm_dev) {
+                          int mode, float* out_dev, int z0, int nz, unsigned int* mm_dev,
+                          const double* hann = nullptr, const float2* hann2 = nullptr) {
     if (B == 0 || n_seg == 0) return;
     ck(c->apod.ensure(static_cast<size_t>(n_seg) * B * kN * sizeof(float) + 16), "cudaMalloc(apod)");
     SpectralArgs a{};
@@ -272,6 +273,8 @@ void launch_spectral_segs(octgb_ctx* c, const void* const* segs, int n_seg, int 
     a.z0 = z0;
     a.nz = nz;
     a.minmax = mm_dev;
+    a.hann = hann;
+    a.hann2 = hann2;
     a.status = c->status_dev;
     ck(launch_apod_mean(a, dtype, c->stream), "apod kernel");
     c->launches++;
@@ -285,13 +288,14 @@ void launch_spectral_segs(octgb_ctx* c, const void* const* segs, int n_seg, int 
 
 // Run the spectral stage of a batch into `out` (device) in the given mode.
 void run_spectral(octgb_ctx* c, const void* raw, int dtype, int loc, int B, int interf, int apod, int mode,
-                  float* out_dev, int z0, int nz, unsigned int* mm_dev) {
+                  float* out_dev, int z0, int nz, unsigned int* mm_dev, const double* hann = nullptr,
+                  const float2* hann2 = nullptr) {
     if (!c->has_geom) throw Error(OCTGB_ERR_STATE, "octgb_set_geometry has not been called");
     if (c->cancel.load()) throw Error(OCTGB_ERR_CANCELLED, "cancelled");
     if (B == 0) return;  // empty batch: nothing to launch
     const size_t bytes = static_cast<size_t>(B) * interf * kN * raw_elem(dtype);
     const void* rd = stage_raw(c, raw, dtype, loc, bytes);
-    launch_spectral_segs(c, &rd, 1, dtype, B, interf, apod, mode, out_dev, z0, nz, mm_dev);
+    launch_spectral_segs(c, &rd, 1, dtype, B, interf, apod, mode, out_dev, z0, nz, mm_dev, hann, hann2);
 }
 
 void copy_out(octgb_ctx* c, void* dst, int loc, const void* src_dev, size_t bytes) {
@@ -1299,22 +1303,38 @@ int octgb_disp_load(octgb_ctx* c, const void* raw, int dtype, int loc, int n_bsc
         require(hann != nullptr, "hann is NULL");
         const int B = n_bscans * rep, nx = interf - apod;
         const size_t lines = static_cast<size_t>(B) * nx;
-        // linearised interferogram (window 1: the kernel's output is sum + m),
-        // then windowed in float64 and rounded once, as
-        // (eq * hann).astype(complex64) (dispersion.py:84)
-        ck(c->out.ensure(lines * kN * sizeof(float2)), "cudaMalloc(spec)");
-        run_spectral(c, raw, dtype, loc, B, interf, apod, kModeSpec, c->out.as<float>(), 0, 0, nullptr);
+        // linearised interferogram (window 1: the kernel's output is sum + m)
+        // windowed in float64 and rounded once, as (eq * hann).astype(complex64)
+        // (dispersion.py:84), written by the spectral kernel itself
         ck(c->disp_x.ensure(lines * kN * sizeof(float)), "cudaMalloc(X)");
-        ck(c->disp_hann.ensure(kN * sizeof(double)), "cudaMalloc(hann)");
-        ck(cudaMemcpyAsync(c->disp_hann.p, hann, kN * sizeof(double), cudaMemcpyHostToDevice, c->stream), "H2D hann");
-        ck(launch_window_pack(c->out.as<float2>(), c->disp_hann.as<double>(), static_cast<int64_t>(lines),
-                              c->disp_x.as<float>(), c->stream),
-           "window kernel");
-        c->launches++;
+        // the window in float64, and split hi + lo in float32 for the kernel's
+        // float32 form of the float64 product
+        std::vector<double> hw(kN * 2);
+        for (int j = 0; j < kN; ++j) {
+            const float hi = static_cast<float>(hann[j]);
+            reinterpret_cast<float*>(hw.data() + kN)[2 * j] = hi;
+            reinterpret_cast<float*>(hw.data() + kN)[2 * j + 1] = static_cast<float>(hann[j] - static_cast<double>(hi));
+            hw[j] = hann[j];
+        }
+        ck(c->disp_hann.ensure(kN * 2 * sizeof(double)), "cudaMalloc(hann)");
+        ck(cudaMemcpyAsync(c->disp_hann.p, hw.data(), hw.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream),
+           "H2D hann");
+        run_spectral(c, raw, dtype, loc, B, interf, apod, kModeLinHann, c->disp_x.as<float>(), 0, 0, nullptr,
+                     c->disp_hann.as<double>(), reinterpret_cast<const float2*>(c->disp_hann.as<double>() + kN));
         check_status(c);
         c->disp_b = n_bscans;
         c->disp_rep = rep;
         c->disp_nx = nx;
+    });
+}
+
+int octgb_disp_lines(octgb_ctx* c, float* out, int out_loc) {
+    return guarded(c, [&] {
+        require(c->disp_b > 0, "octgb_disp_load has not been called");
+        require(out != nullptr, "out is NULL");
+        copy_out(c, out, out_loc, c->disp_x.p,
+                 static_cast<size_t>(c->disp_b) * c->disp_rep * c->disp_nx * kN * sizeof(float));
+        check_status(c);
     });
 }
 
@@ -1324,6 +1344,20 @@ int octgb_disp_set_dk2(octgb_ctx* c, const double* dk2) {
         c->dk2.assign(dk2, dk2 + kN);
     });
 }
+
+namespace {
+// exp(-i beta dk^2) in float64, rounded to complex64 (dispersion.py:88-89), times 1/N
+void disp_phase_rows(const octgb_ctx* c, const double* betas, int n, float2* ph) {
+    for (int gi = 0; gi < n; ++gi) {
+        const double beta = betas[gi];
+        for (int j = 0; j < kN; ++j) {
+            const double t = beta * c->dk2[j];
+            ph[static_cast<size_t>(gi) * kN + j] = make_float2(static_cast<float>(std::cos(t)) * (1.0f / kN),
+                                                               static_cast<float>(-std::sin(t)) * (1.0f / kN));
+        }
+    }
+}
+}  // namespace
 
 int octgb_disp_eval(octgb_ctx* c, int n_beta, const double* betas, int b0, int nb, int metric, int64_t top_k,
                     int z_min, double* scores, float* mag, int mag_loc) {
@@ -1349,16 +1383,7 @@ int octgb_disp_eval(octgb_ctx* c, int n_beta, const double* betas, int b0, int n
         ck(c->disp_score.ensure(static_cast<size_t>(n_beta) * nb * sizeof(double)), "cudaMalloc(scores)");
         for (int g0 = 0; g0 < n_beta; g0 += per) {
             const int ng = std::min(per, n_beta - g0);
-            // exp(-i beta dk^2) in float64, rounded to complex64 (dispersion.py:88-89), times 1/N
-            for (int gi = 0; gi < ng; ++gi) {
-                const double beta = betas[g0 + gi];
-                for (int j = 0; j < kN; ++j) {
-                    const double t = beta * c->dk2[j];
-                    ph[static_cast<size_t>(gi) * kN + j] =
-                        make_float2(static_cast<float>(std::cos(t)) * (1.0f / kN),
-                                    static_cast<float>(-std::sin(t)) * (1.0f / kN));
-                }
-            }
+            disp_phase_rows(c, betas + g0, ng, ph.data());
             ck(c->disp_phase.ensure(static_cast<size_t>(per) * kN * sizeof(float2)), "cudaMalloc(phase)");
             ck(cudaMemcpyAsync(c->disp_phase.p, ph.data(), static_cast<size_t>(ng) * kN * sizeof(float2),
                                cudaMemcpyHostToDevice, c->stream),
@@ -1764,6 +1789,46 @@ int octgb_magnitude_precision(octgb_ctx* c, const void* raw, int dtype, int loc,
 // ---------------------------------------------------------------------------
 // Learned beta/focus estimator: device pointers only, asynchronous on the
 // context's stream (no counterpart in the reference).
+
+int octgb_disp_images(octgb_ctx* c, int n_beta, const double* betas, int b0, int nb, int z_keep, float* img,
+                      int normalise) {
+    return guarded(c, [&] {
+        require(c->disp_b > 0, "octgb_disp_load has not been called");
+        require(static_cast<int>(c->dk2.size()) == kN, "octgb_disp_set_dk2 has not been called");
+        require(n_beta >= 1 && betas != nullptr, "no betas");
+        require(b0 >= 0 && nb >= 1 && b0 + nb <= c->disp_b, "B-scan range outside the loaded B-scans");
+        require(z_keep >= 1 && z_keep <= kHalf, "z_keep must be in [1, N/2]");
+        require(img != nullptr, "img is NULL");
+        if (c->cancel.load()) throw Error(OCTGB_ERR_CANCELLED, "cancelled");
+        const int nx = c->disp_nx;
+        std::vector<float2> ph(static_cast<size_t>(n_beta) * kN);
+        disp_phase_rows(c, betas, n_beta, ph.data());
+        ck(c->disp_phase.ensure(ph.size() * sizeof(float2)), "cudaMalloc(phase)");
+        ck(cudaMemcpyAsync(c->disp_phase.p, ph.data(), ph.size() * sizeof(float2), cudaMemcpyHostToDevice, c->stream),
+           "H2D phase");
+        const size_t cols = static_cast<size_t>(n_beta) * nb * nx * 256;
+        ck(c->disp_a.ensure(cols * sizeof(float)), "cudaMalloc(columns)");
+        DispArgs a{};
+        a.X = c->disp_x.as<float>();
+        a.phase = c->disp_phase.as<float2>();
+        a.tw = c->tw.as<float2>();
+        a.A = nullptr;
+        a.zcol = c->disp_a.as<float>();
+        a.z_keep = z_keep;
+        a.n_beta = n_beta;
+        a.nb = nb;
+        a.b0 = b0;
+        a.nx = nx;
+        a.rep = c->disp_rep;
+        ck(launch_disp_mag(a, c->num_sms, c->stream), "dispersion magnitude kernel");
+        ck(launch_image_cols(a.zcol, n_beta, nb, nx, z_keep, img, c->stream), "image column kernel");
+        c->launches += 2;
+        if (normalise) {
+            ck(launch_image_norm(img, nb, static_cast<int64_t>(n_beta) * 256 * 256, c->stream), "image norm kernel");
+            c->launches++;
+        }
+    });
+}
 
 int octgb_cnn_images(octgb_ctx* c, const float* mag, int n_probe, int nb, int nx, int z_keep, float* img,
                      int normalise) {

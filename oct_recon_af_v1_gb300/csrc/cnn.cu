@@ -7,6 +7,8 @@
 //                   20 log10 of the area mean over z < z_keep (adaptive
 //                   average pooling, the block-average of estimation/
 //                   preview.py:49-53 with fractional edges)
+//   k_image_cols    the same images from the dispersion kernel's depth-pooled
+//                   column sums (the magnitudes never reach memory)
 //   k_image_norm    per image: (v - mean) / std over all its probes and pixels
 //   k_conv3x3       3x3 convolution, stride 1, zero padding 1, + bias: a CTA
 //                   computes a 16x16 pixel tile of 16 output channels, input
@@ -50,14 +52,61 @@ __global__ void k_image_pool(const float* __restrict__ A, int n_probe, int nb, i
     }
 }
 
+// k_image_pool from depth-pooled column sums zcol (probes, B, nx, 256): the
+// sum over the row's A-scans, divided by the window's element count.  A CTA
+// makes 32 image rows of one (B-scan, probe) image, 32 columns at a time: the
+// column sums of the A-scans those columns cover are staged in shared memory
+// (rows of 32 depths, read along depth), summed per pixel and written along
+// the image row.
+constexpr int kColTile = 32;
+__global__ void __launch_bounds__(256) k_image_cols(const float* __restrict__ zcol, int n_probe, int nb, int nx,
+                                                     int z_keep, float* __restrict__ img) {
+    extern __shared__ float T[];                         // [A-scans of the chunk][kColTile + 1]
+    const int zb = blockIdx.x * kColTile;
+    const int p = blockIdx.y % n_probe, b = blockIdx.y / n_probe;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const float* c = zcol + (static_cast<int64_t>(p) * nb + b) * nx * kImg + zb;
+    float* out = img + ((static_cast<int64_t>(b) * n_probe + p) * kImg + zb) * kImg;
+    for (int xc = 0; xc < kImg; xc += kColTile) {
+        const int xa = xc * nx / kImg, xe = ((xc + kColTile) * nx + kImg - 1) / kImg;
+        for (int x = xa + warp; x < xe; x += 8) T[(x - xa) * (kColTile + 1) + lane] = c[static_cast<int64_t>(x) * kImg + lane];
+        __syncthreads();
+        const int xi = xc + lane;
+        const int x0 = xi * nx / kImg, x1 = ((xi + 1) * nx + kImg - 1) / kImg;
+        for (int zl = warp; zl < kColTile; zl += 8) {
+            const int zi = zb + zl;
+            const int z0 = zi * z_keep / kImg, z1 = ((zi + 1) * z_keep + kImg - 1) / kImg;
+            float sum = 0.f;
+            for (int x = x0; x < x1; ++x) sum += T[(x - xa) * (kColTile + 1) + zl];
+            const float m = sum / static_cast<float>((x1 - x0) * (z1 - z0));
+            out[static_cast<int64_t>(zl) * kImg + xi] = 20.0f * log10f(fmaxf(m, 1e-30f));
+        }
+        __syncthreads();
+    }
+}
+
+// Sums in float64 of float32 partial sums over 16 pixels (four float4 loads),
+// so the FP64 pipe sees a quarter of an operation per pixel; per_image is a
+// multiple of 4 (probes x 256 x 256).
 __global__ void __launch_bounds__(1024) k_image_norm(float* __restrict__ img, int64_t per_image) {
     __shared__ double red[32];
     float* v = img + blockIdx.x * per_image;
+    const float4* v4 = reinterpret_cast<const float4*>(v);
+    const int64_t n4 = per_image / 4;
     double s = 0.0, s2 = 0.0;
-    for (int64_t i = threadIdx.x; i < per_image; i += blockDim.x) {
-        const double t = v[i];
-        s += t;
-        s2 += t * t;
+    for (int64_t i0 = threadIdx.x; i0 < n4; i0 += 4 * static_cast<int64_t>(blockDim.x)) {
+        float fs = 0.f, fs2 = 0.f;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int64_t i = i0 + u * static_cast<int64_t>(blockDim.x);
+            if (i < n4) {
+                const float4 q = v4[i];
+                fs += (q.x + q.y) + (q.z + q.w);
+                fs2 += fmaf(q.x, q.x, q.y * q.y) + fmaf(q.z, q.z, q.w * q.w);
+            }
+        }
+        s += static_cast<double>(fs);
+        s2 += static_cast<double>(fs2);
     }
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     for (int o = 16; o > 0; o >>= 1) {
@@ -87,7 +136,11 @@ __global__ void __launch_bounds__(1024) k_image_norm(float* __restrict__ img, in
     const double var = red2[0] / per_image - mean * mean;
     const float inv = static_cast<float>(1.0 / sqrt(var > 1e-12 ? var : 1e-12));
     const float mf = static_cast<float>(mean);
-    for (int64_t i = threadIdx.x; i < per_image; i += blockDim.x) v[i] = (v[i] - mf) * inv;
+    float4* w4 = reinterpret_cast<float4*>(v);
+    for (int64_t i = threadIdx.x; i < n4; i += blockDim.x) {
+        const float4 q = w4[i];
+        w4[i] = make_float4((q.x - mf) * inv, (q.y - mf) * inv, (q.z - mf) * inv, (q.w - mf) * inv);
+    }
 }
 
 // ---------------------------------------------------------------- convolution
@@ -353,6 +406,15 @@ int grid_for(int64_t n, int threads, int cap = 1 << 20) {
 cudaError_t launch_image_pool(const float* A, int n_probe, int nb, int nx, int z_keep, float* img, cudaStream_t st) {
     k_image_pool<<<grid_for(static_cast<int64_t>(nb) * n_probe * kImg * kImg, 256, 65536), 256, 0, st>>>(
         A, n_probe, nb, nx, z_keep, img);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_image_cols(const float* zcol, int n_probe, int nb, int nx, int z_keep, float* img,
+                              cudaStream_t st) {
+    // A-scans of a 32-column chunk: at most 32 nx / 256 + 2
+    const size_t smem = static_cast<size_t>(kColTile * nx / kImg + 2) * (kColTile + 1) * sizeof(float);
+    if (smem > 48 * 1024 || static_cast<int64_t>(nb) * n_probe > 65535) return cudaErrorInvalidValue;
+    k_image_cols<<<dim3(kImg / kColTile, nb * n_probe), 256, smem, st>>>(zcol, n_probe, nb, nx, z_keep, img);
     return cudaGetLastError();
 }
 

@@ -83,6 +83,25 @@ __global__ void __launch_bounds__(kThreads, 2) k_disp_mag(const DispArgs a) {
 #pragma unroll
                 for (int r = 0; r < 4; ++r) acc[h][r] += mag[h][r];
         }
+        if (a.zcol != nullptr) {
+            // probe images: |X| into the group's (now free) line, then per image
+            // row zi the sum over depths [zi z_keep / 256, ceil((zi + 1) z_keep / 256))
+            float* M = reinterpret_cast<float*>(S.spec[g]);
+            group_sync(g);                              // every thread has read the line's last stage
+#pragma unroll
+            for (int h = 0; h < 2; ++h)
+#pragma unroll
+                for (int r = 0; r < 4; ++r)
+                    M[lt + 128 * h + 256 * r] = a.rep == 1 ? acc[h][r] : __fdiv_rn(acc[h][r], static_cast<float>(a.rep));
+            group_sync(g);
+            for (int zi = lt; zi < 256; zi += kGroup) {
+                const int z0 = zi * a.z_keep / 256, z1 = ((zi + 1) * a.z_keep + 255) / 256;
+                float sum = 0.f;
+                for (int z = z0; z < z1; ++z) sum += M[z];
+                a.zcol[item * 256 + zi] = sum;
+            }
+            continue;                                   // the next transform writes the line after a group barrier
+        }
         float* out = a.A + item * kHalf;
 #pragma unroll
         for (int h = 0; h < 2; ++h)
@@ -370,22 +389,7 @@ __global__ void __launch_bounds__(kMedCols * 32) k_xmedian(const float* __restri
     }
 }
 
-__global__ void k_window_pack(const float2* __restrict__ spec, const double* __restrict__ hann, int64_t n,
-                              float* __restrict__ X) {
-    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
-         i += static_cast<int64_t>(gridDim.x) * blockDim.x)
-        X[i] = static_cast<float>(static_cast<double>(spec[i].x) * hann[i % kN]);
-}
-
 }  // namespace
-
-cudaError_t launch_window_pack(const float2* spec, const double* hann, int64_t lines, float* X, cudaStream_t st) {
-    const int64_t n = lines * kN;
-    int64_t grid = (n + 255) / 256;
-    if (grid > 4096) grid = 4096;
-    k_window_pack<<<static_cast<int>(grid), 256, 0, st>>>(spec, hann, n, X);
-    return cudaGetLastError();
-}
 
 cudaError_t launch_disp_mag(const DispArgs& a, int num_sms, cudaStream_t st) {
     const size_t smem = sizeof(DispSmem);

@@ -18,7 +18,9 @@ constexpr int kThreads = kGroup * kPerCta;
 constexpr int kStatusOk = 0;
 constexpr int kStatusTimeout = 1;
 
-enum OutMode : int { kModeSpec = 0, kModeMag = 1, kModeDb = 2, kModeResample = 3 };
+// kModeLinHann: the real linearised line times a float64 window, rounded once
+// to float32 (the scorer's input, (eq * hann).astype(complex64) with a window of ones)
+enum OutMode : int { kModeSpec = 0, kModeMag = 1, kModeDb = 2, kModeResample = 3, kModeLinHann = 4 };
 
 constexpr int kBlk = 32;          // output rows / columns per stitch block
 constexpr int kMaxSeg = 32;       // tiles per multi-tile launch
@@ -59,7 +61,9 @@ struct SpectralArgs {
     int64_t n_ascans;         // n_seg * B * nx
     const float* apod_mean;   // (n_seg * B, kN) float32 apodisation mean
     DevGeometry g;
-    float* out;               // spec (M, kN, 2) | mag (M, kHalf) | db (M, nz)
+    float* out;               // spec (M, kN, 2) | mag (M, kHalf) | db (M, nz) | windowed line (M, kN)
+    const double* hann;       // kModeLinHann: the float64 window (kN)
+    const float2* hann2;      // kModeLinHann: the window split hi + lo in float32 (kN)
     int z0, nz;               // depth crop (db mode)
     unsigned int* minmax;     // [2] ordered-uint min / max (db / resample modes), may be null
     int* status;              // device status word
@@ -142,12 +146,12 @@ struct DispArgs {
     const float* X;        // (B, rep, nx, kN) linearised, windowed, real
     const float2* phase;   // (n_beta, kN) exp(-i beta dk^2) / N
     const float2* tw;      // (kN) e^(2 pi i k / N)
-    float* A;              // (n_beta, nb, nx, kHalf)
+    float* A;              // (n_beta, nb, nx, kHalf), or null with zcol
+    float* zcol;           // (n_beta, nb, nx, 256) depth-pooled sums of |X| (probe images), or null
+    int z_keep;            // depths pooled into the 256 image rows
     int n_beta, nb, b0, nx, rep;
 };
 cudaError_t launch_disp_mag(const DispArgs& a, int num_sms, cudaStream_t st);
-// X[l][j] = float32(float64(spec[l][j].re) * hann[j]) over `lines` lines of kN
-cudaError_t launch_window_pack(const float2* spec, const double* hann, int64_t lines, float* X, cudaStream_t st);
 // per segment (n_seg rows of nx x kHalf magnitudes): metric 1 top_percentile
 // (top_k elements), 2 kurtosis, 3 entropy, 4 legacy_peak, depths >= z_min
 cudaError_t launch_disp_metric(const float* A, int n_seg, int nx, int z_min, int metric, unsigned int top_k,
@@ -210,6 +214,9 @@ size_t prec_smem_bytes();
 
 // learned beta/focus estimator (cnn.cu)
 cudaError_t launch_image_pool(const float* A, int n_probe, int nb, int nx, int z_keep, float* img, cudaStream_t st);
+// the same images from k_disp_mag's depth-pooled column sums (n_probe, nb, nx, 256)
+cudaError_t launch_image_cols(const float* zcol, int n_probe, int nb, int nx, int z_keep, float* img,
+                              cudaStream_t st);
 cudaError_t launch_image_norm(float* img, int n_images, int64_t per_image, cudaStream_t st);
 // tensor-core 3x3 convolution (cnn_tc.cu): same contract as launch_conv3x3 for
 // the shapes conv3x3_tc_supported accepts; FP16 operands, float32 accumulation

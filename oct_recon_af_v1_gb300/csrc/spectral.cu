@@ -63,6 +63,29 @@ constexpr int kDLine = kN + kTail;                        // d line incl. zero t
 constexpr int kDSkew = kDLine + kDLine / 32 + 4;           // skewed length (+1 word per 32)
 __device__ __forceinline__ int skew(int w) { return w + (w >> 5); }
 
+// float32(float64(x) * h) for a float64 h given as float32 hi + lo (h2.x +
+// h2.y, the rest below 2^-48 |h|) without the FP64 pipe: p + e1 = x * hi
+// exactly (fma), q = x lo + e1 (one rounding), o = p + q rounded once.  The
+// exact product differs from p + q by < 2^-46 |o|; when p + q lies more than
+// 2^-40 |o| from a float32 rounding boundary (r = (p + q) - o exactly, by
+// Fast2Sum), both the product and its float64 rounding round to o.  Otherwise
+// (about one sample in 65 000), and for powers of two (asymmetric boundaries)
+// and tiny values, the float64 product is formed as the reference does.
+// The caller forms the float64 product for the lanes whose `safe` is false,
+// behind a warp vote, so the FP64 pipe only runs in the rare warps that need it.
+__device__ __forceinline__ float mul_window(float x, float2 h2, bool& safe) {
+    const float p = x * h2.x;
+    const float e1 = fmaf(x, h2.x, -p);
+    const float q = fmaf(x, h2.y, e1);
+    const float o = p + q;
+    const float r = q - (o - p);
+    const float ao = fabsf(o);
+    const int bits = __float_as_int(ao);
+    const float half_ulp = __int_as_float((bits & 0x7f800000) - (24 << 23));
+    safe = ao > 1e-30f && (bits & 0x007fffff) != 0 && fabsf(fabsf(r) - half_ulp) > ao * 9.094947e-13f;
+    return o;
+}
+
 template <typename RawT>
 struct Smem {
     uint64_t bar[2];
@@ -299,6 +322,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
                 float win[U];
 #pragma unroll
                 for (int u = 0; u < U; ++u) win[u] = S.d[k][skew(s0 + u)];
+                float lh[4], lx[4];
+                bool lsafe[4];
 #pragma unroll
                 for (int r = 0; r < 4; ++r) {
                     float acc = 0.f;
@@ -306,7 +331,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
                     for (int u = 0; u < U; ++u) acc = fmaf(wr[r][u], win[u], acc);
                     const float v = acc + mk;
                     const float2 sp = make_float2(v * wre[r], v * wim[r]);
-                    if (Mode == kModeSpec) {
+                    if (Mode == kModeLinHann) {
+                        // the real part of the spec output (1/N undone) times the
+                        // float64 window, one rounding to float32
+                        lx[r] = sp.x * kN;
+                        lh[r] = mul_window(lx[r], __ldg(a.hann2 + i0 + r), lsafe[r]);
+                    } else if (Mode == kModeSpec) {
                         // spec output undoes the 1/N ifft scaling folded into the window
                         if (a0 + k < a.n_ascans)
                             reinterpret_cast<float2*>(a.out)[(a0 + k) * kN + i0 + r] =
@@ -315,10 +345,21 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
                         S.spec[k][pad(i0 + r)] = sp;
                     }
                 }
+                if (Mode == kModeLinHann) {
+                    const bool all_safe = lsafe[0] && lsafe[1] && lsafe[2] && lsafe[3];
+                    if (__any_sync(0xffffffffu, !all_safe)) {
+#pragma unroll
+                        for (int r = 0; r < 4; ++r)
+                            if (!lsafe[r])
+                                lh[r] = static_cast<float>(static_cast<double>(lx[r]) * __ldg(a.hann + i0 + r));
+                    }
+                    if (a0 + k < a.n_ascans)
+                        *reinterpret_cast<float4*>(a.out + (a0 + k) * kN + i0) = make_float4(lh[0], lh[1], lh[2], lh[3]);
+                }
             }
         }
         __syncthreads();
-        if (Mode == kModeSpec) continue;
+        if (Mode == kModeSpec || Mode == kModeLinHann) continue;
 
         // ---- (e)+(f) inverse FFT, group g on its own line; |X[k]|, k < N/2 ----
         float2* X = S.spec[g];
@@ -506,6 +547,7 @@ cudaError_t launch_mode(const SpectralArgs& a, int mode, int grid, cudaStream_t 
         case kModeSpec: return launch_u<RawT, kModeSpec>(a, grid, st);
         case kModeMag: return launch_u<RawT, kModeMag>(a, grid, st);
         case kModeResample: return launch_u<RawT, kModeResample>(a, grid, st);
+        case kModeLinHann: return launch_u<RawT, kModeLinHann>(a, grid, st);
         default: return launch_u<RawT, kModeDb>(a, grid, st);
     }
 }

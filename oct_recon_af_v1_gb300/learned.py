@@ -86,11 +86,11 @@ class ImageMaker:
         torch = self.torch
         self.ctx.follow_torch_stream()
         P = len(self.probes)
-        mag = torch.empty((P, self.B, self.nx, self.n // 2), dtype=torch.float32, device=self.device)
-        self.ctx.disp_eval(self.probes - float(beta_shift), 0, self.B, 0, mag=mag)
         if out is None:
             out = torch.empty((self.B, P, IMG, IMG), dtype=torch.float32, device=self.device)
-        self.ctx._check(self.ctx.lib.octgb_cnn_images(self.ctx.h, _p(mag), P, self.B, self.nx, Z_KEEP, _p(out), 1))
+        betas = np.ascontiguousarray(self.probes - float(beta_shift), dtype=np.float64)
+        self.ctx._check(self.ctx.lib.octgb_disp_images(self.ctx.h, P, betas.ctypes.data, 0, self.B, Z_KEEP, _p(out),
+                                                       1))
         return out
 
     def images(self, raw, out=None, raw_dtype=None):

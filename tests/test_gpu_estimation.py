@@ -166,3 +166,30 @@ def test_plugin_detect_focus_matches_reference(built, volume):
     for m, r in zip(foc["drift"]["measurements"], ref["drift"]["measurements"]):
         p, q = np.asarray(m["profile"], float), np.asarray(r["profile"], float)
         assert np.nanmax(np.abs(p - q) / np.nanmax(np.abs(q))) < 1e-5
+
+
+def test_windowed_lines_bit_exact(built):
+    """The scorer's windowed lines equal float32(float64(linearised line) *
+    hann) bit for bit (dispersion.py:84): the kernel's float32 form of the
+    float64 product, with its float64 fallback near rounding boundaries, on
+    lines whose samples span many binades (so both paths are exercised)."""
+    from oct_recon_af_v1_gb300 import estimation as E
+    from oct_recon_af_v1_gb300 import geometry as G
+    from oct_recon_af_v1_gb300 import synthetic as S
+    from oct_recon_af_v1_gb300._lib import Context
+    lam = S.lambda_nm()
+    sg = G.build_spectral_geometry(lam, 0.0, 1.33)
+    ctx = Context(0)
+    try:
+        ctx.set_geometry(sg.sinc_idx, sg.sinc_w, np.ones(len(lam), np.complex128))
+        rng = np.random.default_rng(17)
+        raw = (rng.integers(0, 60000, size=(6, 25 + 40, 2048)) >> rng.integers(0, 14, size=(6, 65, 1))).astype(np.uint16)
+        hann = E.hann_rms(len(lam))
+        ctx.disp_load(raw, 25, 6, 1, hann, raw_dtype=0)
+        got = ctx.disp_lines()
+        lin = ctx.fused_pre_fft(raw, 25, raw_dtype=0)          # window of ones: the linearised line
+        ref = (lin.real.astype(np.float64) * hann).astype(np.float32)
+        assert got.dtype == np.float32 and got.shape == ref.shape
+        np.testing.assert_array_equal(got.view(np.int32), ref.view(np.int32))
+    finally:
+        ctx.close()
