@@ -157,7 +157,7 @@ struct octgb_ctx {
     // legacy TIFF encoding
     DevBuf enc_bits, enc_lut, enc_slots, enc_sizes;
     // rare raw formats: prepared batch, frame-mean lines, per-file magnitudes
-    DevBuf prep, prep_apod, magrep, srr;
+    DevBuf prep, prep_apod, magrep, srr, gemm_part;
     // precision form (tensor-core sinc)
     bool prec_ok = false;
     DevBuf prec_w, prec_kb, prec_hi, prec_lo, prec_m, prec_x;
@@ -476,7 +476,7 @@ int octgb_destroy(octgb_ctx* c) {
                       &c->den, &c->plan_table, &c->run_mm, &c->magbuf, &c->dbbuf, &c->planemm, &c->segs, &c->qtable,
                       &c->qcounter, &c->disp_x, &c->disp_hann, &c->disp_phase, &c->disp_a, &c->disp_score, &c->xmed,
                       &c->prec_w, &c->prec_kb, &c->prec_hi, &c->prec_lo, &c->prec_m, &c->prec_x, &c->prep,
-                      &c->prep_apod, &c->magrep, &c->srr, &c->enc_bits, &c->enc_lut, &c->enc_slots, &c->enc_sizes})
+                      &c->prep_apod, &c->magrep, &c->srr, &c->gemm_part, &c->enc_bits, &c->enc_lut, &c->enc_slots, &c->enc_sizes})
         b->release();
     for (QTable* t : c->qtables) {
         t->buf.release();
@@ -1193,7 +1193,7 @@ int octgb_graph_end(octgb_ctx* c, int* graph_id) {
                           &c->run_mm, &c->magbuf, &c->dbbuf, &c->planemm, &c->segs, &c->qtable, &c->qcounter,
                           &c->disp_x, &c->disp_hann, &c->disp_phase, &c->disp_a, &c->disp_score, &c->xmed,
                           &c->prec_hi, &c->prec_lo, &c->prec_m, &c->prec_x, &c->prep, &c->prep_apod,
-                          &c->magrep, &c->srr, &c->enc_bits, &c->enc_lut, &c->enc_slots, &c->enc_sizes})
+                          &c->magrep, &c->srr, &c->gemm_part, &c->enc_bits, &c->enc_lut, &c->enc_slots, &c->enc_sizes})
             b->keep_old = true;
         for (int k = 0; k < octgb_ctx::kRing; ++k) c->ring[k].keep_old = true;
         c->launches.store(c->capture_launch0);
@@ -1918,9 +1918,13 @@ int octgb_cnn_dense(octgb_ctx* c, const float* x, const float* w, const float* b
                     int in, int out) {
     return guarded(c, [&] {
         require(x && w && b && pre && m >= 1 && in >= 1 && out >= 1, "bad dense shape");
-        ck(launch_gemm(x, in, 1, w, 1, in, pre, out, m, out, in, 0, c->stream), "gemm kernel");
+        // few output tiles over a long K (the flattened features): split K across the SMs
+        const int S = gemm_splits(m, out, in, c->num_sms);
+        if (S > 1) ck(c->gemm_part.ensure(static_cast<size_t>(S) * m * out * sizeof(float)), "cudaMalloc(gemm)");
+        ck(launch_gemm_split(x, in, 1, w, 1, in, pre, out, m, out, in, 0, S, c->gemm_part.as<float>(), c->stream),
+           "gemm kernel");
         ck(launch_bias_relu(pre, b, m, out, act, c->stream), "bias kernel");
-        c->launches += 2;
+        c->launches += S > 1 ? 3 : 2;
     });
 }
 

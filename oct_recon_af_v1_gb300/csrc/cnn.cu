@@ -282,21 +282,28 @@ __global__ void k_relu_pool_bwd(const float* __restrict__ dp, const float* __res
 // ---------------------------------------------------------------- dense layers
 constexpr int kGT = 64, kGK = 16;
 
-// C[i][j] (+)= sum_k A(i,k) B(k,j), A(i,k) = A[i*sa0 + k*sa1], B(k,j) = B[k*sb0 + j*sb1]
+// C[i][j] (+)= sum_k A(i,k) B(k,j), A(i,k) = A[i*sa0 + k*sa1], B(k,j) = B[k*sb0 + j*sb1].
+// Split K: blockIdx.z takes k in [z k_chunk, (z + 1) k_chunk) and writes its
+// partial product to the slice Cm + z M ldc (k_sum_splits adds the slices in
+// order).  Tiles are loaded along whichever index is contiguous in memory.
 __global__ void __launch_bounds__(256) k_gemm(const float* __restrict__ A, int64_t sa0, int64_t sa1,
                                               const float* __restrict__ B, int64_t sb0, int64_t sb1,
                                               float* __restrict__ Cm, int64_t ldc, int M, int N, int Kd,
-                                              int accumulate) {
+                                              int accumulate, int k_chunk) {
     __shared__ float as[kGK][kGT + 4];
     __shared__ float bs[kGK][kGT + 4];
     const int i0 = blockIdx.y * kGT, j0 = blockIdx.x * kGT;
     const int ti = threadIdx.x / 16, tj = threadIdx.x % 16;
+    const int kb = blockIdx.z * k_chunk, ke = min(Kd, kb + k_chunk);
+    Cm += static_cast<int64_t>(blockIdx.z) * M * ldc;
+    const bool a_kfast = sa1 == 1, b_kfast = sb0 == 1;
     float acc[4][4] = {};
-    for (int k0 = 0; k0 < Kd; k0 += kGK) {
+    for (int k0 = kb; k0 < ke; k0 += kGK) {
         for (int e = threadIdx.x; e < kGK * kGT; e += 256) {
-            const int kk = e / kGT, r = e % kGT;
-            as[kk][r] = (i0 + r < M && k0 + kk < Kd) ? A[(i0 + r) * sa0 + (k0 + kk) * sa1] : 0.f;
-            bs[kk][r] = (j0 + r < N && k0 + kk < Kd) ? B[(k0 + kk) * sb0 + (j0 + r) * sb1] : 0.f;
+            const int kk = a_kfast ? e % kGK : e / kGT, r = a_kfast ? e / kGK : e % kGT;
+            as[kk][r] = (i0 + r < M && k0 + kk < ke) ? A[(i0 + r) * sa0 + (k0 + kk) * sa1] : 0.f;
+            const int kk2 = b_kfast ? e % kGK : e / kGT, r2 = b_kfast ? e / kGK : e % kGT;
+            bs[kk2][r2] = (j0 + r2 < N && k0 + kk2 < ke) ? B[(k0 + kk2) * sb0 + (j0 + r2) * sb1] : 0.f;
         }
         __syncthreads();
 #pragma unroll
@@ -324,6 +331,17 @@ __global__ void __launch_bounds__(256) k_gemm(const float* __restrict__ A, int64
                 *c = accumulate ? *c + acc[u][v] : acc[u][v];
             }
         }
+}
+
+// C[i][j] (+)= sum over s in order of P[s][i][j] (the split-K slices)
+__global__ void k_sum_splits(const float* __restrict__ P, int S, int M, int N, float* __restrict__ Cm, int64_t ldc,
+                             int accumulate) {
+    const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    if (i >= static_cast<int64_t>(M) * N) return;
+    float v = P[i];
+    for (int s = 1; s < S; ++s) v += P[static_cast<int64_t>(s) * M * N + i];
+    float* c = Cm + (i / N) * ldc + i % N;
+    *c = accumulate ? *c + v : v;
 }
 
 // y[i][j] += b[j]; out = relu(y) (out may be NULL)
@@ -460,7 +478,29 @@ cudaError_t launch_relu_pool_bwd(const float* dp, const float* y, int64_t nk, in
 cudaError_t launch_gemm(const float* A, int64_t sa0, int64_t sa1, const float* B, int64_t sb0, int64_t sb1, float* C,
                         int64_t ldc, int M, int N, int K, int accumulate, cudaStream_t st) {
     dim3 grid((N + kGT - 1) / kGT, (M + kGT - 1) / kGT);
-    k_gemm<<<grid, 256, 0, st>>>(A, sa0, sa1, B, sb0, sb1, C, ldc, M, N, K, accumulate);
+    k_gemm<<<grid, 256, 0, st>>>(A, sa0, sa1, B, sb0, sb1, C, ldc, M, N, K, accumulate, K);
+    return cudaGetLastError();
+}
+
+int gemm_splits(int M, int N, int K, int num_sms) {
+    const int tiles = ((N + kGT - 1) / kGT) * ((M + kGT - 1) / kGT);
+    int S = (2 * num_sms + tiles - 1) / tiles;
+    const int max_s = K / 256;                       // at least 256 of K per slice
+    S = S < max_s ? S : max_s;
+    return S < 1 ? 1 : S;
+}
+
+cudaError_t launch_gemm_split(const float* A, int64_t sa0, int64_t sa1, const float* B, int64_t sb0, int64_t sb1,
+                              float* C, int64_t ldc, int M, int N, int K, int accumulate, int S, float* partial,
+                              cudaStream_t st) {
+    if (S <= 1) return launch_gemm(A, sa0, sa1, B, sb0, sb1, C, ldc, M, N, K, accumulate, st);
+    const int chunk = ((K + S - 1) / S + kGK - 1) / kGK * kGK;
+    S = (K + chunk - 1) / chunk;
+    dim3 grid((N + kGT - 1) / kGT, (M + kGT - 1) / kGT, S);
+    k_gemm<<<grid, 256, 0, st>>>(A, sa0, sa1, B, sb0, sb1, partial, N, M, N, K, 0, chunk);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_sum_splits<<<grid_for(static_cast<int64_t>(M) * N, 256), 256, 0, st>>>(partial, S, M, N, C, ldc, accumulate);
     return cudaGetLastError();
 }
 

@@ -101,7 +101,7 @@ __device__ __forceinline__ void unit_tile(const ConvGeom& g, int64_t u, int h, i
     }
 }
 
-__global__ void __launch_bounds__(kCThreads, 2)
+__global__ void __launch_bounds__(kCThreads, 4)
     k_conv3x3_tc(const float* __restrict__ x, const float* __restrict__ w, const float* __restrict__ bias,
                  float* __restrict__ y, const ConvGeom g, int* status) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];

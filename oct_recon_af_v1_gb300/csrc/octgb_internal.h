@@ -235,6 +235,11 @@ cudaError_t launch_relu_pool_bwd(const float* dp, const float* y, int64_t nk, in
                                  cudaStream_t st);
 cudaError_t launch_gemm(const float* A, int64_t sa0, int64_t sa1, const float* B, int64_t sb0, int64_t sb1, float* C,
                         int64_t ldc, int M, int N, int K, int accumulate, cudaStream_t st);
+// split-K form (S slices of K, partial: S x M x N floats of scratch); gemm_splits picks S
+int gemm_splits(int M, int N, int K, int num_sms);
+cudaError_t launch_gemm_split(const float* A, int64_t sa0, int64_t sa1, const float* B, int64_t sb0, int64_t sb1,
+                              float* C, int64_t ldc, int M, int N, int K, int accumulate, int S, float* partial,
+                              cudaStream_t st);
 cudaError_t launch_bias_relu(float* y, const float* b, int M, int N, float* out, cudaStream_t st);
 cudaError_t launch_bias_grad(const float* g, int Nn, int K, int64_t inner, float* db, cudaStream_t st);
 cudaError_t launch_relu_bwd(float* g, const float* pre, int64_t n, cudaStream_t st);
