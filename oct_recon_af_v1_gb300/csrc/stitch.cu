@@ -491,7 +491,20 @@ __device__ __forceinline__ void quantise_span(const float* __restrict__ db, int6
         const int64_t n4 = n >> 2;
         const float4* d4 = reinterpret_cast<const float4*>(db);
         uint2* b4 = reinterpret_cast<uint2*>(bits);
-        for (int64_t i = tid; i < n4; i += stride) {
+        // four independent 16-byte loads in flight per thread
+        int64_t i = tid;
+        for (; i + 3 * stride < n4; i += 4 * stride) {
+            float4 v[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) v[u] = d4[i + u * stride];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const unsigned int c0 = quantise_one(v[u].x, q, T), c1 = quantise_one(v[u].y, q, T);
+                const unsigned int c2 = quantise_one(v[u].z, q, T), c3 = quantise_one(v[u].w, q, T);
+                b4[i + u * stride] = make_uint2(c0 | (c1 << 16), c2 | (c3 << 16));
+            }
+        }
+        for (; i < n4; i += stride) {
             const float4 v = d4[i];
             const unsigned int c0 = quantise_one(v.x, q, T), c1 = quantise_one(v.y, q, T);
             const unsigned int c2 = quantise_one(v.z, q, T), c3 = quantise_one(v.w, q, T);
