@@ -633,10 +633,32 @@ def gpu_arm_config4(args, rank, world, torch, ctx, stream, dev):
     beta_l, focus_l = L.decode(pred_host.numpy())
     host_raw = raw_t.cpu().pin_memory()
     dev_raw = torch.empty_like(raw_t)
+    # end to end: the step's raw B-scans go up in 5 chunks on a copy stream and
+    # the probe images of a chunk are made as soon as it has arrived (uploads
+    # overlap image making); the CNN then runs on all of them and the
+    # predictions come back.  The next step's uploads wait until this step's
+    # image making has finished reading the buffer.
+    up = torch.cuda.Stream()
+    n_chunks = 5
+    bounds = [n_test * c // n_chunks for c in range(n_chunks + 1)]
+    arrived = [torch.cuda.Event() for _ in range(n_chunks)]
+    raw_free = torch.cuda.Event()
+    raw_free.record(stream)
 
     def e2e_step():
-        dev_raw.copy_(host_raw, non_blocking=True)
-        learned_step(dev_raw)
+        up.wait_event(raw_free)
+        with torch.cuda.stream(up):
+            for c in range(n_chunks):
+                sl = slice(bounds[c], bounds[c + 1])
+                dev_raw[sl].copy_(host_raw[sl], non_blocking=True)
+                arrived[c].record(up)
+        for c in range(n_chunks):
+            sl = slice(bounds[c], bounds[c + 1])
+            stream.wait_event(arrived[c])
+            mk.images(dev_raw[sl], out=img_buf[sl], raw_dtype=U16)
+        raw_free.record(stream)
+        pred = net.predict(img_buf)
+        pred_host.copy_(pred, non_blocking=True)
 
     ms_e2e, _ = timed(e2e_step, args.steps, 1)
     # ---- the plain search on the same B-scans (GPU scorer + host Brent + focus rules)
