@@ -207,6 +207,23 @@ def run_step(ctx, vol, src, db_vol, bits, batch=9):
     ctx.quantise_running(db_vol, bits)
 
 
+FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12     # SMs x FP32 lanes x FMA x max SM clock
+
+
+def fp32_ceiling(ascans_per_s, sg):
+    """Nominal FLOP of one A-scan's spectral stage (background 2N, banded sinc
+    2 T N with T the geometry's taps, complex window 2N, 2048-point FFT
+    5 N log2 N, |.| 3 N/2) at the measured rate, against the CUDA cores'
+    nominal FP32 peak."""
+    n = 2048
+    taps = int(np.asarray(sg.sinc_idx).shape[1])
+    flops = 2 * n + 2 * taps * n + 2 * n + 5 * n * 11 + 3 * n // 2
+    achieved = ascans_per_s * flops / 1e12
+    return {"flops_per_ascan": flops, "achieved_tflops": achieved, "peak_tflops": FP32_NOMINAL_TFLOPS,
+            "frac": achieved / FP32_NOMINAL_TFLOPS,
+            "peak_source": "nominal: 152 SMs x 128 FP32 lanes x 2 x 2.07 GHz (no measured FP32 peak on this pool)"}
+
+
 def time_spectral_kernel(ctx, torch, raw_tile, stream, reps=10):
     """CUDA-event time of the spectral stage (apod mean + fused kernel) on a slab of one tile."""
     B = raw_tile.shape[0]
@@ -331,7 +348,10 @@ def gpu_arm(args, rank, world):
                      "traffic": SPECTRAL_DRAM_BYTES_PER_ASCAN * kascans,
                      "kernel": "spectral stage (apod mean + k_spectral, magnitude out)",
                      "bytes_per_launch": kbytes, "ms_per_launch": kms, "a_scans_per_launch": kascans,
-                     "peak_source": src + " (burst copy)"},
+                     "peak_source": src + " (burst copy)",
+                     # the arithmetic intensity (~21 flop/B) is above the FP32 ridge: the same
+                     # launch against the CUDA cores' nominal FP32 rate
+                     "fp32_ceiling": fp32_ceiling(kascans / (kms * 1e-3), vol.sg)},
         "clocks": clk,
     }
     if e2e_ms is not None:
