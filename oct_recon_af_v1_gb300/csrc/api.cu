@@ -61,7 +61,7 @@ struct Plan {
     std::vector<int2> zblk_h, cblk_h;   // host copies of the block tables
     bool lateral_identity = false;      // WxT is the identity (single-tile output grid)
     bool lateral_quad_local = false;    // every non-zero lateral weight stays inside the column's B-scan quad
-    DevBuf zr, wz0, wz1, xr, wx0, wx1, fz, shift, lo, hi, zblk, cblk;
+    DevBuf zr, wz0, wz1, xr, wx0, wx1, fz, shift, lo, hi, zblk, cblk, zrow, zf;
     bool opc = false;
     StitchDev dev() const {
         StitchDev d;
@@ -77,6 +77,8 @@ struct Plan {
         d.hi = opc ? hi.as<int>() : nullptr;
         d.zblk = zblk.as<int2>();
         d.cblk = cblk.as<int2>();
+        d.zrow = zrow.as<float4>();
+        d.zf = zf.as<float2>();
         d.cblk_first = cblk_first;
         d.n_cblk = n_cblk;
         d.r0 = r0;
@@ -89,7 +91,8 @@ struct Plan {
         return d;
     }
     void release() {
-        for (DevBuf* b : {&zr, &wz0, &wz1, &xr, &wx0, &wx1, &fz, &shift, &lo, &hi, &zblk, &cblk}) b->release();
+        for (DevBuf* b : {&zr, &wz0, &wz1, &xr, &wx0, &wx1, &fz, &shift, &lo, &hi, &zblk, &cblk, &zrow, &zf})
+            b->release();
     }
 };
 
@@ -864,6 +867,23 @@ int octgb_stitch_plan(octgb_ctx* c, int n_rows, int r0, int r1, int c0, int c1, 
             up(p->fz, fzf.data(), fzf.size() * sizeof(float));
             up(p->zblk, zb.data(), zb.size() * sizeof(int2));
             up(p->cblk, cbt.data(), cbt.size() * sizeof(int2));
+            // per output row, for the batched form's depth resampling: {zr, w0,
+            // w1, d} and the focus weights {F[zr], F[zr + 1] (0 past the window)},
+            // d = fma(F1, w1, F0 w0) as the kernel forms it
+            std::vector<float4> zrow(n_out_z);
+            std::vector<float2> zfv(n_out_z);
+            for (int zo = 0; zo < n_out_z; ++zo) {
+                const int z = zr[zo];
+                const float f0 = z >= 0 ? fzf[z] : 0.f;
+                const float f1 = z >= 0 && z + 1 < R ? fzf[z + 1] : 0.f;
+                const float prod = f0 * wz0[zo];
+                float zrf;
+                memcpy(&zrf, &z, sizeof(float));
+                zrow[zo] = make_float4(zrf, wz0[zo], wz1[zo], std::fmaf(f1, wz1[zo], prod));
+                zfv[zo] = make_float2(f0, f1);
+            }
+            up(p->zrow, zrow.data(), zrow.size() * sizeof(float4));
+            up(p->zf, zfv.data(), zfv.size() * sizeof(float2));
             if (shift != nullptr) {
                 require(n_y >= 1, "n_y must be >= 1 with optical-path correction");
                 const size_t m = static_cast<size_t>(n_y) * n_tile_x;

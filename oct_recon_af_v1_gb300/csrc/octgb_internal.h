@@ -103,6 +103,10 @@ struct StitchDev {
     const int2* zblk;
     // per absolute 32-column output block cblk_first + i: A-scans [x, y] it reads; x = -1: none
     const int2* cblk;
+    // per output row: {zr (int bits), wz0, wz1, d = fma(F1, wz1, F0 wz0)} and
+    // {F0 = fz[zr], F1 = fz[zr + 1] or 0 past the window} (batched form)
+    const float4* zrow;
+    const float2* zf;
     int cblk_first, n_cblk;
     int r0, R, c0, C, n_out_z, n_tile_x, n_rows;
 };

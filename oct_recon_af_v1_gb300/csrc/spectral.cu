@@ -408,15 +408,17 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
 #pragma unroll
                 for (int r = 0; r < 4; ++r) M[lt + 128 * h + 256 * r] = magv[h][r];
             group_sync(g);
+            // per output row one 16-byte {zr, w0, w1, d} and one 8-byte {F0, F1}
+            // load (F1 = 0: no second row)
             for (int zo = lt; zo < tile.nz; zo += kGroup) {
-                const int zr = p.zr[zo];
+                const float4 rw = __ldg(p.zrow + zo);
+                const int zr = __float_as_int(rw.x);
                 float u = 0.f;
                 if (zr >= 0) {
-                    const bool has1 = zr + 1 < p.R;
-                    const float w0 = p.wz0[zo], w1 = p.wz1[zo];
-                    const float a0v = M[p.r0 + zr] * p.fz[zr];
-                    const float a1v = has1 ? M[p.r0 + zr + 1] * p.fz[zr + 1] : 0.f;
-                    u = fmaf(a1v, w1, a0v * w0);
+                    const float2 ff = __ldg(p.zf + zo);
+                    const float a0v = M[p.r0 + zr] * ff.x;
+                    const float a1v = ff.y != 0.f ? M[p.r0 + zr + 1] * ff.y : 0.f;
+                    u = fmaf(a1v, rw.z, a0v * rw.y);
                 }
                 Uz[zo] = u;
             }
@@ -432,13 +434,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
                 const float* U1 = reinterpret_cast<const float*>(S.spec[in1 ? s1i : 0]) + kHalf;
                 float* out = tile.out + me.as * tile.nz;
                 for (int zo = lt; zo < tile.nz; zo += kGroup) {
-                    const int zr = p.zr[zo];
+                    const float4 rw = __ldg(p.zrow + zo);
+                    const int zr = __float_as_int(rw.x);
                     float v = __int_as_float(0x7fc00000);
                     if (zr >= 0 && xr >= 0) {
-                        const bool has1 = zr + 1 < p.R;
-                        const float w0 = p.wz0[zo], w1 = p.wz1[zo];
-                        const float f0 = p.fz[zr], f1 = has1 ? p.fz[zr + 1] : 0.f;
-                        const float d = fmaf(f1, w1, f0 * w0);
+                        const float d = rw.w;
                         const float u0 = in0 ? U0[zo] : 0.f, u1 = in1 ? U1[zo] : 0.f;
                         const float d0 = in0 ? d : 0.f, d1 = in1 ? d : 0.f;
                         const float num = fmaf(u1, wx1, u0 * wx0);
