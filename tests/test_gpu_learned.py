@@ -258,3 +258,57 @@ def test_trained_network_gains_over_no_estimator(torch_ctx):
     finally:
         mk.close()
         net_ctx.close()
+
+
+def test_fused_probe_images_match_magnitude_path(torch_ctx):
+    """octgb_disp_images (depth pooling inside the dispersion kernel, then over
+    A-scans) against the two-step path (octgb_disp_eval magnitudes, then
+    octgb_cnn_images) with B-scan repeats averaged (rep 2) and a width that is
+    not a multiple of 256: the same images up to float32 summation order."""
+    torch, _ = torch_ctx
+    from oct_recon_af_v1_gb300 import learned as L
+    from oct_recon_af_v1_gb300 import synthetic as S
+    from oct_recon_af_v1_gb300._lib import U16
+    from oct_recon_af_v1_gb300.estimation import hann_rms
+    from oct_recon_af_v1_gb300.learned import _p
+    mk = L.ImageMaker(S.lambda_nm(), 25)
+    try:
+        nb, rep, nx = 3, 2, 300
+        raw = S.u16_bits(S.generate(nb * rep, nx, 25, seed=33, device="cuda", beta_px=2e-5, focus_px=500.0,
+                                    chunk=nb * rep, precision="float32"))
+        ctx = mk.ctx
+        ctx.disp_load(raw, 25, nb, rep, hann_rms(2048), raw_dtype=U16)
+        betas = np.array([-3e6, 0.0, 4e6])
+        fused = torch.empty((nb, 3, L.IMG, L.IMG), dtype=torch.float32, device="cuda")
+        ctx._check(ctx.lib.octgb_disp_images(ctx.h, 3, betas.ctypes.data, 0, nb, L.Z_KEEP, _p(fused), 0))
+        mag = torch.empty((3, nb, nx, 1024), dtype=torch.float32, device="cuda")
+        ctx.disp_eval(betas, 0, nb, 0, mag=mag)
+        ref = torch.empty_like(fused)
+        ctx._check(ctx.lib.octgb_cnn_images(ctx.h, _p(mag), 3, nb, nx, L.Z_KEEP, _p(ref), 0))
+        ctx.synchronize()
+        np.testing.assert_allclose(fused.cpu().numpy(), ref.cpu().numpy(), rtol=0, atol=1e-4)
+    finally:
+        mk.close()
+
+
+def test_dense_split_k_matches_float64(torch_ctx):
+    """The dense layer over 8192 flattened features (split K across the SMs,
+    slices summed in a fixed order) against float64, and bit-identical run to run."""
+    torch, ctx = torch_ctx
+    from oct_recon_af_v1_gb300.learned import _p
+    rng = np.random.default_rng(9)
+    m, k, n = 300, 8192, 64
+    x = rng.standard_normal((m, k)).astype(np.float32)
+    w = (rng.standard_normal((n, k)) / np.sqrt(k)).astype(np.float32)
+    b = rng.standard_normal(n).astype(np.float32)
+    xd, wd, bd = (torch.tensor(a, device="cuda") for a in (x, w, b))
+    pre = torch.empty((m, n), device="cuda")
+    act = torch.empty((m, n), device="cuda")
+    ctx._check(ctx.lib.octgb_cnn_dense(ctx.h, _p(xd), _p(wd), _p(bd), _p(pre), _p(act), m, k, n))
+    first = pre.clone()
+    ctx._check(ctx.lib.octgb_cnn_dense(ctx.h, _p(xd), _p(wd), _p(bd), _p(pre), _p(act), m, k, n))
+    ctx.synchronize()
+    ref = x.astype(np.float64) @ w.astype(np.float64).T + b
+    np.testing.assert_allclose(pre.cpu().numpy(), ref, rtol=0, atol=2e-5 * np.abs(ref).max())
+    np.testing.assert_array_equal(act.cpu().numpy(), np.maximum(pre.cpu().numpy(), 0))
+    assert torch.equal(first, pre)
