@@ -536,25 +536,20 @@ int octgb_set_geometry(octgb_ctx* c, int n, int taps, const int64_t* idx, const 
         std::vector<float> wt(static_cast<size_t>(taps) * kN);
         std::vector<int> st(kN);
         for (int i = 0; i < kN; ++i) {
-            int s = -1, len = 0;
+            int s = -1;
             for (int t = 0; t < taps; ++t) {
                 const double wv = w[static_cast<size_t>(i) * taps + t];
                 const int64_t j = idx[static_cast<size_t>(i) * taps + t];
                 require(j >= 0 && j < kN, "sinc index out of range");
                 if (t == 0) s = static_cast<int>(j);
                 const bool pad_entry = (wv == 0.0 && j == 0 && t > 0);
-                if (!pad_entry) {
-                    require(j == s + t, "sinc taps of a row must be contiguous increasing indices");
-                    len = t + 1;
-                }
+                if (!pad_entry) require(j == s + t, "sinc taps of a row must be contiguous increasing indices");
                 wt[static_cast<size_t>(t) * kN + i] = static_cast<float>(wv);
             }
-            (void)len;
             st[i] = s;
         }
         // shifted dense weights of the spectral kernel: thread t owns outputs
         // 4t..4t+3; wsh[t][r][u] = weight of source s0_t + u for output 4t + r
-        int len_max = 0;
         std::vector<int> len(kN, 0);
         for (int i = 0; i < kN; ++i) {
             for (int t = 0; t < taps; ++t)
@@ -570,7 +565,6 @@ int octgb_set_geometry(octgb_ctx* c, int n, int taps, const int64_t* idx, const 
                 U_need = U_need > reach ? U_need : reach;
             }
         }
-        (void)len_max;
         int U = U_need <= 16 ? 16 : (U_need <= 20 ? 20 : (U_need <= 24 ? 24 : 0));
         require(U > 0, "sinc band too wide for the spectral kernel (4 outputs need > 24 source samples)");
         std::vector<float> wsh(static_cast<size_t>(kThreads) * 4 * U, 0.f);

@@ -236,7 +236,6 @@ constexpr uint32_t kRawTileBytes = kPChunks * kAChunkBytes;            // 12 chu
 constexpr uint32_t kRStageBytes = kRawTileBytes + 2 * kATileBytes + 2 * kBTileBytes;
 constexpr uint32_t kRLoadBytes = kRawTileBytes + 2 * kBTileBytes + kPKW * 4;   // bytes the copies deliver per block
 
-constexpr uint32_t kRSBytes = kPKW * 4;                                // apodisation sums of one window
 
 struct RawSmem {
     alignas(1024) uint8_t stage[kPStages][kRStageBytes];   // raw | A_hi | A_lo | B_hi | B_lo
