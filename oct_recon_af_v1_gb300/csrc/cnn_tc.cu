@@ -167,10 +167,9 @@ __global__ void __launch_bounds__(kCThreads, 4)
         pcs[k] = p < g.pix_c ? p - prs[k] * g.cols_s : 0;
     }
 
-    auto epilogue = [&](int64_t u, int ab) {
+    // the tile origin (img, y0, x0) of the unit (its first tile with pool)
+    auto epilogue = [&](int ab, int img, int y0, int x0) {
         const int m = 32 * warp + lane;
-        int img, y0, x0;
-        unit_tile(g, u, 0, img, y0, x0);
         const uint32_t taddr = tmem + (static_cast<uint32_t>(32 * warp) << 16) + static_cast<uint32_t>(ab * U * g.cout);
         if (!g.pool) {
             const int oy = y0 + m / g.wseg, ox = x0 + m % g.wseg;
@@ -186,22 +185,28 @@ __global__ void __launch_bounds__(kCThreads, 4)
             }
         } else {
             // rows y0 (accumulator 0) and y0 + 1 (accumulator 1); lanes m, m + 1
-            // are the two columns: 0.25 ((relu + relu) + (relu + relu)) as k_relu_pool
+            // are the two columns.  Per pair of channels each lane sums its
+            // column's two ReLUs for both, swaps one with its neighbour and
+            // writes one: the even lane the first channel, the odd lane the
+            // second (0.25 x the 2x2 sum; the summation order is not
+            // k_relu_pool's, the operands being FP16-rounded already)
             const int Ho = g.H / 2, Wo = g.W / 2;
             const int64_t pw = static_cast<int64_t>(Ho) * Wo;
-            float* po = y + static_cast<int64_t>(img) * g.cout * pw + static_cast<int64_t>(y0 / 2) * Wo + (x0 + m) / 2;
+            const int odd = lane & 1;
+            float* po = y + static_cast<int64_t>(img) * g.cout * pw + static_cast<int64_t>(y0 / 2) * Wo + (x0 + m) / 2 +
+                        odd * pw;
             for (int c0 = 0; c0 < g.cout; c0 += 32) {
                 float v0[32], v1[32];
                 tmem_ld32(taddr + static_cast<uint32_t>(c0), v0);
                 tmem_ld32(taddr + static_cast<uint32_t>(g.cout + c0), v1);
 #pragma unroll
-                for (int i = 0; i < 32; ++i) {
-                    const float bb = S.bias[c0 + i];
-                    const float top = fmaxf(v0[i] + bb, 0.f), bot = fmaxf(v1[i] + bb, 0.f);
-                    const float tsum = top + __shfl_xor_sync(0xffffffffu, top, 1);
-                    const float bsum = bot + __shfl_xor_sync(0xffffffffu, bot, 1);
-                    if ((lane & 1) == 0) *po = 0.25f * (tsum + bsum);
-                    po += pw;
+                for (int i = 0; i < 32; i += 2) {
+                    const float b0 = S.bias[c0 + i], b1 = S.bias[c0 + i + 1];
+                    const float t0 = fmaxf(v0[i] + b0, 0.f) + fmaxf(v1[i] + b0, 0.f);
+                    const float t1 = fmaxf(v0[i + 1] + b1, 0.f) + fmaxf(v1[i + 1] + b1, 0.f);
+                    const float other = __shfl_xor_sync(0xffffffffu, odd ? t0 : t1, 1);
+                    *po = 0.25f * ((odd ? t1 : t0) + other);
+                    po += 2 * pw;
                 }
             }
         }
@@ -210,19 +215,23 @@ __global__ void __launch_bounds__(kCThreads, 4)
 
     uint32_t j = 0;            // tiles staged by this CTA so far
     uint32_t ju = 0;           // units so far (accumulator set ju & 1)
-    int64_t prev = -1;
+    bool have_prev = false;
+    int prev_img = 0, prev_y0 = 0, prev_x0 = 0;  // origin of the previous unit
     bool ok = true;
     for (int64_t u = blockIdx.x; u < g.n_units && ok; u += gridDim.x, ++ju) {
         const int ab = static_cast<int>(ju & 1);
+        int img, y0u, x0;
+        unit_tile(g, u, 0, img, y0u, x0);
         for (int h = 0; h < U && ok; ++h, ++j) {
-            const int b = static_cast<int>(j % static_cast<uint32_t>(g.nbuf));
+            // nbuf is 1 or 2: the buffer and the parity of its previous use
+            const int b = g.nbuf == 2 ? static_cast<int>(j & 1u) : 0;
             if (j >= static_cast<uint32_t>(g.nbuf)) {
                 // the MMAs of the tile staged nbuf tiles ago have read X[b]
-                ok = conv_wait(&S.x[b], ((j - g.nbuf) / g.nbuf) & 1u, S, status);
+                const uint32_t use = g.nbuf == 2 ? (j - 2) >> 1 : j - 1;
+                ok = conv_wait(&S.x[b], use & 1u, S, status);
                 if (!ok) break;
             }
-            int img, y0, x0;
-            unit_tile(g, u, h, img, y0, x0);
+            const int y0 = y0u + h;
             uint4* X = reinterpret_cast<uint4*>(base + b * g.xbytes);
             const float* xi = x + static_cast<int64_t>(img) * g.cin * hw;
             int off[kCSlots];
@@ -243,9 +252,12 @@ __global__ void __launch_bounds__(kCThreads, 4)
                 for (int k = 0; k < kCSlots; ++k) {
                     if (prs[k] < 0) continue;
                     float v[8];
+                    const float* pe = xc + (off[k] >= 0 ? off[k] : 0);
 #pragma unroll
-                    for (int e = 0; e < 8; ++e)
-                        v[e] = (off[k] >= 0 && e < ne) ? __ldg(xc + static_cast<int64_t>(e) * hw + off[k]) : 0.f;
+                    for (int e = 0; e < 8; ++e) {
+                        v[e] = (off[k] >= 0 && e < ne) ? __ldg(pe) : 0.f;
+                        pe += hw;
+                    }
                     const uint4 q = make_uint4(pack_h2(v[0], v[1]), pack_h2(v[2], v[3]), pack_h2(v[4], v[5]),
                                                pack_h2(v[6], v[7]));
                     const int p = tid + kCThreads * k;
@@ -287,21 +299,24 @@ __global__ void __launch_bounds__(kCThreads, 4)
             }
         }
         if (!ok) break;
-        if (prev >= 0) {
+        if (have_prev) {
             const int pab = static_cast<int>((ju - 1) & 1);
             ok = conv_wait(&S.d[pab], ((ju - 1) >> 1) & 1u, S, status);
             if (!ok) break;
             tc_fence_after();
-            epilogue(prev, pab);
+            epilogue(pab, prev_img, prev_y0, prev_x0);
         }
-        prev = u;
+        have_prev = true;
+        prev_img = img;
+        prev_y0 = y0u;
+        prev_x0 = x0;
     }
-    if (ok && prev >= 0) {
+    if (ok && have_prev) {
         const int pab = static_cast<int>((ju - 1) & 1);
         ok = conv_wait(&S.d[pab], ((ju - 1) >> 1) & 1u, S, status);
         if (ok) {
             tc_fence_after();
-            epilogue(prev, pab);
+            epilogue(pab, prev_img, prev_y0, prev_x0);
         }
     }
     // every MMA this CTA issued has completed before its TMEM is released
