@@ -224,6 +224,26 @@ def fp32_ceiling(ascans_per_s, sg):
             "peak_source": "nominal: 152 SMs x 128 FP32 lanes x 2 x 2.07 GHz (no measured FP32 peak on this pool)"}
 
 
+def link_bandwidth(torch, stream, dev, nbytes=1 << 30):
+    """Host<->device copy bandwidth (GB/s) of this box between pinned host
+    memory and the device, CUDA events around 3 copies each way."""
+    h = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    d = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+    out = {}
+    for name, (dst, src) in (("h2d_gbs", (d, h)), ("d2h_gbs", (h, d))):
+        dst.copy_(src, non_blocking=True)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(3):
+            dst.copy_(src, non_blocking=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        out[name] = 3 * nbytes / (e0.elapsed_time(e1) * 1e-3) / 1e9
+    del h, d
+    return out
+
+
 def time_spectral_kernel(ctx, torch, raw_tile, stream, reps=10):
     """CUDA-event time of the spectral stage (apod mean + fused kernel) on a slab of one tile."""
     B = raw_tile.shape[0]
@@ -329,7 +349,9 @@ def gpu_arm(args, rank, world):
     ms, launches = timed(vol.raw, args.steps, args.warmup)
     clk = clocks.stop()
     e2e_ms = None
+    link = None
     if not args.no_e2e:
+        link = link_bandwidth(torch, stream, dev)
         # at least 8 volumes back to back: the last volume's code read-back (no
         # next volume to overlap with) is inside the timed region
         e2e_ms, _ = timed(vol.host, max(8, args.steps), 1, e2e=True)
@@ -356,6 +378,11 @@ def gpu_arm(args, rank, world):
                      "fp32_ceiling": fp32_ceiling(kascans / (kms * 1e-3), vol.sg)},
         "clocks": clk,
     }
+    if e2e_ms is not None:
+        h2d, d2h = vol.raw_bytes(), int(bits.numel()) * 2
+        line["e2e_link"] = dict(link, h2d_floor_ms=h2d / (link["h2d_gbs"] * 1e6),
+                                note="pinned-memory copy bandwidth measured on this box just before the e2e run; "
+                                     "the volume's raw upload alone needs h2d_floor_ms")
     if e2e_ms is not None:
         line["e2e"] = {"value": ascans / (e2e_ms * 1e-3), "unit": "A-scans/s", "ms_per_step": e2e_ms,
                        "h2d_bytes_per_step": vol.raw_bytes(), "d2h_bytes_per_step": int(bits.numel()) * 2}
