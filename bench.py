@@ -25,7 +25,10 @@ spectra in pinned host memory (H2D inside the timed region) and reads the
 uint16 volume back (D2H).  Volumes are processed back to back: a volume's
 codes need its global clim, so their read-back overlaps the next volume's
 upload and reconstruction (second stream, double-buffered codes); the timed
-region holds max(8, K) volumes and ends after the last read-back.  `--impl reference` times the reference
+region holds max(8, K) volumes and ends after the last read-back; `e2e_link`
+gives this box's pinned host<->device copy bandwidth measured just before.
+`roofline` is the spectral stage's against HBM; its `fp32_ceiling` is the same
+launch against the CUDA cores' nominal FP32 rate.  `--impl reference` times the reference
 algorithm's CPU restatement (the oracle: Numba kernel restated in C/OpenMP +
 pocketfft + NumPy stitching) on the host cores over bounded samples.
 
