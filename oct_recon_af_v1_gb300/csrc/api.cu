@@ -390,9 +390,11 @@ const SlotTable& slot_table(octgb_ctx* c, int n_tiles, const int* plan_ids, int 
 // The device copy of a batched-form tile table.  Tables are kept by content:
 // a batch repeated with the same tiles reuses its table, a table used while a
 // graph is captured is pinned (the graph replays with its address), and at
-// most kMaxFreeTables unpinned tables are kept, the least recently used one
-// being overwritten (in stream order, after every kernel that read it).
-constexpr int kMaxFreeTables = 8;
+// most kMaxFreeTables unpinned tables (16 KiB each) are kept, the least
+// recently used one being overwritten (in stream order, after every kernel
+// that read it): a sequence of up to that many distinct batches (one per tile,
+// say) can be run once and then captured.
+constexpr int kMaxFreeTables = 128;
 
 const QueueTile* tile_table(octgb_ctx* c, const std::vector<QueueTile>& qt) {
     const size_t bytes = qt.size() * sizeof(QueueTile);
