@@ -72,9 +72,11 @@ def config1_layout(seed=1, bscans=270):
 
 
 def config1_desc(bscans=270):
+    """The workload alone (the same dict in both arms); how an arm runs it
+    (parallelism, batch, the A-scans one timed step covers) is its `execution`."""
     return {"workload": f"config1: 2x2 tiles x 3 depths, tile {bscans} B-scans x 1000 A-scans x 2048 uint16, "
                         "focus 400+-30 px sigma 80, 10% overlap, n 1.33, 1 um output, uint16 legacy codes",
-            "a_scans_per_step": 12 * bscans * 1000, "tiles": 12, "bscans_per_tile": bscans,
+            "a_scans_per_volume": 12 * bscans * 1000, "tiles": 12, "bscans_per_tile": bscans,
             "ascans_per_bscan": 1000,
             "apod_lines": APOD, "spectral_samples": 2048, "l2_flush": "inputs (13.3 GB) larger than L2"}
 
@@ -368,8 +370,9 @@ def gpu_arm(args, rank, world):
         "metric": METRIC, "value": value, "unit": "A-scans/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_all, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 (uint16 in, uint16 out)", "data": "synthetic (seeded, generated on device)",
-        "config": dict(config1_desc(vol.ny), parallelism=f"replicas x{world} (independent volumes)",
-                       frame_batch=args.batch, cuda_graph=graph is not None),
+        "config": config1_desc(vol.ny),
+        "execution": {"parallelism": f"replicas x{world} (independent volumes)", "frame_batch": args.batch,
+                      "cuda_graph": graph is not None, "a_scans_per_step": ascans},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": SPECTRAL_DRAM_BYTES_PER_ASCAN * kascans,
@@ -391,6 +394,8 @@ def gpu_arm(args, rank, world):
                        "h2d_bytes_per_step": vol.raw_bytes(), "d2h_bytes_per_step": int(bits.numel()) * 2}
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline_config1(vol, torch, budget_s=args.cpu_budget)
+        first = {k: vol.raw[(0,) + k][:1].cpu().numpy().view(np.uint16) for k in vol.order}
+        line["cpu_numpy_path"] = numpy_path_baseline(vol, vol.tg, first, frames=1)
     if rank == 0 and not args.no_plain:
         torch.cuda.synchronize()
         pf = plain_form_arm(vol, torch, dev)
@@ -1013,14 +1018,57 @@ def reference_arm(args, rank, world):
         n += _cpu_sample(tiles, vol, np.arange(F), g, sts)
     dt = time.perf_counter() - t0
     v = n / dt
+    per_step = n // args.steps
+    sample = f"each step: frames 0..{F - 1} of the 6 tiles of y-row 0 ({per_step} A-scans)"
     return {"impl": "reference", "metric": METRIC, "value": v, "unit": "A-scans/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64 (Numba types)",
-            "data": "synthetic (seeded)", "config": dict(config1_desc(), parallelism="host cores"),
+            "data": "synthetic (seeded)", "config": config1_desc(),
+            "execution": {"parallelism": f"host cores ({os.cpu_count()} threads)", "a_scans_per_step": per_step,
+                          "sample": sample},
             "cpu_baseline": {"value": v, "unit": "A-scans/s", "cores": os.cpu_count(), "kind": "port",
-                             "sample": f"each step: frames 0..{F - 1} of the 6 tiles of y-row 0 "
-                                       f"({6 * F * lay.n_x_px} A-scans)"},
+                             "sample": sample},
+            "numpy_path": numpy_path_baseline(vol, tg, tiles, frames=1),
             "e2e": {"value": v, "unit": "A-scans/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def numpy_path_baseline(vol, tg, tiles, frames=1):
+    """The reference's own NumPy path (SpectralProcessor with use_numba=False,
+    float32; TileStitcher.contribute; the row finalise of pipeline.py:296-300),
+    unmodified, on the first `frames` frames of the 6 tiles of y-row 0."""
+    if _import_reference_octrecon() is None:
+        return {"unavailable": "octrecon is not installed in baseline/_ref"}
+    from octrecon.core.geometry import build_spectral_geometry
+    from octrecon.core.spectral import SpectralProcessor
+    from octrecon.core.stitching import TileStitcher, min_weight_threshold
+
+    from oct_recon_af_v1_gb300 import synthetic
+    os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
+    sg = build_spectral_geometry(synthetic.lambda_nm(), synthetic.beta_ref_from_px(1e-5), 1.33, "sinc5")
+    sp = SpectralProcessor(sg, APOD, xp=np, dtype=np.float32, use_numba=False)
+    sts = {k: TileStitcher(tg, None, vol.lay.x_centers_mm[k[0]], vol.lay.z_depths_mm[k[1]], vol.focus[k[1]], 80.0,
+                           xp=np, dtype=np.float32) for k in vol.order}
+
+    def row():
+        num = np.zeros((frames, vol.nz, vol.nx), np.float32)
+        den = np.zeros_like(num)
+        fr = np.arange(frames)
+        for k in vol.order:
+            n_, d_ = sts[k].contribute(sp.magnitude(tiles[k][:frames]), fr)
+            num[:, :, sts[k].c0:sts[k].c1] += n_
+            den[:, :, sts[k].c0:sts[k].c1] += d_
+        den[den < min_weight_threshold(np.float32)] = np.nan
+        with np.errstate(divide="ignore", invalid="ignore"):
+            return 20 * np.log10(num / den)
+
+    row()
+    t0 = time.perf_counter()
+    row()
+    dt = time.perf_counter() - t0
+    n = 6 * frames * vol.lay.n_x_px
+    return {"value": n / dt, "unit": "A-scans/s", "cores": os.cpu_count(), "kind": "reference",
+            "sample": f"frames 0..{frames - 1} of the 6 tiles of y-row 0 ({n} A-scans): the reference's NumPy "
+                      "path (use_numba=False, float32), its TileStitcher and row finalise"}
 
 
 def main():

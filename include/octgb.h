@@ -82,7 +82,11 @@ int64_t octgb_launch_count(const octgb_ctx *ctx);
  *            `sg.sinc_w.astype(float32)` does);
  *   window   (n, 2) float64 re/im: Hann/rms * exp(i*phase) (rounded to
  *            complex64).
- * n must be 2048 (the kernels' FFT length); taps <= 32. */
+ * n must be 2048 (the kernels' FFT length); taps <= 32.
+ * Refused (OCTGB_ERR_STATE) while a graph is being captured or while the
+ * context holds captured graphs: a graph replays the geometry buffers it was
+ * captured with, and a new geometry may reallocate them.  Release the graphs
+ * first (octgb_graphs_release). */
 int octgb_set_geometry(octgb_ctx *ctx, int n, int taps, const int64_t *sinc_idx, const double *sinc_w,
                        const double *window);
 
@@ -267,6 +271,10 @@ int octgb_quantise_running(octgb_ctx *ctx, const float *db, int64_t n, int db_lo
 int octgb_graph_begin(octgb_ctx *ctx);
 int octgb_graph_end(octgb_ctx *ctx, int *graph_id);
 int octgb_graph_launch(octgb_ctx *ctx, int graph_id);
+/* Destroy every graph captured on the context (after the work already
+ * launched has completed); their ids become invalid and octgb_set_geometry is
+ * accepted again.  No counterpart in the reference (its loop has no graphs). */
+int octgb_graphs_release(octgb_ctx *ctx);
 
 /* ---------------------------------------------------------------- batched form */
 

@@ -49,6 +49,7 @@ SIGNATURES = {
     "octgb_graph_begin": (c_int, [c_void_p]),
     "octgb_graph_end": (c_int, [c_void_p, POINTER(c_int)]),
     "octgb_graph_launch": (c_int, [c_void_p, c_int]),
+    "octgb_graphs_release": (c_int, [c_void_p]),
     "octgb_magnitude_noalloc": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_void_p]),
     "octgb_batch_process": (c_int, [c_void_p, c_int, c_void_p, c_int, c_float, c_int]),
     "octgb_disp_load": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_int, c_int, c_void_p]),
@@ -541,6 +542,10 @@ class Context:
 
     def graph_launch(self, gid: int):
         self._check(self.lib.octgb_graph_launch(self.h, int(gid)))
+
+    def graphs_release(self):
+        """Destroy the context's captured graphs (a new geometry is refused while any exist)."""
+        self._check(self.lib.octgb_graphs_release(self.h))
 
     # -------------------------------------------------------------- batched form
     def batch_process(self, tiles, threshold: float, grab: int = 4, raw_dtype: int = U16):

@@ -532,6 +532,11 @@ int64_t octgb_launch_count(const octgb_ctx* c) { return c ? c->launches.load() :
 
 int octgb_set_geometry(octgb_ctx* c, int n, int taps, const int64_t* idx, const double* w, const double* window) {
     return guarded(c, [&] {
+        if (c->capturing) throw Error(OCTGB_ERR_STATE, "octgb_set_geometry during graph capture");
+        if (!c->graphs.empty())
+            throw Error(OCTGB_ERR_STATE,
+                        "the context holds captured graphs that replay its current geometry: "
+                        "call octgb_graphs_release before setting a new geometry");
         require(n == kN, "n must be 2048");
         require(taps >= 1 && taps <= kMaxTaps, "taps must be in [1, 32]");
         require(idx && w && window, "NULL geometry array");
@@ -1227,6 +1232,18 @@ int octgb_graph_launch(octgb_ctx* c, int graph_id) {
     });
 }
 
+
+int octgb_graphs_release(octgb_ctx* c) {
+    return guarded(c, [&] {
+        if (c->capturing) throw Error(OCTGB_ERR_STATE, "octgb_graphs_release during graph capture");
+        ck(cudaStreamSynchronize(c->stream), "sync before graph release");
+        for (cudaGraphExec_t g : c->graphs)
+            if (g) cudaGraphExecDestroy(g);
+        c->graphs.clear();
+        c->graph_kernels.clear();
+        for (QTable* t : c->qtables) t->pinned = false;
+    });
+}
 
 int octgb_batch_process(octgb_ctx* c, int n_tiles, const octgb_tile* tiles, int dtype, float thr, int grab) {
     return guarded(c, [&] {

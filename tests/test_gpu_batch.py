@@ -82,6 +82,7 @@ def test_batch_equals_frame_path_and_oracle(gpu_ctx):
             np.testing.assert_array_equal(t["db"].cpu().numpy(), g)
     finally:
         gpu_ctx.set_stream(None)
+        gpu_ctx.graphs_release()
 
 
 def test_batch_close_to_oracle(gpu_ctx):
@@ -145,3 +146,4 @@ def test_graph_replay_survives_other_batches(gpu_ctx):
             np.testing.assert_array_equal(t["db"].cpu().numpy(), g)
     finally:
         gpu_ctx.set_stream(None)
+        gpu_ctx.graphs_release()

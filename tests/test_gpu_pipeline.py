@@ -121,8 +121,21 @@ def test_graph_capture_replays_frame_batch(gpu_ctx, telesto):
         from oracle import numerics as O
         clim = (float(np.nanmin(ref)), float(np.nanmax(ref)))
         np.testing.assert_array_equal(bits.cpu().numpy().view(np.uint16), O.db_to_bits(ref, clim))
+        # a new geometry would reallocate buffers the graph replays: refused
+        # until the context's graphs are released
+        from oct_recon_af_v1_gb300 import _lib
+        from oct_recon_af_v1_gb300 import geometry as G
+        sg = G.build_spectral_geometry(t["lambda_nm"], float(t["dispersion"]), float(t["n_medium"]))
+        with pytest.raises(_lib.OctgbError) as e:
+            gpu_ctx.set_geometry(sg.sinc_idx, sg.sinc_w, sg.window)
+        assert e.value.code == _lib.ERR_STATE
+        gpu_ctx.graphs_release()
+        gpu_ctx.set_geometry(sg.sinc_idx, sg.sinc_w, sg.window)
+        with pytest.raises(_lib.OctgbError):
+            gpu_ctx.graph_launch(gid)
     finally:
         gpu_ctx.set_stream(None)
+        gpu_ctx.graphs_release()
 
 
 def test_frames_host_input_ring_matches_device_input(gpu_ctx):
