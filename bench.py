@@ -62,13 +62,8 @@ SPECTRAL_DRAM_BYTES_PER_ASCAN = (49.461504e6 + 11.174144e6) / 12000
 def config1_layout(seed=1, bscans=270):
     """Config-1 scan layout; `bscans` < 270 gives a small case of the same
     geometry (used for profiling captures)."""
-    from oct_recon_af_v1_gb300 import stitching as S
-    rng = np.random.default_rng(seed)
-    ty = int(bscans) * 1e-3                       # 1 um y pixels
-    lay = S.ScanLayout(np.array([-0.45, 0.45]), np.array([-0.45 * ty, 0.45 * ty]), np.array([0.0, 0.15, 0.30]),
-                       1000, int(bscans), 1.0, ty)
-    focus = 400.0 + rng.uniform(-30, 30, 3)
-    return lay, focus
+    from oct_recon_af_v1_gb300 import synthetic
+    return synthetic.config1_layout(seed, bscans)
 
 
 def config1_desc(bscans=270):

@@ -137,3 +137,16 @@ def u16_bits(t):
     values in [0, 65535]; pass it with raw_dtype=U16."""
     import torch
     return (t - 65536 * (t > 32767).to(t.dtype)).to(torch.int16)
+
+
+def config1_layout(seed: int = 1, bscans: int = 270):
+    """The tiled scan of the 2 x 2 tiles x 3 depths workload: tiles of 1000
+    A-scans x `bscans` B-scans at 1 um pixels, centres +-0.45 mm (10 % lateral
+    overlap), depths 0 / 0.15 / 0.30 mm, focus 400 + U[-30, 30] px per depth.
+    Returns (stitching.ScanLayout, focus pixels)."""
+    from .stitching import ScanLayout
+    rng = np.random.default_rng(seed)
+    ty = int(bscans) * 1e-3
+    lay = ScanLayout(np.array([-0.45, 0.45]), np.array([-0.45 * ty, 0.45 * ty]), np.array([0.0, 0.15, 0.30]),
+                     1000, int(bscans), 1.0, ty)
+    return lay, 400.0 + rng.uniform(-30, 30, 3)

@@ -168,6 +168,19 @@ def magnitude_numba(raw, g: Geometry, apod_size: int) -> np.ndarray:
     return np.abs(ft[..., : N // 2]).astype(np.float32, copy=False)
 
 
+def magnitude_numba_exact_fft(raw, g: Geometry, apod_size: int) -> np.ndarray:
+    """The Numba path's complex64 spectrum (core/cpu_kernels.py:12-41) through
+    an inverse FFT without float32 rounding (complex128), |.| rounded to
+    float32.  Against magnitude_numba this measures pocketfft's own float32
+    rounding (core/spectral.py:160-164): the deviation from the reference
+    path that any float32 FFT of another operation order starts from."""
+    N = len(g.lambda_nm)
+    spec = fused_pre_fft_numba(raw, apod_size, g.sinc_idx.T, g.sinc_w.T.astype(np.float32),
+                               g.window.astype(np.complex64))
+    ft = ifft_rows(spec.astype(np.complex128))
+    return np.abs(ft[..., : N // 2]).astype(np.float32)
+
+
 def linearise_numpy(raw, g: Geometry, apod_size: int, dtype) -> np.ndarray:
     """core/spectral.py:123-134 (the unfused NumPy path) at `dtype`."""
     x = np.asarray(raw).astype(dtype, copy=False)
@@ -385,6 +398,41 @@ def lsb_report(a_db, b_db, clim, floor_db=None):
     d = np.abs(qa - qb)[sel]
     return {"max_lsb": int(d.max()) if d.size else 0, "exact_frac": float((d == 0).mean()) if d.size else 1.0,
             "n": int(d.size)}
+
+
+# dB levels relative to the reference's median (deep noise floor to strong reflectors)
+DB_LEVELS = ((-np.inf, -30.0), (-30.0, -20.0), (-20.0, -10.0), (-10.0, 0.0), (0.0, 10.0), (10.0, np.inf))
+
+
+def lsb_levels(a_db, b_db, clim, levels=DB_LEVELS):
+    """Codes of a and b with ONE shared clim, compared per dB level of b
+    (relative to b's median over voxels finite in both).  Returns a list of
+    dict(lo, hi, n, exact_frac, max_lsb, n_diff), the overall row last
+    (lo = hi = None)."""
+    a_db, b_db = np.asarray(a_db), np.asarray(b_db)
+    qa = db_to_bits(a_db, clim).astype(np.int64)
+    qb = db_to_bits(b_db, clim).astype(np.int64)
+    sel = np.isfinite(a_db) & np.isfinite(b_db)
+    d = np.abs(qa - qb)[sel]
+    rel = np.asarray(b_db, np.float64)[sel]
+    rel = rel - np.median(rel)
+    rows = []
+    for lo, hi in tuple(levels) + ((None, None),):
+        m = np.ones(d.shape, bool) if lo is None else (rel >= lo) & (rel < hi)
+        dm = d[m]
+        rows.append({"lo": lo, "hi": hi, "n": int(dm.size), "n_diff": int((dm != 0).sum()),
+                     "exact_frac": float((dm == 0).mean()) if dm.size else 1.0,
+                     "max_lsb": int(dm.max()) if dm.size else 0})
+    return rows
+
+
+def format_levels(name, rows):
+    """One printable line per level table."""
+    out = [f"{name}:"]
+    for r in rows:
+        lvl = "all" if r["lo"] is None else f"[{r['lo']:g},{r['hi']:g}) dB"
+        out.append(f"  {lvl:>14s} n={r['n']:9d} exact={100 * r['exact_frac']:8.4f}% max={r['max_lsb']} LSB")
+    return "\n".join(out)
 
 
 # ----------------------------------------------------------------------------- estimation
