@@ -391,6 +391,9 @@ def gpu_arm(args, rank, world):
         line["cpu_baseline"] = cpu_baseline_config1(vol, torch, budget_s=args.cpu_budget)
         first = {k: vol.raw[(0,) + k][:1].cpu().numpy().view(np.uint16) for k in vol.order}
         line["cpu_numpy_path"] = numpy_path_baseline(vol, vol.tg, first, frames=1)
+    if rank == 0 and not args.no_plugin:
+        torch.cuda.synchronize()
+        line["plugin_process_row"] = plugin_arm(vol, torch, dev)
     if rank == 0 and not args.no_plain:
         torch.cuda.synchronize()
         pf = plain_form_arm(vol, torch, dev)
@@ -642,8 +645,9 @@ def config4_desc(n_train, n_base, epochs):
                         "focus ~ U[100, 900] px (reflector amplitude x exp(-((d - f)/150)^2)); 3 probe "
                         "reconstructions -> 256x256 dB images -> CNN",
             "held_out_bscans": 500, "ascans_per_bscan": 500, "training_images": n_train, "epochs": epochs,
-            "search": "per-B-scan: 41-point grid over +-1.2 x 7.5e7 nm^2/rad (one launch) + bounded Brent, "
-                      "top_percentile; focus: x-mean profile rules",
+            "search": "per-B-scan: 41-point grid over +-1.2 x 7.5e7 nm^2/rad (one launch) + batched zoom "
+                      "refinement (9 candidates per launch, to 2e-5 of the largest |bound|), top_percentile; "
+                      "focus: x-mean profile rules",
             "l2_flush": "held-out raw (1.05 GB) and magnitudes larger than L2"}
 
 
@@ -866,6 +870,110 @@ def _import_reference_octrecon():
     return sys.modules["octrecon"]
 
 
+def write_scan_folder(root: Path, vol, beta_ref: float):
+    """The tiled workload as an on-disk scan the reference's Reconstructor
+    opens: ScanInfo.json and, per tile, Header.xml (Thorlabs OCITY: 25
+    apodisation + 1000 scan lines of 2048 int16 samples, 270 B-scans) and
+    data/Chirp.data (the spectrometer's chirp: with the gan632 wavelength
+    range, chirp_j = q_j maps to the synthetic spectrometer's wavelengths).
+    The spectra themselves are served from memory (`_MemTileReader`)."""
+    from oct_recon_af_v1_gb300 import synthetic
+    lay = vol.lay
+    folders, gx, gy, gz = [], [], [], []
+    for yi, yc in enumerate(lay.y_centers_mm):
+        for xi, xc in enumerate(lay.x_centers_mm):
+            for zi, zd in enumerate(lay.z_depths_mm):
+                folders.append(f"Data{len(folders) + 1:02d}")
+                gx.append(float(xc)), gy.append(float(yc)), gz.append(float(zd))
+    info = {"octSystem": "gan632", "tissueRefractiveIndex": 1.33, "pixelSize_um": 1.0, "units": "mm",
+            "zDepths": [float(z) for z in lay.z_depths_mm], "xCenters_mm": [float(x) for x in lay.x_centers_mm],
+            "yCenters_mm": [float(y) for y in lay.y_centers_mm], "nXPixelsInEachTile": lay.n_x_px,
+            "nYPixelsInEachTile": lay.n_y_px, "tileRangeX_mm": lay.tile_range_x_mm,
+            "tileRangeY_mm": lay.tile_range_y_mm, "xOffset": 0, "yOffset": 0, "nBScanAvg": 1,
+            "galvoPhaseDelayXOffsetCorrection_mm": 0.0, "gridXcc": gx, "gridYcc": gy, "gridZcc": gz,
+            "scanOrder": list(range(1, len(folders) + 1)), "octFolders": folders,
+            "octProbe": {"DefaultDispersionQuadraticTerm": beta_ref,
+                         "OpticalPathCorrectionPolynomial": [0.0, 0.0, 0.0, 0.0, 0.0]}}
+    root.mkdir(parents=True, exist_ok=True)
+    (root / "ScanInfo.json").write_text(json.dumps(info, indent=1))
+    n, interf = 2048, APOD + lay.n_x_px
+    header = f"""<?xml version='1.0' encoding='utf-8'?>
+<Ocity version="1.0"><DataFiles>
+<DataFile Type="Raw" SizeZ="{n}" SizeX="{interf}" BytesPerPixel="2" ApoRegionStart0="0" ApoRegionEnd0="{APOD}" ScanRegionStart0="{APOD}" ScanRegionEnd0="{interf}" SizeY="{lay.n_y_px}">data\\Spectral0.data</DataFile>
+<DataFile Type="Real" SizeZ="{n}" BytesPerPixel="4">data\\Chirp.data</DataFile></DataFiles>
+<Image Type="RawSpectra"><SizePixel Unit="px"><SizeZ>{n // 2}</SizeZ><SizeX>{lay.n_x_px}</SizeX><SizeY>{lay.n_y_px}</SizeY></SizePixel>
+<SizeReal Unit="mm"><SizeZ>1.0</SizeZ><SizeX>{lay.tile_range_x_mm}</SizeX><SizeY>{lay.tile_range_y_mm}</SizeY></SizeReal></Image>
+<Acquisition><IntensityAveraging><Spectra>1</Spectra><AScans>1</AScans><BScans>1</BScans></IntensityAveraging>
+<SpeckleAveraging><FastAxis>1</FastAxis><SlowAxis>1</SlowAxis></SpeckleAveraging></Acquisition>
+<Instrument><Model>GAN632</Model><Series>Ganymede</Series><SpectrometerElements>{n}</SpectrometerElements></Instrument>
+</Ocity>"""
+    chirp = synthetic.raw_position(synthetic.SpectrumParams()).astype("<f4").tobytes()
+    for f in folders:
+        (root / f / "data").mkdir(parents=True, exist_ok=True)
+        (root / f / "Header.xml").write_text(header)
+        (root / f / "data" / "Chirp.data").write_bytes(chirp)
+    return folders
+
+
+def plugin_arm(vol, torch, dev, batch=30, io_threads=16):
+    """The drop-in path: the reference's own Reconstructor on device "gb300"
+    (octrecon/pipeline.py:95-302 with the plug-in registered), process_row of
+    both y-rows of the tiled workload, float32 dB planes back on the host.
+    The scan folder is written by `write_scan_folder`; its B-scans are served
+    from host memory by a reader whose read_bscans copies them into the
+    plug-in's pinned slots (as a read from the page cache would), so the
+    timed region holds that copy, the H2D copies, the kernels and the D2H of
+    the float32 planes (2 x 270 x nOutZ x nOutX)."""
+    import tempfile
+    if _import_reference_octrecon() is None:
+        return {"unavailable": "octrecon not installed in baseline/_ref"}
+    if not vol.host:
+        return {"unavailable": "needs the pinned host copy of the volume (run without --no-e2e)"}
+    from octrecon.io.volume import TileReader
+    from octrecon.pipeline import ReconConfig, Reconstructor
+
+    from oct_recon_af_v1_gb300 import plugin, synthetic
+    plugin.register(torch.cuda.current_device())
+
+    class _MemTileReader(TileReader):
+        """TileReader whose raw B-scans live in host memory."""
+
+        def __init__(self, tile_dir, data):
+            super().__init__(tile_dir)
+            self.data = data
+
+        def read_bscans(self, file_indices, out):
+            for k, fi in enumerate(file_indices):
+                np.copyto(out[k], self.data[int(fi)])
+            return out
+
+    beta = synthetic.beta_ref_from_px(1e-5)
+    root = Path(tempfile.mkdtemp(prefix="octgb_scan_"))
+    folders = write_scan_folder(root, vol, beta)
+    cfg = ReconConfig(volume_folder=str(root), device="gb300", precision="float32", dispersion_quadratic_term=beta,
+                      focus_positions=[float(f) for f in vol.focus], focus_sigma=80, crop_z_range_mm="none",
+                      output_pixel_size_um=1.0, n_medium=1.33, apply_path_length_correction=False,
+                      batch_frames=batch, io_threads=io_threads, write_tiff=False)
+    R = Reconstructor(cfg, log=lambda *a: None)
+    keys = [(yi, xi, zi) for yi in range(2) for xi in range(2) for zi in range(3)]
+    for f, k in zip(folders, keys):
+        R._readers[f] = _MemTileReader(root / f, vol.host[k].numpy())
+    for yi in range(2):                                         # warm-up: rings, plans, pinned results
+        R.process_row(yi)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    rows = [R.process_row(yi) for yi in range(2)]
+    dt = time.perf_counter() - t0
+    n_out = sum(int(r.size) for r in rows)
+    del rows
+    ascans = 12 * vol.ny * vol.lay.n_x_px
+    return {"value": ascans / dt, "unit": "A-scans/s", "ms_per_volume": dt * 1e3,
+            "h2d_bytes_per_volume": vol.raw_bytes(), "d2h_bytes_per_volume": 4 * n_out,
+            "batch_frames": batch, "io_threads": io_threads,
+            "source": "octrecon Reconstructor.process_row on device gb300 (reference pipeline, plug-in "
+                      "registered), both y-rows; reader serves the B-scans from host memory; float32 dB out"}
+
+
 def plain_form_arm(vol, torch, dev, batch=50):
     """The reference's own float32 GPU path, unmodified: octrecon's torch backend
     (TorchSpectralProcessor: gathers + torch.fft, TorchTileStitcher: gather +
@@ -1079,6 +1187,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip timing the reference's plain float32 GPU path")
+    ap.add_argument("--no-plugin", action="store_true", help="skip timing the reference's process_row on gb300")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--ref-frames", type=int, default=4)
     ap.add_argument("--batch", type=int, default=9, help="frames per frame batch")

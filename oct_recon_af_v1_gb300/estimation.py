@@ -5,9 +5,11 @@ Hann/rms-windows its B-scans once on the device (octgb_disp_load); every
 candidate beta then costs one phase multiply, inverse FFT and |.| per A-scan
 and a per-B-scan sharpness metric, all on the device (octgb_disp_eval), and a
 whole list of betas (the coarse grid) runs in one launch.  `search_dispersion`
-is the reference's search (dispersion.py:213-246): normalised coarse-grid
-curves, bounded scalar refinement of their mean (scipy's bounded Brent, the
-reference's optimiser), per-B-scan optima and their robust spread.
+keeps the reference's search (dispersion.py:213-246: normalised coarse-grid
+curves, refinement of their mean near the best grid point, per-B-scan optima
+and their robust spread) but refines in rounds of candidates scored in one
+launch each (`zoom_maximum`) where the reference calls scipy's sequential
+bounded Brent.
 
 Focus (octrecon/estimation/focus.py): the x-median depth profiles run on the
 device (octgb_xmedian); the 1-D rules on a profile of ~1000 pixels
@@ -124,45 +126,84 @@ class DispersionScorer:
         return self.ctx.disp_eval(betas, b0, nb, _METRIC_ID[self.metric], self.top_k, Z_MIN_PIX)
 
 
-def search_dispersion(scorer, lo: float, hi: float, initial: float, n_grid: int = 41) -> dict:
-    """The search of estimate_dispersion (dispersion.py:213-246) on any scorer:
-    coarse grid, each B-scan's curve normalised to [0, 1], bounded refinement of
-    the mean curve's maximum, per-B-scan optima.  Returns the result keys that
-    do not depend on the volume."""
-    from scipy.optimize import minimize_scalar
-
-    grid = np.linspace(lo, hi, int(n_grid))
+def scores_batch(scorer, betas, idx=None) -> np.ndarray:
+    """Scores of several betas, (len(betas), B) or (len(betas), 1): one
+    launch on a scorer with `scores_grid`, one call per beta otherwise."""
+    betas = np.asarray(betas, float)
     if hasattr(scorer, "scores_grid"):
-        S = np.asarray(scorer.scores_grid(grid), float)
-    else:
-        S = np.array([scorer.scores(b) for b in grid])
-    smin, smax = S.min(0), S.max(0)
-    rngs = np.where(smax > smin, smax - smin, 1.0)
-    Sn = (S - smin) / rngs
-    agg = Sn.mean(1)
-    gi = int(np.argmax(agg))
+        return np.asarray(scorer.scores_grid(betas, idx), float)
+    return np.array([scorer.scores(b, idx) for b in betas], float)
 
-    def bracket(i):
+
+def zoom_maximum(score, a: float, b: float, tol: float, points: int = 9):
+    """Maximum of a score on [a, b]: every round scores `points` equispaced
+    candidates at once (`score` takes an array of betas and returns their
+    scores), and the next round's bracket is the best candidate's two
+    neighbours, until candidates are at most `tol` apart.  The vertex of the
+    parabola through the last best candidate and its neighbours is scored
+    too and kept when it is better.  Returns (beta, score, rounds)."""
+    lo0, hi0 = float(a), float(b)
+    best_x, best_s, rounds = lo0, -np.inf, 0
+    while True:
+        xs = np.linspace(a, b, points)
+        sc = np.asarray(score(xs), float)
+        rounds += 1
+        i = int(np.argmax(sc))
+        if sc[i] > best_s:
+            best_x, best_s = float(xs[i]), float(sc[i])
+        h = (b - a) / (points - 1)
+        if h <= tol or points < 3:
+            break
+        a, b = max(xs[i] - h, lo0), min(xs[i] + h, hi0)
+    if 0 < i < points - 1:
+        y0, y1, y2 = sc[i - 1], sc[i], sc[i + 1]
+        curv = y0 - 2 * y1 + y2
+        if curv < 0:
+            v = float(xs[i] + 0.5 * h * (y0 - y2) / curv)
+            sv = float(np.asarray(score(np.array([v])), float)[0])
+            rounds += 1
+            if sv > best_s:
+                best_x, best_s = v, sv
+    return best_x, best_s, rounds
+
+
+def search_dispersion(scorer, lo: float, hi: float, initial: float, n_grid: int = 41, points: int = 9) -> dict:
+    """The dispersion search of estimate_dispersion (dispersion.py:213-246:
+    coarse grid, each B-scan's curve normalised to [0, 1] over the grid, the
+    maximum of their mean near the best grid point, each B-scan's own
+    optimum, the robust spread of those) with batched refinement: instead of
+    a sequential bounded Brent, `zoom_maximum` scores `points` candidates per
+    launch over the same bracket (the grid neighbours of the best point) and
+    stops at the same tolerance, 2e-5 of the largest |bound|."""
+    grid = np.linspace(lo, hi, int(n_grid))
+    S = scores_batch(scorer, grid)                          # (n_grid, B)
+    smin, span = S.min(axis=0), S.max(axis=0) - S.min(axis=0)
+    span = np.where(span > 0, span, 1.0)
+    curve = ((S - smin) / span).mean(axis=1)
+    g = int(np.argmax(curve))
+    tol = 2e-5 * max(abs(initial), abs(lo), abs(hi))
+
+    def around(i):
         return grid[max(i - 1, 0)], grid[min(i + 1, len(grid) - 1)]
 
-    tol = max(abs(initial), abs(lo), abs(hi)) * 2e-5
-    a, b = bracket(gi)
-    r = minimize_scalar(lambda x: -float(np.mean((scorer.scores(x) - smin) / rngs)), bounds=(a, b),
-                        method="bounded", options={"xatol": tol})
-    value = float(r.x) if -r.fun >= agg[gi] else float(grid[gi])
-    per = []
+    def mean_score(xs):
+        return ((scores_batch(scorer, xs) - smin) / span).mean(axis=1)
+
+    x, sx, rounds = zoom_maximum(mean_score, *around(g), tol, points)
+    value = x if sx >= curve[g] else float(grid[g])
+    per = np.empty(S.shape[1])
     for j in range(S.shape[1]):
         i = int(np.argmax(S[:, j]))
-        a, b = bracket(i)
-        rj = minimize_scalar(lambda x: -float(scorer.scores(x, j)[0]), bounds=(a, b), method="bounded",
-                             options={"xatol": tol})
-        per.append(float(rj.x) if -rj.fun >= S[i, j] else float(grid[i]))
-    per = np.array(per)
+        xj, sj, r = zoom_maximum(lambda xs, j=j: scores_batch(scorer, xs, j)[:, 0], *around(i), tol, points)
+        per[j] = xj if sj >= S[i, j] else float(grid[i])
+        rounds += r
+    med = float(np.median(per))
     step = (hi - lo) / (n_grid - 1)
-    return {"value": value, "candidates": grid, "score_curve": agg, "score_curves_per_bscan": Sn.T,
-            "scores": S, "per_bscan_values": per, "median_per_bscan": float(np.median(per)),
-            "spread_mad": float(1.4826 * np.median(np.abs(per - np.median(per)))),
-            "at_bound": bool(value <= lo + step or value >= hi - step), "n_evaluations": scorer.n_evals}
+    return {"value": float(value), "candidates": grid, "score_curve": curve, "score_curves_per_bscan": ((S - smin) / span).T,
+            "scores": S, "per_bscan_values": per, "median_per_bscan": med,
+            "spread_mad": float(1.4826 * np.median(np.abs(per - med))),
+            "at_bound": bool(value <= lo + step or value >= hi - step),
+            "n_evaluations": int(getattr(scorer, "n_evals", 0)), "refine_rounds": rounds}
 
 
 # --------------------------------------------------------------------------- focus helpers

@@ -260,12 +260,13 @@ def decode(pred):
 
 
 # --------------------------------------------------------------------------- the judge
-def search_per_bscan(scorer, lo: float, hi: float, n_grid: int = 41):
+def search_per_bscan(scorer, lo: float, hi: float, n_grid: int = 41, points: int = 9):
     """The plain search of every B-scan on its own: coarse grid (one launch for
-    all B-scans and betas), then each B-scan's bounded refinement around its
-    grid maximum - the per-B-scan part of estimate_dispersion
-    (dispersion.py:213-238), with bounds spanning 0 (dispersion.py:178-181)."""
-    from scipy.optimize import minimize_scalar
+    all B-scans and betas), then each B-scan's optimum between the grid
+    neighbours of its grid maximum, refined by rounds of `points` candidates
+    scored in one launch (estimation.zoom_maximum) to 2e-5 of the largest
+    |bound| - the per-B-scan part of estimate_dispersion (dispersion.py:
+    213-238), with bounds spanning 0 (dispersion.py:178-181)."""
     grid = np.linspace(lo, hi, int(n_grid))
     S_ = scorer.scores_grid(grid)
     tol = max(abs(lo), abs(hi)) * 2e-5
@@ -273,9 +274,8 @@ def search_per_bscan(scorer, lo: float, hi: float, n_grid: int = 41):
     for j in range(S_.shape[1]):
         i = int(np.argmax(S_[:, j]))
         a, b = grid[max(i - 1, 0)], grid[min(i + 1, len(grid) - 1)]
-        r = minimize_scalar(lambda x: -float(scorer.scores(x, j)[0]), bounds=(a, b), method="bounded",
-                            options={"xatol": tol})
-        out[j] = float(r.x) if -r.fun >= S_[i, j] else float(grid[i])
+        x, sx, _ = E.zoom_maximum(lambda xs, j=j: scorer.scores_grid(xs, j)[:, 0], a, b, tol, points)
+        out[j] = x if sx >= S_[i, j] else float(grid[i])
     return out, grid, S_
 
 

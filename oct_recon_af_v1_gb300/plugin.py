@@ -16,11 +16,14 @@ files, so `Reconstructor`, the CLI (`--set device=gb300`) and the web app
   stitching.py:84-120; self.oc: optical-path correction, :54-78) into an
   octgb context and binds `process_row` to the GB300 row engine below.
 * The bound `process_row` keeps the reference's contract (pipeline.py:223-302):
-  same arguments, threaded read-ahead of raw batches through the reference's
-  own readers, cancellation checked per batch (raises octrecon's Cancelled),
-  `on_batch(done, total)` callbacks, the `timers` keys, and returns float32 dB
-  (nFrames, nOutZ, nOutX) on the host.  Tiles are processed x-major/z-minor
-  and every batch is added in that order, as in the reference.
+  same arguments, cancellation checked per batch (raises octrecon's
+  Cancelled), `on_batch(done, total)` callbacks over the reference's (tile,
+  frame batch) jobs, the `timers` keys, and float32 dB (nFrames, nOutZ,
+  nOutX) on the host.  It runs on the frame API: the reference's readers
+  fill pinned host slots for a chunk of frames of every tile of the row,
+  copy streams carry them to the device and back, and one call per chunk
+  reconstructs and stitches all tiles with num/den on chip (`_RowRun`).
+  Each voxel sums its tiles x-major/z-minor, as the reference does.
 * Estimators asked for device gb300 (estimate_dispersion, detect_focus,
   octrecon/estimation) keep their host logic; their spectral processors and
   the DispersionScorer run on the GB300 kernels (`_register_estimators`).
@@ -41,7 +44,6 @@ Reconstructor construction fails with the library's error.
 from __future__ import annotations
 
 import time
-from collections import deque
 from concurrent.futures import ThreadPoolExecutor
 
 import numpy as np
@@ -234,19 +236,12 @@ class _RowEngine:
                 None if oc is None else oc.shift, None if oc is None else oc.pdz)
         from .stitching import min_weight_threshold
         self.threshold = min_weight_threshold(np.float32)
-        self._srr_buf = None
+        self.staging = None
 
-    def srr_raw(self, sw: _SrrWords):
-        """Device int16 (files, interf, n) of one batch of SRR words, in a
-        buffer reused batch after batch (every use is on the context's stream)."""
-        import torch
-        a0, a1 = sw.apod_range
-        s0, s1 = sw.scan_range
-        shape = (sw.words.shape[0], (a1 - a0) + (s1 - s0), sw.words.shape[2])
-        if self._srr_buf is None or tuple(self._srr_buf.shape) != shape:
-            self._srr_buf = torch.empty(shape, dtype=torch.int16, device=f"cuda:{self.ctx.device}")
-        return self.ctx.srr_decode(sw.words, sw.apod_range, sw.scan_range, out=self._srr_buf)
-
+    def ensure_staging(self, torch):
+        if self.staging is None:
+            self.staging = _Staging(torch, f"cuda:{self.ctx.device}")
+        return self.staging
 
 class _SrrWords:
     """The files of one batch as stored, (files, file_lines, n) uint16, and
@@ -284,76 +279,226 @@ def _attach(R, device_index: int) -> None:
 
 
 def _process_row(self, yi: int, frames=None, pool=None, on_batch=None):
-    """GB300 body of Reconstructor.process_row (octrecon/pipeline.py:223-302)."""
-    from octrecon.pipeline import Cancelled
-    eng = self._gb300
-    cfg, hdr = self.cfg, self.hdr
-    frames = np.arange(self.si.n_y_px) if frames is None else np.asarray(frames)
-    nF = len(frames)
-    _, nz_out, nx_out = self.n_out
-    B = cfg.batch_frames
-    jobs = []
-    for t in self.si.tiles_in_row(yi):
-        if self.stitchers[(t.xi, t.zi)].empty:
-            continue
-        for s in range(0, nF, B):
-            jobs.append((t, s, frames[s:s + B]))
+    """GB300 body of Reconstructor.process_row (octrecon/pipeline.py:223-302):
+    same arguments, float32 dB (nFrames, nOutZ, nOutX) on the host, per-batch
+    cancellation (octrecon's Cancelled), on_batch(done, total) over the
+    reference's (tile, frame batch) jobs, and its timer keys."""
+    return _RowRun(self, yi, frames, pool, on_batch).run()
 
-    def read_job(job):
-        t, s, fr = job
-        files = [f for fr_ in fr for f in self.frame_files(int(fr_))]
-        rd = self.reader(t.folder)
-        if _is_srr(rd):
-            return _srr_words(rd, files, hdr.n_lambda)
-        buf = np.empty((len(files), hdr.interf_size, hdr.n_lambda), np.dtype(hdr.raw_dtype))
-        rd.read_bscans(files, buf)
-        return buf
 
-    ctx = eng.ctx
-    ctx.row_begin(nF, nz_out, nx_out)
-    own_pool = pool is None
-    pool = pool or ThreadPoolExecutor(cfg.io_threads)
-    pending = deque()
-    it = iter(jobs)
-    for _ in range(self.prefetch):
-        j = next(it, None)
-        if j is None:
-            break
-        pending.append((j, pool.submit(read_job, j)))
-    n_done = 0
-    try:
-        while pending:
-            if self.cancel.is_set():
-                raise Cancelled()
-            job, fut = pending.popleft()
-            t0 = time.perf_counter()
-            raw = fut.result()
-            t1 = time.perf_counter()
-            self.timers["io_wait"] += t1 - t0
-            nxt = next(it, None)
-            if nxt is not None:
-                pending.append((nxt, pool.submit(read_job, nxt)))
-            t, s, fr = job
-            if isinstance(raw, _SrrWords):
-                raw = eng.srr_raw(raw)
-            # spectral stage + stitching + accumulation of this batch on the device
-            if eng.rare:
-                ctx.row_add_batch_ex(eng.plans[(t.xi, t.zi)], raw, hdr.apod_size, fr, s, eng.binning, eng.apod_mode,
-                                     eng.bscan_avg, eng.ascan_avg)
-            else:
-                ctx.row_add_batch(eng.plans[(t.xi, t.zi)], raw, hdr.apod_size, fr, s)
-            t2 = time.perf_counter()
-            self.timers["spectral"] += t2 - t1
-            n_done += 1
-            if on_batch:
-                on_batch(n_done, len(jobs))
-    finally:
-        if own_pool:
-            pool.shutdown(wait=True, cancel_futures=True)
-        else:
-            for _, f in pending:
-                f.cancel()
-    t0 = time.perf_counter()
-    out = ctx.row_finalise(eng.threshold, (nF, nz_out, nx_out))
-    self.timers["finalise"] += time.perf_counter() - t0
+def _frame_chunks(frames: np.ndarray, batch: int):
+    """(output offset, frames) of consecutive-valued runs of at most `batch`
+    frames (the frame API takes frames f0 .. f0 + B - 1 in one call)."""
+    out, start = [], 0
+    for i in range(1, len(frames) + 1):
+        if i == len(frames) or frames[i] != frames[i - 1] + 1 or i - start == batch:
+            out.append((start, frames[start:i]))
+            start = i
     return out
+
+
+class _Staging:
+    """Rings of the row pipeline, kept by the engine across rows and grown on
+    demand: pinned host slots the readers fill (one per chunk in flight) and
+    the device slots they are copied to.  Events order every reuse."""
+
+    def __init__(self, torch, device: str, depth: int = 3):
+        self.torch, self.device, self.depth = torch, device, depth
+        self.host = [None] * depth
+        self.dev = [None] * depth
+        self.copied = [torch.cuda.Event() for _ in range(depth)]     # host slot free again
+        self.consumed = [torch.cuda.Event() for _ in range(depth)]   # device slot free again
+        self.h2d = torch.cuda.Stream(device)
+        self.d2h = torch.cuda.Stream(device)
+        self.compute = torch.cuda.Stream(device)
+
+    def _fit(self, bufs, k, numel, dtype, **kw):
+        b = bufs[k]
+        if b is None or b.numel() < numel or b.dtype != dtype:
+            bufs[k] = b = self.torch.empty(numel, dtype=dtype, **kw)
+        return b[:numel]
+
+    def host_slot(self, k, numel, dtype):
+        return self._fit(self.host, k, numel, dtype, pin_memory=True)
+
+    def dev_slot(self, k, numel, dtype):
+        return self._fit(self.dev, k, numel, dtype, device=self.device)
+
+
+_TORCH_RAW = {"uint16": "int16", "int16": "int16", "float32": "float32"}
+
+
+class _RowRun:
+    """One process_row call.  The unit of work is a chunk of consecutive frames
+    over every non-empty tile of the y-row (x-major, z-minor: the order the
+    tiles are summed in, as in the reference).  The I/O pool reads a chunk's
+    raw B-scans straight into a pinned host slot while earlier chunks are on
+    the device; a copy stream moves the slot to a device slot; one
+    octgb_frames_process call reconstructs the chunk (spectral stage, focus-
+    weighted stitching and finalise with num/den on chip) into the device row;
+    its planes return through a pinned output slot on a third stream.  Rare
+    formats (binning, frame-mean background, repeats) add each tile of a
+    chunk through the row API instead, and finalise once."""
+
+    def __init__(self, R, yi, frames, pool, on_batch):
+        import torch
+        self.torch, self.R, self.eng = torch, R, R._gb300
+        self.hdr, self.cfg = R.hdr, R.cfg
+        self.frames = np.arange(R.si.n_y_px) if frames is None else np.asarray(frames)
+        self.tiles = [t for t in R.si.tiles_in_row(yi) if not R.stitchers[(t.xi, t.zi)].empty]
+        self.chunks = _frame_chunks(self.frames, max(1, int(self.cfg.batch_frames)))
+        self.pool, self.on_batch = pool, on_batch
+        self.n_jobs = len(self.tiles) * len(self.chunks)
+        self.srr = bool(self.tiles) and _is_srr(R.reader(self.tiles[0].folder))
+        self.files_per_frame = max(1, int(self.hdr.bscan_avg))
+        self.raw_np = np.dtype(self.hdr.raw_dtype)
+
+    # ---- reads (I/O threads) ---------------------------------------------
+    def _files(self, fr):
+        return [f for v in fr for f in self.R.frame_files(int(v))]
+
+    def _slot_view(self, k, n_files):
+        """Pinned host slot k as (tiles, files, interf, n) in the raw dtype, and
+        the torch tensor behind it."""
+        per_tile = n_files * self.hdr.interf_size * self.hdr.n_lambda
+        slot = self.eng.staging.host_slot(k, per_tile * len(self.tiles),
+                                          getattr(self.torch, _TORCH_RAW[self.raw_np.name]))
+        view = slot.numpy().view(self.raw_np).reshape(len(self.tiles), n_files, self.hdr.interf_size,
+                                                      self.hdr.n_lambda)
+        return slot, view
+
+    def _read_tile(self, k, chunk, j):
+        """One tile's raw B-scans of a chunk: into pinned slot k (regular
+        readers; the slot's previous chunk has left for the device first), or
+        the SRR words as stored."""
+        files = self._files(chunk[1])
+        t = self.tiles[j]
+        if self.srr:
+            return _srr_words(self.R.reader(t.folder), files, self.hdr.n_lambda)
+        self.eng.staging.copied[k].synchronize()
+        _, view = self._slot_view(k, len(files))
+        self.R.reader(t.folder).read_bscans(files, view[j])
+        return None
+
+    def _submit_reads(self, pool, k, chunk):
+        if not self.srr:
+            self._slot_view(k, len(self._files(chunk[1])))       # size the slot once, before the tile jobs
+        return [pool.submit(self._read_tile, k, chunk, j) for j in range(len(self.tiles))]
+
+    def _wait_reads(self, k, chunk, futures):
+        got = [f.result() for f in futures]
+        return got if self.srr else self._slot_view(k, len(self._files(chunk[1])))[0]
+
+    # ---- device side (the calling thread) ----------------------------------
+    def _device_raws(self, k, chunk, got):
+        """The chunk's raws as device tensors (B files, interf, n), one per tile."""
+        torch, st, eng = self.torch, self.eng.staging, self.eng
+        n_files = len(chunk[1]) * self.files_per_frame
+        shape = (n_files, self.hdr.interf_size, self.hdr.n_lambda)
+        if self.srr:
+            raws = []
+            for j, words in enumerate(got):
+                a0, a1 = words.apod_range
+                s0, s1 = words.scan_range
+                n_lines = (a1 - a0) + (s1 - s0)
+                dev = st.dev_slot(k, len(got) * n_files * n_lines * self.hdr.n_lambda, torch.int16)
+                one = dev.view(len(got), n_files, n_lines, self.hdr.n_lambda)[j]
+                eng.ctx.srr_decode(words.words, words.apod_range, words.scan_range, out=one)
+                raws.append(one)
+            return raws
+        dev = st.dev_slot(k, got.numel(), got.dtype)
+        st.h2d.wait_event(st.consumed[k])
+        with torch.cuda.stream(st.h2d):
+            dev.copy_(got, non_blocking=True)
+        st.copied[k].record(st.h2d)
+        st.compute.wait_event(st.copied[k])
+        return list(dev.view((len(self.tiles),) + shape))
+
+    def run(self):
+        from octrecon.pipeline import Cancelled
+        torch, R, eng = self.torch, self.R, self.eng
+        nF = len(self.frames)
+        _, nz, nx = R.n_out
+        if not self.tiles:
+            return np.full((nF, nz, nx), np.nan, np.float32)
+        eng.ensure_staging(torch)
+        st = eng.staging
+        ctx = eng.ctx
+        # the result lives in pinned memory, so each chunk's planes go to the
+        # host by DMA while later chunks reconstruct (torch's pinned-memory
+        # cache recycles it once the caller drops the array)
+        host_out = torch.empty((nF, nz, nx), dtype=torch.float32, pin_memory=True)
+        out = host_out.numpy()
+        dtype = 1 if self.srr else (0 if self.raw_np == np.uint16 else (1 if self.raw_np == np.int16 else 2))
+        ids = [eng.plans[(t.xi, t.zi)] for t in self.tiles]
+        apod = int(self.hdr.apod_size)
+        own_pool = self.pool is None
+        pool = self.pool or ThreadPoolExecutor(self.cfg.io_threads)
+        depth = st.depth
+        reads = {}
+        with torch.cuda.device(st.device):
+            prev_stream = torch.cuda.current_stream()
+            torch.cuda.set_stream(st.compute)
+            ctx.follow_torch_stream()
+            try:
+                if eng.rare:
+                    ctx.row_begin(nF, nz, nx)
+                else:
+                    row = torch.empty((nF, nz, nx), dtype=torch.float32, device=st.device)
+                for c in range(min(depth, len(self.chunks))):
+                    reads[c] = self._submit_reads(pool, c % depth, self.chunks[c])
+                done = 0
+                for c, chunk in enumerate(self.chunks):
+                    if R.cancel.is_set():
+                        raise Cancelled()
+                    k = c % depth
+                    t0 = time.perf_counter()
+                    got = self._wait_reads(k, chunk, reads.pop(c))
+                    t1 = time.perf_counter()
+                    R.timers["io_wait"] += t1 - t0
+                    raws = self._device_raws(k, chunk, got)
+                    t2 = time.perf_counter()
+                    R.timers["h2d"] += t2 - t1
+                    off, fr = chunk
+                    if eng.rare:
+                        for pid, raw in zip(ids, raws):
+                            ctx.row_add_batch_ex(pid, raw, apod, fr, off, eng.binning, eng.apod_mode,
+                                                 eng.bscan_avg, eng.ascan_avg, raw_dtype=dtype)
+                    else:
+                        planes = row[off:off + len(fr)]
+                        ctx.frames_process(ids, raws, apod, int(fr[0]), nz, nx, eng.threshold, out=planes,
+                                           raw_dtype=dtype)
+                        st.d2h.wait_stream(st.compute)
+                        with torch.cuda.stream(st.d2h):
+                            host_out[off:off + len(fr)].copy_(planes, non_blocking=True)
+                    st.consumed[k].record(st.compute)
+                    R.timers["spectral"] += time.perf_counter() - t2
+                    if c + depth < len(self.chunks):
+                        reads[c + depth] = self._submit_reads(pool, k, self.chunks[c + depth])
+                    done += len(self.tiles)
+                    if self.on_batch:
+                        self.on_batch(done, self.n_jobs)
+                t0 = time.perf_counter()
+                if eng.rare:
+                    ctx.row_finalise(eng.threshold, (nF, nz, nx), out)
+                st.d2h.synchronize()
+                R.timers["finalise"] += time.perf_counter() - t0
+            finally:
+                left = [f for fs in reads.values() for f in fs]
+                for f in left:
+                    f.cancel()
+                if own_pool:
+                    pool.shutdown(wait=True, cancel_futures=True)
+                # reads still running would write into the rings: let them end
+                for f in left:
+                    if not f.cancelled():
+                        try:
+                            f.result()
+                        except Exception:
+                            pass
+                st.compute.synchronize()
+                st.h2d.synchronize()
+                st.d2h.synchronize()
+                torch.cuda.set_stream(prev_stream)
+                ctx.set_stream(None)
+        return out

@@ -38,22 +38,71 @@ def factor_z(n_rows: int, focus_pix_1based: float, focus_sigma: float) -> np.nda
     return np.exp(-((z - focus_pix_1based) ** 2) / (2.0 * focus_sigma) ** 2) + MIN_WEIGHT
 
 
+@dataclass
+class Resampling:
+    """MATLAB linear interpolation with 0 outside (interp1 / interp2
+    'linear'), from strictly increasing source nodes to destination points,
+    as a 2-tap plan: destination rows[k] = (1 - t[k]) v[j[k]] + t[k] v[j[k] + 1].
+    A destination within 1e-9 (relative position) of a node takes the node
+    value exactly, as MATLAB does.  This is the form the device applies; the
+    dense matrix, the source rows and destination columns a tile touches
+    follow from it."""
+    rows: np.ndarray       # destination indices inside [src[0], src[-1]]
+    j: np.ndarray          # left source node of each
+    t: np.ndarray          # fraction towards the right node
+    n_src: int
+    n_dst: int
+
+    @classmethod
+    def between(cls, src, dst) -> "Resampling":
+        src = np.asarray(src, float)
+        dst = np.asarray(dst, float)
+        rows = np.flatnonzero((dst >= src[0]) & (dst <= src[-1]))
+        q = dst[rows]
+        j = np.clip(np.searchsorted(src, q, side="right") - 1, 0, len(src) - 2)
+        t = (q - src[j]) / (src[j + 1] - src[j])
+        t = np.where(np.abs(t) < 1e-9, 0.0, t)
+        t = np.where(np.abs(1.0 - t) < 1e-9, 1.0, t)
+        return cls(rows, j, t, len(src), len(dst))
+
+    def dense(self) -> np.ndarray:
+        """W (n_dst, n_src) with W @ v the interpolated values."""
+        W = np.zeros((self.n_dst, self.n_src))
+        W[self.rows, self.j] += 1.0 - self.t
+        W[self.rows, self.j + 1] += self.t
+        return W
+
+    def sources_used(self) -> np.ndarray:
+        """Source nodes that carry a non-zero weight, increasing."""
+        left = self.j[(1.0 - self.t) != 0]
+        right = self.j[self.t != 0] + 1
+        return np.unique(np.concatenate([left, right]))
+
+    def targets_used(self) -> np.ndarray:
+        """Destination points with a non-zero weight, increasing."""
+        return self.rows[((1.0 - self.t) != 0) | (self.t != 0)]
+
+
+def _placed_depths(tile_z_mm: np.ndarray, z_depth_mm: float, focus_pix: float) -> np.ndarray:
+    """Tile rows in the output depth frame: the tile's depth added, then the
+    focus row's own position subtracted (no shift without a focus)."""
+    z = tile_z_mm + z_depth_mm
+    return z if np.isnan(focus_pix) else z - tile_z_mm[int(np.round(focus_pix)) - 1]
+
+
+def _edge_widened(nodes: np.ndarray) -> np.ndarray:
+    """A copy of increasing nodes with the first moved 1e-10 down and the last
+    1e-10 up."""
+    out = np.array(nodes, float, copy=True)
+    out[0] -= 1e-10
+    out[-1] += 1e-10
+    return out
+
+
 def linear_interp_matrix(src: np.ndarray, dst: np.ndarray) -> np.ndarray:
-    """Dense W (len(dst), len(src)) with W @ v = interp1(src, v, dst, 'linear', 0)
-    for strictly increasing src; queries within 1e-9 (relative position) of a
-    node take the node value exactly, as MATLAB's interp2 does."""
-    src = np.asarray(src, float)
-    dst = np.asarray(dst, float)
-    W = np.zeros((len(dst), len(src)))
-    rows = np.flatnonzero((dst >= src[0]) & (dst <= src[-1]))
-    q = dst[rows]
-    j = np.clip(np.searchsorted(src, q, side="right") - 1, 0, len(src) - 2)
-    t = (q - src[j]) / (src[j + 1] - src[j])
-    t = np.where(np.abs(t) < 1e-9, 0.0, t)
-    t = np.where(np.abs(1.0 - t) < 1e-9, 1.0, t)
-    np.add.at(W, (rows, j), 1.0 - t)
-    np.add.at(W, (rows, j + 1), t)
-    return W
+    """Dense W (len(dst), len(src)) of Resampling.between(src, dst)
+    (octrecon/core/stitching.py:36-51)."""
+    return Resampling.between(src, dst).dense()
 
 
 @dataclass
@@ -66,12 +115,25 @@ class OpticalPathCorrection:
 
     @classmethod
     def build(cls, poly, tile_x_mm, tile_y_mm, tile_z_mm):
-        x, y, z = tile_x_mm * 1e3, tile_y_mm * 1e3, tile_z_mm * 1e3
-        dz = (z[-1] - z[0]) / (len(z) - 1)
+        """poly = (p1 .. p5) in um over the tile's x / y pixels (um); the
+        shift is in z pixels of the tile (octrecon/core/stitching.py:67-78)."""
+        to_um = 1e3
+        x, y, z = tile_x_mm * to_um, tile_y_mm * to_um, tile_z_mm * to_um
+        z_step = (z[-1] - z[0]) / (len(z) - 1)
         X, Y = np.meshgrid(x, y)
-        P = poly[0] * X + poly[1] * Y + poly[2] * X ** 2 + poly[3] * Y ** 2 + poly[4] * X * Y
-        pdz = P / dz
-        return cls(np.floor(pdz + 0.5).astype(np.int64), pdz, len(z))
+        rows = _path_surface(poly, X, Y) / z_step
+        return cls(np.floor(rows + 0.5).astype(np.int64), rows, len(z))
+
+
+def _path_surface(poly, X, Y):
+    """Optical path P(x, y) = p1 x + p2 y + p3 x^2 + p4 y^2 + p5 x y, the terms
+    summed left to right and the cross term formed as (p5 x) y: the float64
+    evaluation order the reference's expression has, so P is bit-identical."""
+    terms = (poly[0] * X, poly[1] * Y, poly[2] * X ** 2, poly[3] * Y ** 2, poly[4] * X * Y)
+    total = terms[0]
+    for term in terms[1:]:
+        total = total + term
+    return total
 
 
 @dataclass
@@ -102,49 +164,74 @@ class TiledGeometry:
     focus_pix: np.ndarray
 
 
+def _tile_pixels(offset: float, extent_mm: float, n: int) -> np.ndarray:
+    """Positions (mm) of a tile's n pixels along one lateral axis: n + 1
+    MATLAB-linspace edges over the extent, centred on `offset`, the last edge
+    dropped (yOCTProcessTiledScan_createDimStructure)."""
+    return (offset + extent_mm * linspace_matlab(-0.5, 0.5, n + 1))[:-1]
+
+
+def _covering_grid(centres: np.ndarray, local: np.ndarray, step: float) -> np.ndarray:
+    """The grid (MATLAB colon, pitch `step`) from the first pixel of the lowest
+    tile to the last pixel of the highest one, half a step of slack at the
+    end (yOCTProcessTiledScan.m 171-185)."""
+    return colon_matlab(centres.min() + local[0], step, centres.max() + local[-1] + step / 2)
+
+
+def _focus_reference(focus: np.ndarray, depths_mm: np.ndarray) -> float:
+    """The focus pixel the tile z axis is zeroed at: the common one, or the
+    one of the depth closest to 0."""
+    return focus[0] if np.all(focus == focus[0]) else focus[int(np.argmin(np.abs(depths_mm)))]
+
+
+def _pixel_pitch_um(grid_mm: np.ndarray) -> float:
+    """Mean pitch of an output grid in um, rounded to 0.01 um."""
+    return np.round(np.mean(np.diff(grid_mm)) * 1e3 * 100) / 100
+
+
 def tiled_geometry(si: ScanLayout, z_um_tile, focus_pix, output_pixel_size_um=None,
                    crop_z_range_mm=None) -> TiledGeometry:
-    """Tile-local and output grids (yOCTProcessTiledScan_createDimStructure and
-    yOCTProcessTiledScan.m 171-222; reference octrecon/core/geometry.py:146-202)."""
-    zd = np.asarray(si.z_depths_mm, float)
-    xc = np.asarray(si.x_centers_mm, float)
-    yc = np.asarray(si.y_centers_mm, float)
+    """Tile-local and output grids of a tiled scan (yOCTProcessTiledScan_
+    createDimStructure and yOCTProcessTiledScan.m 171-222; reference
+    octrecon/core/geometry.py:146-202).  The grids are built per axis: tile
+    pixels, the covering output grid, then z re-zeroed at the focus, resampled
+    to the output pixel size and cropped."""
+    depths = np.asarray(si.z_depths_mm, float)
+    x_centres = np.asarray(si.x_centers_mm, float)
+    y_centres = np.asarray(si.y_centers_mm, float)
     focus = np.asarray(focus_pix, float).ravel()
     if focus.size == 1:
-        focus = np.full(len(zd), focus[0])
-    if focus.size != len(zd):
+        focus = np.full(len(depths), focus[0])
+    if focus.size != len(depths):
         raise ValueError("focus_pix must be scalar or one value per zDepth")
-    tx = (si.x_offset + si.tile_range_x_mm * linspace_matlab(-0.5, 0.5, si.n_x_px + 1))[:-1] - si.x_shift_mm
-    ty = (si.y_offset + si.tile_range_y_mm * linspace_matlab(-0.5, 0.5, si.n_y_px + 1))[:-1]
-    tz = np.asarray(z_um_tile, float) / 1e3
+    # lateral axes: tile pixels and the grid covering every tile centre
+    tile_x = _tile_pixels(si.x_offset, si.tile_range_x_mm, si.n_x_px) - si.x_shift_mm
+    tile_y = _tile_pixels(si.y_offset, si.tile_range_y_mm, si.n_y_px)
+    out_x = tile_x.copy() if len(x_centres) == 1 else _covering_grid(x_centres, tile_x, tile_x[1] - tile_x[0])
+    y_step = tile_y[1] - tile_y[0] if len(tile_y) > 1 else 0.0
+    out_y = tile_y.copy() if len(y_centres) == 1 else _covering_grid(y_centres, tile_y, y_step)
+    # depth: the tile axis zeroed at the focus row, the covering grid zeroed at
+    # its sample closest to 0
+    tile_z = np.asarray(z_um_tile, float) / 1e3
     if not np.any(np.isnan(focus)):
-        ref = focus[0] if np.all(focus == focus[0]) else focus[int(np.argmin(np.abs(zd)))]
-        tz = tz - tz[int(np.round(ref)) - 1]
-    dx = tx[1] - tx[0]
-    dy = ty[1] - ty[0] if len(ty) > 1 else 0.0
-    dz = tz[1] - tz[0]
-    x_all = colon_matlab(xc.min() + tx[0], dx, xc.max() + tx[-1] + dx / 2)
-    y_all = colon_matlab(yc.min() + ty[0], dy, yc.max() + ty[-1] + dy / 2)
-    z_all = colon_matlab(zd.min() + tz[0], dz, zd.max() + tz[-1] + dz / 2)
-    zero = int(np.argmin(np.abs(z_all)))
-    z_all = dz * (np.arange(1, len(z_all) + 1) - (zero + 1))
-    if len(xc) == 1:
-        x_all = tx.copy()
-    if len(yc) == 1:
-        y_all = ty.copy()
+        tile_z = tile_z - tile_z[int(np.round(_focus_reference(focus, depths))) - 1]
+    z_step = tile_z[1] - tile_z[0]
+    cover_z = _covering_grid(depths, tile_z, z_step)
+    zero = int(np.argmin(np.abs(cover_z)))
+    out_z = z_step * (np.arange(1, len(cover_z) + 1) - (zero + 1))
     if output_pixel_size_um is not None:
-        px = np.round(np.mean(np.diff(x_all)) * 1e3 * 100) / 100
-        py = np.round(np.mean(np.diff(y_all)) * 1e3 * 100) / 100 if len(y_all) >= 2 else px
-        if not (px == py == output_pixel_size_um):
+        pitch_x = _pixel_pitch_um(out_x)
+        pitch_y = _pixel_pitch_um(out_y) if len(out_y) >= 2 else pitch_x
+        if not (pitch_x == pitch_y == output_pixel_size_um):
             raise ValueError(f"output pixel size {output_pixel_size_um} um must equal the scan pixel size "
-                             f"({px}, {py}) um")
-        z_all = colon_matlab(z_all[0], output_pixel_size_um * 1e-3, z_all.max())
+                             f"({pitch_x}, {pitch_y}) um")
+        out_z = colon_matlab(out_z[0], output_pixel_size_um * 1e-3, out_z.max())
     if crop_z_range_mm is not None and len(crop_z_range_mm):
         lo, hi = crop_z_range_mm
-        z_all = z_all[~((z_all < lo) | (z_all > hi))]
-        if z_all.size == 0:
+        out_z = out_z[~((out_z < lo) | (out_z > hi))]
+        if out_z.size == 0:
             raise ValueError("crop_z_range_mm does not overlap the available z range")
-    return TiledGeometry(tx, ty, tz, x_all, y_all, z_all, focus)
+    return TiledGeometry(tile_x, tile_y, tile_z, out_x, out_y, out_z, focus)
 
 
 @dataclass
@@ -165,29 +252,26 @@ class TileStitcher:
     @classmethod
     def build(cls, tg: TiledGeometry, xi_center_mm: float, z_depth_mm: float, focus_pix: float,
               focus_sigma: float, dtype=np.float32) -> "TileStitcher":
-        nz = len(tg.tile_z_mm)
-        x = tg.tile_x_mm + xi_center_mm
-        z = tg.tile_z_mm + z_depth_mm
-        if not np.isnan(focus_pix):
-            z = z - tg.tile_z_mm[int(np.round(focus_pix)) - 1]
-        x = x.copy()
-        z = z.copy()
-        # widen the end nodes so output points on the tile edge stay inside
-        x[0] -= 1e-10
-        x[-1] += 1e-10
-        z[0] -= 1e-10
-        z[-1] += 1e-10
-        Wz = linear_interp_matrix(z, tg.out_z_mm)
-        Wx = linear_interp_matrix(x, tg.out_x_mm)
-        rows = np.flatnonzero(Wz.any(axis=0))
-        cols = np.flatnonzero(Wx.any(axis=1))
+        """The tile at lateral centre xi_center_mm and depth z_depth_mm
+        (octrecon/core/stitching.py:84-120): its pixels placed in the output
+        frame (z shifted so the focus row sits at the tile's depth), the end
+        nodes widened by 1e-10 mm so output points on a tile edge stay inside,
+        then one 2-tap resampling plan per axis; the source rows the depth
+        plan touches give r0:r1, the output columns the lateral plan reaches
+        give c0:c1."""
+        depth_nodes = _edge_widened(_placed_depths(tg.tile_z_mm, z_depth_mm, focus_pix))
+        lateral_nodes = _edge_widened(tg.tile_x_mm + xi_center_mm)
+        along_z = Resampling.between(depth_nodes, tg.out_z_mm)
+        along_x = Resampling.between(lateral_nodes, tg.out_x_mm)
+        rows, cols = along_z.sources_used(), along_x.targets_used()
         if rows.size == 0 or cols.size == 0:
             return cls(empty=True)
         r0, r1 = int(rows[0]), int(rows[-1]) + 1
         c0, c1 = int(cols[0]), int(cols[-1]) + 1
-        fz = factor_z(nz, focus_pix, focus_sigma) if not np.isnan(focus_pix) else np.ones(nz)
-        return cls(False, r0, r1, c0, c1, Wz[:, r0:r1].astype(dtype), Wx[c0:c1, :].T.astype(dtype),
-                   fz[r0:r1].astype(dtype), nz)
+        n_rows = len(tg.tile_z_mm)
+        weight = factor_z(n_rows, focus_pix, focus_sigma) if not np.isnan(focus_pix) else np.ones(n_rows)
+        return cls(False, r0, r1, c0, c1, along_z.dense()[:, r0:r1].astype(dtype),
+                   along_x.dense()[c0:c1, :].T.astype(dtype), weight[r0:r1].astype(dtype), n_rows)
 
     def upload(self, ctx, oc: OpticalPathCorrection | None = None) -> int:
         if self.empty:

@@ -60,9 +60,11 @@ def test_per_bscan_search_finds_known_optima():
             o = opt if idx is None else opt[idx:idx + 1]
             return -((beta - o) / 1e7) ** 2
 
-        def scores_grid(self, betas):
-            return np.stack([self.scores(b) for b in betas])
+        def scores_grid(self, betas, idx=None):
+            return np.stack([self.scores(b, idx) for b in betas])
 
     got, grid, S = L.search_per_bscan(Quad(), -8e7, 8e7, 41)
     assert S.shape == (41, 4)
-    np.testing.assert_allclose(got, opt, rtol=0, atol=8e7 * 2e-5 * 2)
+    # the zoom stops at candidates 2e-5 x 8e7 apart; the parabolic step lands
+    # on a quadratic's vertex
+    np.testing.assert_allclose(got, opt, rtol=0, atol=1.0)
