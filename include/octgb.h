@@ -271,6 +271,19 @@ int octgb_quantise_running(octgb_ctx *ctx, const float *db, int64_t n, int db_lo
 int octgb_graph_begin(octgb_ctx *ctx);
 int octgb_graph_end(octgb_ctx *ctx, int *graph_id);
 int octgb_graph_launch(octgb_ctx *ctx, int graph_id);
+/* Self-test of the bounded device waits (no counterpart in the reference):
+ * runs the spectral kernel (which = 0) or the precision form's tensor-core
+ * sinc (which = 1, integer raws; needs a geometry with precision tiles) on a
+ * small internal batch of zero raws, with the waits' limit cut to
+ * wait_limit_us (100 .. 2 000 000) and each CTA's first bulk-copy barrier
+ * expecting 16 bytes more than its copies deliver.  Every copy still lands;
+ * only that barrier never completes, so the wait runs out, the kernel drains
+ * what it issued (and frees its tensor memory) and reports through the status
+ * word.  Returns OCTGB_ERR_TIMEOUT when that happened (the expected result),
+ * OCTGB_ERR_STATE if the wait did not expire; the limit and switch are
+ * restored either way and the context stays usable. */
+int octgb_selftest_wait_expiry(octgb_ctx *ctx, int which, int wait_limit_us);
+
 /* Destroy every graph captured on the context (after the work already
  * launched has completed); their ids become invalid and octgb_set_geometry is
  * accepted again.  No counterpart in the reference (its loop has no graphs). */

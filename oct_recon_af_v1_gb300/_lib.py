@@ -50,6 +50,7 @@ SIGNATURES = {
     "octgb_graph_end": (c_int, [c_void_p, POINTER(c_int)]),
     "octgb_graph_launch": (c_int, [c_void_p, c_int]),
     "octgb_graphs_release": (c_int, [c_void_p]),
+    "octgb_selftest_wait_expiry": (c_int, [c_void_p, c_int, c_int]),
     "octgb_magnitude_noalloc": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_void_p]),
     "octgb_batch_process": (c_int, [c_void_p, c_int, c_void_p, c_int, c_float, c_int]),
     "octgb_disp_load": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_int, c_int, c_void_p]),

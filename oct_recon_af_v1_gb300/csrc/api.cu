@@ -572,7 +572,7 @@ int octgb_set_geometry(octgb_ctx* c, int n, int taps, const int64_t* idx, const 
                 U_need = U_need > reach ? U_need : reach;
             }
         }
-        int U = U_need <= 16 ? 16 : (U_need <= 20 ? 20 : (U_need <= 24 ? 24 : 0));
+        int U = U_need <= 14 ? 14 : (U_need <= 16 ? 16 : (U_need <= 20 ? 20 : (U_need <= 24 ? 24 : 0)));
         require(U > 0, "sinc band too wide for the spectral kernel (4 outputs need > 24 source samples)");
         std::vector<float> wsh(static_cast<size_t>(kThreads) * 4 * U, 0.f);
         std::vector<int> s0v(kThreads);
@@ -1769,6 +1769,40 @@ float* precision_linearise(octgb_ctx* c, const void* raw, int dtype, int loc, in
     return X;
 }
 }  // namespace
+
+int octgb_selftest_wait_expiry(octgb_ctx* c, int which, int wait_limit_us) {
+    return guarded(c, [&] {
+        require(which == 0 || which == 1, "which must be 0 (spectral kernel) or 1 (precision form)");
+        require(wait_limit_us >= 100 && wait_limit_us <= 2000000, "wait_limit_us must be in [100, 2000000]");
+        if (!c->has_geom) throw Error(OCTGB_ERR_STATE, "octgb_set_geometry has not been called");
+        if (which == 1) require(c->prec_ok, "the geometry has no precision-form (tensor-core) tiles");
+        if (c->capturing) throw Error(OCTGB_ERR_STATE, "self-test during graph capture");
+        auto set = which == 0 ? set_wait_test_spectral : set_wait_test_precision;
+        constexpr unsigned long long kDefaultLimit = 2000000000ull;
+        // zero raws, 2 B-scans x (1 apodisation + 256) lines, already on the device
+        const int B = 2, interf = 257, apod = 1;
+        const size_t bytes = static_cast<size_t>(B) * interf * kN * sizeof(uint16_t);
+        ck(c->raw.ensure(bytes), "cudaMalloc(raw)");
+        ck(cudaMemsetAsync(c->raw.p, 0, bytes, c->stream), "memset raw");
+        ck(set(static_cast<unsigned long long>(wait_limit_us) * 1000ull, 1, c->stream), "set wait limit");
+        try {
+            if (which == 0) {
+                ck(c->magbuf.ensure(static_cast<size_t>(B) * (interf - apod) * kHalf * sizeof(float)),
+                   "cudaMalloc(mag)");
+                run_spectral(c, c->raw.p, OCTGB_U16, OCTGB_DEVICE, B, interf, apod, kModeMag, c->magbuf.as<float>(), 0,
+                             0, nullptr);
+            } else {
+                precision_linearise(c, c->raw.p, OCTGB_U16, OCTGB_DEVICE, B, interf, apod);
+            }
+            check_status(c);                    // a wait that expired throws OCTGB_ERR_TIMEOUT here
+        } catch (...) {
+            set(kDefaultLimit, 0, c->stream);
+            throw;
+        }
+        ck(set(kDefaultLimit, 0, c->stream), "restore wait limit");
+        throw Error(OCTGB_ERR_STATE, "self-test: the starved bulk-copy wait did not expire");
+    });
+}
 
 int octgb_linearise_precision(octgb_ctx* c, const void* raw, int dtype, int loc, int B, int interf, int apod,
                               float* x, int x_loc) {

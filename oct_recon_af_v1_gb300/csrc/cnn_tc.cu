@@ -398,4 +398,8 @@ cudaError_t launch_conv3x3_tc(const float* x, const float* w, const float* b, fl
     return cudaGetLastError();
 }
 
+cudaError_t set_wait_test_cnn(unsigned long long limit_ns, int starve, cudaStream_t st) {
+    return set_wait_test_here(limit_ns, starve, st);
+}
+
 }  // namespace octgb

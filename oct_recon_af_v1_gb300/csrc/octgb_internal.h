@@ -272,4 +272,10 @@ __host__ __device__ inline float ord2f(unsigned int u) {
 #endif
 }
 
+// the bounded waits' limit and self-test switch of each kernel file (see
+// octgb_device.cuh); only octgb_selftest_wait_expiry calls these
+cudaError_t set_wait_test_spectral(unsigned long long limit_ns, int starve, cudaStream_t st);
+cudaError_t set_wait_test_precision(unsigned long long limit_ns, int starve, cudaStream_t st);
+cudaError_t set_wait_test_cnn(unsigned long long limit_ns, int starve, cudaStream_t st);
+
 }  // namespace octgb

@@ -134,7 +134,7 @@ __global__ void __launch_bounds__(kPThreads, 1)
             const int64_t tile = blockIdx.x + (q / kPBlocks) * gridDim.x;
             const int b = static_cast<int>(q % kPBlocks);
             uint8_t* st = S.stage[s];
-            mbar_expect_tx(&S.full[s], kStageBytes);
+            mbar_expect_tx(&S.full[s], kStageBytes + starved_bytes(q == 0));
             const int x0 = kb[b], y0 = static_cast<int>(tile * kPM);
             for (int c = 0; c < kPChunks; ++c) {
                 tma_load_2d(st + c * kAChunkBytes, &tm_hi, x0 + 8 * c, y0, &S.full[s]);
@@ -310,7 +310,7 @@ __global__ void __launch_bounds__(kRThreads, 1)
             const int b = static_cast<int>(q % kPBlocks);
             const int bs = static_cast<int>(tile / xtiles), xt = static_cast<int>(tile % xtiles);
             uint8_t* st = S.stage[s];
-            mbar_expect_tx(&S.full[s], kRLoadBytes);
+            mbar_expect_tx(&S.full[s], kRLoadBytes + starved_bytes(q == 0));
             for (int c = 0; c < kPChunks; ++c)
                 tma_load_3d(st + c * kAChunkBytes, &tm_raw, kb[b] + 8 * c, xt * kPM, bs, &S.full[s]);
             const uint8_t* wsrc = wtiles + static_cast<size_t>(b) * 2 * kBTileBytes;
@@ -726,6 +726,10 @@ bool build_prec_tiles(const int* start, const int* len, const float* wt, std::ve
         }
     }
     return true;
+}
+
+cudaError_t set_wait_test_precision(unsigned long long limit_ns, int starve, cudaStream_t st) {
+    return set_wait_test_here(limit_ns, starve, st);
 }
 
 }  // namespace octgb

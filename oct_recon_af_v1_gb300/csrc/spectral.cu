@@ -95,18 +95,19 @@ struct Smem {
     alignas(128) RawT stage[2][kPerCta][kN];        // bulk-copy destinations (16-byte aligned)
     alignas(16) float d[kPerCta][kDSkew];           // background-free line, skewed
     alignas(16) float2 spec[kPerCta][kSpecStride];  // windowed spectrum / FFT work line
+    // second FFT line of each A-scan (16-bit raws; float32 raws need the
+    // shared memory for their larger staging rows and transform in place)
+    alignas(16) float2 fft_y[sizeof(RawT) == 2 ? kPerCta : 1][kSpecStride];
     alignas(16) float2 tw2[16][16];                 // stage-2 twiddles [r][j mod 16]
     alignas(16) float2 tw3[8][256];                 // stage-3 twiddles [r][j]
 };
 
-// One CTA (512 threads) = 4 A-scans per iteration of a persistent loop.
-// Sinc: thread t owns output samples 4t..4t+3 of all four A-scans; its band
-// weights live in registers for the whole kernel in a shifted dense form
-// wr[r][u] (the weight of source sample s0_t + u for output 4t + r, zero
-// outside the band), so each A-scan costs U conflict-free shared loads of the
-// source window (d is stored skewed by one word per 32) and 4*U FMAs, summed
-// in the reference's tap order.  FFT: 128 threads per A-scan, radix 16,16,8
-// Stockham through the padded spec line, per-group named barriers.
+// dynamic + static shared memory of the kernel within the 227 KB a CTA may use
+static_assert(sizeof(Smem<uint16_t>) + 2 * sizeof(int64_t) + kMaxQueueTiles * sizeof(unsigned) <= 232448,
+              "spectral kernel shared memory (16-bit raws) exceeds 227 KB");
+static_assert(sizeof(Smem<float>) + 2 * sizeof(int64_t) + kMaxQueueTiles * sizeof(unsigned) <= 232448,
+              "spectral kernel shared memory (float32 raws) exceeds 227 KB");
+
 // Where slot s of quad q reads its raw row and apodisation row and writes
 // its result.  Static mode: quads of one batch (n_seg segments of B x nx
 // A-scans).  Queue mode: quads of the tile table (quad0 prefix in shared
@@ -188,7 +189,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
 
     // this thread's shifted sinc weights and source window base
     float wr[4][U];
-    {
+    if (U % 4 == 0) {
         const float4* wp = reinterpret_cast<const float4*>(a.g.wsh + static_cast<int64_t>(tid) * 4 * U);
 #pragma unroll
         for (int r = 0; r < 4; ++r)
@@ -199,6 +200,16 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
                 wr[r][4 * q + 1] = v.y;
                 wr[r][4 * q + 2] = v.z;
                 wr[r][4 * q + 3] = v.w;
+            }
+    } else {                                          // U = 14: rows of 56 bytes, 8-byte aligned
+        const float2* wp = reinterpret_cast<const float2*>(a.g.wsh + static_cast<int64_t>(tid) * 4 * U);
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+#pragma unroll
+            for (int q = 0; q < U / 2; ++q) {
+                const float2 v = __ldg(wp + r * (U / 2) + q);
+                wr[r][2 * q] = v.x;
+                wr[r][2 * q + 1] = v.y;
             }
     }
     const int s0 = __ldg(a.g.s0 + tid);
@@ -238,7 +249,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
         item_end = base + a.grab < nquads ? base + a.grab : nquads;
         return base;
     };
-    auto issue = [&](int64_t quad, int buf) {
+    auto issue = [&](int64_t quad, int buf, bool first) {
         int nvalid = 0;
         SlotRef r[kPerCta];
 #pragma unroll
@@ -246,7 +257,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
             r[k] = slot_ref<RawT, kQueue>(a, quad0_s, quad, k);
             nvalid += r[k].valid ? 1 : 0;
         }
-        mbar_expect_tx(&S.bar[buf], static_cast<uint32_t>(nvalid) * kN * sizeof(RawT));
+        mbar_expect_tx(&S.bar[buf], static_cast<uint32_t>(nvalid) * kN * sizeof(RawT) + starved_bytes(first));
 #pragma unroll
         for (int k = 0; k < kPerCta; ++k)
             if (r[k].valid) tma_bulk_g2s(&S.stage[buf][k][0], r[k].row, kN * sizeof(RawT), &S.bar[buf]);
@@ -255,7 +266,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
     if (tid == 0) {
         const int64_t q0 = next_quad(-1);
         qbuf[0] = q0;
-        if (q0 >= 0) issue(q0, 0);
+        if (q0 >= 0) issue(q0, 0, true);
     }
     __syncthreads();
 
@@ -266,11 +277,17 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
         if (tid == 0) {
             const int64_t nq = next_quad(quad);
             qbuf[buf ^ 1] = nq;
-            if (nq >= 0) issue(nq, buf ^ 1);
+            if (nq >= 0) issue(nq, buf ^ 1, false);
         }
 
         const bool ok = mbar_wait_bounded(&S.bar[buf], (it >> 1) & 1, a.status);
-        if (__syncthreads_or(!ok)) return;
+        if (__syncthreads_or(!ok)) {
+            // the next quad's rows may still be arriving: let them land before
+            // the CTA's shared memory is released
+            if (tid == 0 && qbuf[buf ^ 1] >= 0) mbar_wait_bounded(&S.bar[buf ^ 1], ((it + 1) >> 1) & 1, a.status);
+            __syncthreads();
+            return;
+        }
 
         // ---- (b) background: d = raw - apod, line mean (group g, A-scan g) ----
         const SlotRef me = slot_ref<RawT, kQueue>(a, quad0_s, quad, g);
@@ -364,7 +381,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
         // ---- (e)+(f) inverse FFT, group g on its own line; |X[k]|, k < N/2 ----
         float2* X = S.spec[g];
         float magv[2][4];
-        ifft2048_low_mag(X, S.tw2, S.tw3, g, lt, magv);
+        if (sizeof(RawT) == 2)
+            ifft2048_low_mag_pp(X, S.fft_y[g], S.tw2, S.tw3, g, lt, magv);
+        else
+            ifft2048_low_mag(X, S.tw2, S.tw3, g, lt, magv);
         if (Mode == kModeMag || Mode == kModeDb) {
             if (valid) {
 #pragma unroll
@@ -534,6 +554,7 @@ cudaError_t launch_t(const SpectralArgs& a, int grid, cudaStream_t st) {
 template <typename RawT, int Mode>
 cudaError_t launch_u(const SpectralArgs& a, int grid, cudaStream_t st) {
     switch (a.g.U) {
+        case 14: return launch_t<RawT, Mode, 14>(a, grid, st);
         case 16: return launch_t<RawT, Mode, 16>(a, grid, st);
         case 20: return launch_t<RawT, Mode, 20>(a, grid, st);
         case 24: return launch_t<RawT, Mode, 24>(a, grid, st);
@@ -583,6 +604,10 @@ cudaError_t launch_spectral(const SpectralArgs& a, int dtype, int mode, int grid
     if (dtype == 0) return launch_mode<uint16_t>(a, mode, grid, st);
     if (dtype == 1) return launch_mode<int16_t>(a, mode, grid, st);
     return launch_mode<float>(a, mode, grid, st);
+}
+
+cudaError_t set_wait_test_spectral(unsigned long long limit_ns, int starve, cudaStream_t st) {
+    return set_wait_test_here(limit_ns, starve, st);
 }
 
 int spectral_max_ctas_per_sm(int dtype, int mode) {
