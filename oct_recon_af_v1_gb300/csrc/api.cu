@@ -556,7 +556,11 @@ int octgb_set_geometry(octgb_ctx* c, int n, int taps, const int64_t* idx, const 
             st[i] = s;
         }
         // shifted dense weights of the spectral kernel: thread t owns outputs
-        // 4t..4t+3; wsh[t][r][u] = weight of source s0_t + u for output 4t + r
+        // 4t..4t+3 and reads the U source samples s0_t .. s0_t + U - 1; at step u
+        // it reads the one congruent to u (mod U), so wsh[t][r][u] = weight of
+        // source s0_t + v, (s0_t + v) = u (mod U), for output 4t + r.  With
+        // gcd(U, 32) = 2 the samples a warp reads at one step are U apart (or
+        // the same sample): distinct banks of a linear line.
         std::vector<int> len(kN, 0);
         for (int i = 0; i < kN; ++i) {
             for (int t = 0; t < taps; ++t)
@@ -572,8 +576,8 @@ int octgb_set_geometry(octgb_ctx* c, int n, int taps, const int64_t* idx, const 
                 U_need = U_need > reach ? U_need : reach;
             }
         }
-        int U = U_need <= 14 ? 14 : (U_need <= 16 ? 16 : (U_need <= 20 ? 20 : (U_need <= 24 ? 24 : 0)));
-        require(U > 0, "sinc band too wide for the spectral kernel (4 outputs need > 24 source samples)");
+        int U = U_need <= 14 ? 14 : (U_need <= 18 ? 18 : (U_need <= 22 ? 22 : (U_need <= 26 ? 26 : 0)));
+        require(U > 0, "sinc band too wide for the spectral kernel (4 outputs need > 26 source samples)");
         std::vector<float> wsh(static_cast<size_t>(kThreads) * 4 * U, 0.f);
         std::vector<int> s0v(kThreads);
         for (int t = 0; t < kThreads; ++t) {
@@ -582,7 +586,7 @@ int octgb_set_geometry(octgb_ctx* c, int n, int taps, const int64_t* idx, const 
             for (int r = 0; r < 4; ++r) {
                 const int i = 4 * t + r;
                 for (int k = 0; k < len[i]; ++k) {
-                    const int u = st[i] - base + k;
+                    const int u = (st[i] + k) % U;         // step that reads source st[i] + k
                     wsh[(static_cast<size_t>(t) * 4 + r) * U + u] = wt[static_cast<size_t>(k) * kN + i];
                 }
             }

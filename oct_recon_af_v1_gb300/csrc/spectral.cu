@@ -59,9 +59,7 @@ struct RawLoad<float> {
     }
 };
 
-constexpr int kDLine = kN + kTail;                        // d line incl. zero tail
-constexpr int kDSkew = kDLine + kDLine / 32 + 4;           // skewed length (+1 word per 32)
-__device__ __forceinline__ int skew(int w) { return w + (w >> 5); }
+constexpr int kDLine = kN + kTail;                        // d line incl. zero tail (16-byte rows)
 
 // float32(float64(x) * h) for a float64 h given as float32 hi + lo (h2.x +
 // h2.y, the rest below 2^-48 |h|) without the FP64 pipe: p + e1 = x * hi
@@ -93,7 +91,7 @@ struct Smem {
     float mval[kPerCta];
     unsigned int mm[2];
     alignas(128) RawT stage[2][kPerCta][kN];        // bulk-copy destinations (16-byte aligned)
-    alignas(16) float d[kPerCta][kDSkew];           // background-free line, skewed
+    alignas(16) float d[kPerCta][kDLine];           // background-free line
     alignas(16) float2 spec[kPerCta][kSpecStride];  // windowed spectrum / FFT work line
     // second FFT line of each A-scan (16-bit raws; float32 raws need the
     // shared memory for their larger staging rows and transform in place)
@@ -164,12 +162,15 @@ __device__ __forceinline__ SlotRef slot_ref(const SpectralArgs& a, const unsigne
 
 // One CTA (512 threads) = 4 A-scans per iteration of a persistent loop.
 // Sinc: thread t owns output samples 4t..4t+3 of all four A-scans; its band
-// weights live in registers for the whole kernel in a shifted dense form
-// wr[r][u] (the weight of source sample s0_t + u for output 4t + r, zero
-// outside the band), so each A-scan costs U conflict-free shared loads of the
-// source window (d is stored skewed by one word per 32) and 4*U FMAs, summed
-// in the reference's tap order.  FFT: 128 threads per A-scan, radix 16,16,8
-// Stockham through the padded spec line, per-group named barriers.
+// weights live in registers for the whole kernel in a dense form over its
+// window of U source samples s0_t .. s0_t + U - 1 (zero outside the band).
+// Step u of the window reads the sample congruent to u (mod U) and wr[r][u]
+// is that sample's weight for output 4t + r: the windows of a warp's threads
+// overlap, so at one step they read the same samples or samples U apart, and
+// with gcd(U, 32) = 2 those sit in distinct banks of the plain (unpadded)
+// line - each A-scan costs U conflict-free shared loads and 4*U FMAs.  FFT:
+// 128 threads per A-scan, radix 16,16,8 Stockham through two padded lines,
+// per-group named barriers.
 // Work: static grid-stride over one batch's quads, or (resample mode) quads
 // taken `grab` at a time from a device work queue spanning many tiles of
 // uneven size.
@@ -213,6 +214,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
             }
     }
     const int s0 = __ldg(a.g.s0 + tid);
+    const int wrot = s0 % U;                          // window samples before s0 wrap to the next period
+    const int wbase = s0 - wrot;
 
     if (tid == 0) {
         mbar_init(&S.bar[0], 1);
@@ -223,7 +226,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
     }
     if (kQueue)
         for (int k = tid; k < a.n_qt; k += kThreads) quad0_s[k] = a.qt[k].quad0;
-    for (int k = tid; k < kPerCta * kTail; k += kThreads) S.d[k / kTail][skew(kN + k % kTail)] = 0.f;
+    for (int k = tid; k < kPerCta * kTail; k += kThreads) S.d[k / kTail][kN + k % kTail] = 0.f;
     for (int k = tid; k < 16 * 16; k += kThreads) {
         const int r = k / 16, j = k % 16;
         S.tw2[r][j] = __ldg(a.g.tw + (r * j * (kN / 256)) % kN);
@@ -318,11 +321,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
             const float m = ((S.red[g][0] + S.red[g][1]) + (S.red[g][2] + S.red[g][3])) * (1.0f / kN);
             if (lt == 0) S.mval[g] = m;
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const int j = 4 * lt + 512 * q;
-#pragma unroll
-                for (int i = 0; i < 4; ++i) S.d[g][skew(j + i)] = dv[4 * q + i] - m;
-            }
+            for (int q = 0; q < 4; ++q)
+                *reinterpret_cast<float4*>(&S.d[g][4 * lt + 512 * q]) =
+                    make_float4(dv[4 * q] - m, dv[4 * q + 1] - m, dv[4 * q + 2] - m, dv[4 * q + 3] - m);
         }
         __syncthreads();
 
@@ -336,9 +337,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
 #pragma unroll 1
             for (int k = 0; k < kPerCta; ++k) {
                 const float mk = S.mval[k];
+                // modular window order: step u reads the window sample congruent
+                // to u (mod U); the weights are stored in the same order
+                const float* dk = S.d[k] + wbase;
                 float win[U];
 #pragma unroll
-                for (int u = 0; u < U; ++u) win[u] = S.d[k][skew(s0 + u)];
+                for (int u = 0; u < U; ++u) win[u] = dk[u < wrot ? u + U : u];
                 float lh[4], lx[4];
                 bool lsafe[4];
 #pragma unroll
@@ -555,9 +559,9 @@ template <typename RawT, int Mode>
 cudaError_t launch_u(const SpectralArgs& a, int grid, cudaStream_t st) {
     switch (a.g.U) {
         case 14: return launch_t<RawT, Mode, 14>(a, grid, st);
-        case 16: return launch_t<RawT, Mode, 16>(a, grid, st);
-        case 20: return launch_t<RawT, Mode, 20>(a, grid, st);
-        case 24: return launch_t<RawT, Mode, 24>(a, grid, st);
+        case 18: return launch_t<RawT, Mode, 18>(a, grid, st);
+        case 22: return launch_t<RawT, Mode, 22>(a, grid, st);
+        case 26: return launch_t<RawT, Mode, 26>(a, grid, st);
         default: return cudaErrorInvalidValue;
     }
 }
