@@ -391,6 +391,9 @@ def gpu_arm(args, rank, world):
         line["cpu_baseline"] = cpu_baseline_config1(vol, torch, budget_s=args.cpu_budget)
         first = {k: vol.raw[(0,) + k][:1].cpu().numpy().view(np.uint16) for k in vol.order}
         line["cpu_numpy_path"] = numpy_path_baseline(vol, vol.tg, first, frames=1)
+    if rank == 0 and not args.no_precision:
+        torch.cuda.synchronize()
+        line["precision_form"] = precision_leg(ctx, vol, torch, stream, args)
     if rank == 0 and not args.no_plugin:
         torch.cuda.synchronize()
         line["plugin_process_row"] = plugin_arm(vol, torch, dev)
@@ -400,7 +403,83 @@ def gpu_arm(args, rank, world):
         if "value" in pf:
             pf["speedup_of_value"] = value / world / pf["value"]
         line["plain_fp32_gpu_form"] = pf
+    if rank == 0 and not args.no_learned:
+        torch.cuda.synchronize()
+        line["learned_vs_search"] = learned_leg(args, torch, stream, dev)
     return line
+
+
+def precision_leg(ctx, vol, torch, stream, args, sample_bscans=2):
+    """The precision form (exact integer background, tcgen05 split-FP16 sinc,
+    FFT, |.|) over every tile of the resident volume, beside the float32 form
+    (the same tiles through the fused kernel), and the legacy codes of both
+    against the float64 oracle on a sample (B-scans 0..1 of one tile, one
+    shared clim)."""
+    from oracle import numerics as O
+    from oct_recon_af_v1_gb300 import synthetic
+    tiles = list(vol.raw.values())
+    B, interf = tiles[0].shape[0], tiles[0].shape[1]
+    nxa = interf - APOD
+    mag = torch.empty((B, nxa, 1024), dtype=torch.float32, device="cuda")
+
+    def run(fn):
+        for t in tiles:
+            fn(t, APOD, mag, raw_dtype=0)
+
+    def timed(fn, steps=3, warm=1):
+        for _ in range(warm):
+            run(fn)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            run(fn)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+    ms_p = timed(ctx.magnitude_precision)
+    ms_f = timed(ctx.magnitude)
+    ascans = len(tiles) * B * nxa
+    sample = tiles[0][:sample_bscans]
+    raw = sample.cpu().numpy().view(np.uint16)
+    og = O.spectral_geometry(synthetic.lambda_nm(), synthetic.beta_ref_from_px(1e-5), 1.33)
+    with np.errstate(divide="ignore"):
+        d64 = 20 * np.log10(O.magnitude_numpy(raw, og, APOD, np.float64))
+        dp = 20 * np.log10(np.asarray(ctx.magnitude_precision(sample, APOD, raw_dtype=0), np.float64))
+        df = 20 * np.log10(np.asarray(ctx.magnitude(sample, APOD, raw_dtype=0), np.float64))
+    fin = np.isfinite(d64)
+    clim = (float(d64[fin].min()), float(d64[fin].max()))
+    rp, rf = (O.lsb_levels(d, d64, clim)[-1] for d in (dp, df))
+    return {"value": ascans / (ms_p * 1e-3), "unit": "A-scans/s", "ms_per_volume": ms_p,
+            "float32_form": {"value": ascans / (ms_f * 1e-3), "ms_per_volume": ms_f},
+            "codes_vs_float64": {"precision_exact": rp["exact_frac"], "precision_max_lsb": rp["max_lsb"],
+                                 "float32_exact": rf["exact_frac"], "float32_max_lsb": rf["max_lsb"],
+                                 "voxels": rp["n"], "sample": f"B-scans 0..{sample_bscans - 1} of one tile, "
+                                 "all 1024 depth bins, one clim (the float64 oracle's)"},
+            "work": "the volume's 12 tiles, spectral stage only (magnitudes out)"}
+
+
+def learned_leg(args, torch, stream, dev):
+    """The learned estimator against the plain search at a reduced, stated
+    size (4 000 training images, 6 epochs, 200 held-out B-scans): both
+    estimators' time per B-scan, the speed-up and the sharpness reached."""
+    import copy
+    from oct_recon_af_v1_gb300._lib import Context
+    a = copy.copy(args)
+    a.train4, a.epochs4, a.test4, a.steps, a.warmup = 4000, 6, 200, 3, 2
+    ctx4 = Context(torch.cuda.current_device())
+    ctx4.set_stream(stream.cuda_stream)
+    try:
+        r = gpu_arm_config4(a, 0, 1, torch, ctx4, stream, dev)
+    finally:
+        ctx4.close()
+    n = r["config"]["held_out_bscans"]
+    return {"learned_ms_per_bscan": r["ms_per_step"] / n, "search_ms_per_bscan": r["search"]["seconds"] * 1e3 / n,
+            "speedup": r["search"]["learned_speedup"], "learned_a_scans_per_s": r["value"],
+            "search_a_scans_per_s": r["search"]["value"], "accuracy": r["accuracy"],
+            "training": {k: r["training"][k] for k in ("train_s", "epochs", "batch")},
+            "config": r["config"]["workload"]}
 
 
 def config3_specs(seed=3, n_tiles=64):
@@ -489,8 +568,16 @@ def gpu_arm_config3(args, rank, world, torch, ctx, stream, dev):
 
     # the last tuning choice: the persistent queue launch or one launch per
     # tile, both captured in a graph (the same kernels and results)
-    ms_queue, _ = timed(lambda: ctx.graph_launch(gid_queue), 3, 2)
-    ms_tiles, _ = timed(lambda: ctx.graph_launch(gid_tiles), 3, 2)
+    # (five interleaved rounds of 3 steps each, medians, with the SM clock
+    # sampled meanwhile: the two forms differ by a few per cent)
+    q_ms, t_ms = [], []
+    choice_clk = Clocks(int(os.environ.get("LOCAL_RANK", 0)))
+    choice_clk.start()
+    for _ in range(5):
+        q_ms.append(timed(lambda: ctx.graph_launch(gid_queue), 3, 1)[0])
+        t_ms.append(timed(lambda: ctx.graph_launch(gid_tiles), 3, 1)[0])
+    choice_clock = choice_clk.stop()
+    ms_queue, ms_tiles = float(np.median(q_ms)), float(np.median(t_ms))
     form = "queue" if ms_queue <= ms_tiles else "per-tile"
     gid = gid_queue if form == "queue" else gid_tiles
     clocks = Clocks(int(os.environ.get("LOCAL_RANK", 0)))
@@ -562,8 +649,10 @@ def gpu_arm_config3(args, rank, world, torch, ctx, stream, dev):
                          "bytes_per_launch": alg, "peak_source": src + " (burst copy)"},
             "clocks": clk,
             "forms": {"chosen": form, "queue_ms": ms_queue, "per_tile_ms": ms_tiles,
+                      "queue_ms_rounds": q_ms, "per_tile_ms_rounds": t_ms, "clocks": choice_clock,
                       "note": "both CUDA graphs: the persistent queue launch over all tiles, or one apodisation "
-                              "+ one spectral launch per tile; the faster one is timed"},
+                              "+ one spectral launch per tile; medians of 5 interleaved rounds, the faster one "
+                              "is timed"},
             "e2e": {"value": ascans / (ms_e2e * 1e-3), "unit": "A-scans/s", "ms_per_step": ms_e2e,
                     "h2d_bytes_per_step": raw_bytes, "d2h_bytes_per_step": out_bytes}}
     return line
@@ -638,13 +727,13 @@ def gpu_arm_config2(args, rank, world, torch, ctx, stream, dev):
             "float32_form": {"value": ascans / (ms_f32 * 1e-3), "unit": "A-scans/s", "ms_per_step": ms_f32}}
 
 
-def config4_desc(n_train, n_base, epochs):
+def config4_desc(n_train, n_base, epochs, n_test=500):
     return {"workload": f"config4: learned beta/focus vs plain search; {n_train} training images from {n_base} "
-                        "dispersion-free B-scans x 10 synthetic dispersions (phase trick), 500 held-out B-scans "
+                        f"dispersion-free B-scans x 10 synthetic dispersions (phase trick), {n_test} held-out B-scans "
                         "x 500 A-scans x 2048 uint16 with beta_px ~ U[-5e-5, 5e-5] in the spectra and a confocal "
                         "focus ~ U[100, 900] px (reflector amplitude x exp(-((d - f)/150)^2)); 3 probe "
                         "reconstructions -> 256x256 dB images -> CNN",
-            "held_out_bscans": 500, "ascans_per_bscan": 500, "training_images": n_train, "epochs": epochs,
+            "ascans_per_bscan": 500, "training_images": n_train, "epochs": epochs,
             "search": "per-B-scan: 41-point grid over +-1.2 x 7.5e7 nm^2/rad (one launch) + batched zoom "
                       "refinement (9 candidates per launch, to 2e-5 of the largest |bound|), top_percentile; "
                       "focus: x-mean profile rules",
@@ -657,7 +746,7 @@ def gpu_arm_config4(args, rank, world, torch, ctx, stream, dev):
     from oct_recon_af_v1_gb300 import synthetic as S
     from oct_recon_af_v1_gb300._lib import U16
     lam = S.lambda_nm()
-    NX, n_test, shifts = 500, 500, 10
+    NX, n_test, shifts = 500, int(getattr(args, "test4", 500)), 10
     n_base = max(1, args.train4 // shifts)
     n_train = n_base * shifts
     rng = np.random.default_rng(404)
@@ -793,7 +882,8 @@ def gpu_arm_config4(args, rank, world, torch, ctx, stream, dev):
     return {"metric": METRIC, "value": v_l, "unit": "A-scans/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_learned, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 (uint16 in)", "data": "synthetic (seeded, generated on device)",
-            "config": config4_desc(n_train, n_base, epochs), "gpu_launches": int(launches),
+            "config": dict(config4_desc(n_train, n_base, epochs, n_test), held_out_bscans=n_test),
+            "gpu_launches": int(launches),
             "roofline": {"bound": "hbm", "achieved": raw_bytes / (ms_learned * 1e-3) / 1e9, "peak": hbm,
                          "unit": "GB/s", "frac": raw_bytes / (ms_learned * 1e-3) / 1e9 / hbm, "traffic": None,
                          "kernel": "whole learned step (linearise, 3 probe FFT passes, pooling, CNN forward on the tensor cores)",
@@ -808,6 +898,12 @@ def gpu_arm_config4(args, rank, world, torch, ctx, stream, dev):
                          "sharpness_gap_p95": float(np.quantile(gap, 0.95)),
                          "sharpness_gap_unit": "(S(search) - S(learned)) / (max - min of the B-scan's grid curve)",
                          "sharpness_truth_minus_search_mean": float(np.mean((s_t - s_s) / rng_j)),
+                         # the score is log(mean of the top 1 % of |A|^2): exp of the score difference is
+                         # the ratio of the top-1 % mean intensities at the predicted and searched betas
+                         "sharpness_gap_relative_mean": float(np.mean((s_s - s_l) / np.abs(s_s))),
+                         "top1pct_intensity_ratio_mean": float(np.mean(np.exp(s_l - s_s))),
+                         "top1pct_intensity_ratio_p05": float(np.quantile(np.exp(s_l - s_s), 0.05)),
+                         "fraction_within_1pct_intensity": float(np.mean(np.exp(s_l - s_s) >= 0.99)),
                          "focus_mae_learned_px": float(np.mean(np.abs(focus_l - focus_t))),
                          "focus_mae_plain_px": float(np.mean(np.abs(focus_s - focus_t)))},
             "training": {"images_s": t_data, "train_s": t_train, "epochs": epochs, "batch": bs,
@@ -1188,6 +1284,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true", help="skip timing the reference's plain float32 GPU path")
     ap.add_argument("--no-plugin", action="store_true", help="skip timing the reference's process_row on gb300")
+    ap.add_argument("--no-precision", action="store_true", help="skip the precision-form leg of the default line")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-vs-search leg of the default line")
+    ap.add_argument("--test4", type=int, default=500, help="held-out B-scans of the learned estimator (config 4)")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--ref-frames", type=int, default=4)
     ap.add_argument("--batch", type=int, default=9, help="frames per frame batch")

@@ -114,6 +114,7 @@ struct SlotTable {
 // capture used it (pinned); unpinned tables are recycled least recently used.
 struct QTable {
     std::vector<QueueTile> key;  // the uploaded contents
+    uint64_t hash = 0;           // FNV-1a of the contents, compared before the bytes
     DevBuf buf;
     bool pinned = false;
     uint64_t last_use = 0;
@@ -396,11 +397,19 @@ const SlotTable& slot_table(octgb_ctx* c, int n_tiles, const int* plan_ids, int 
 // say) can be run once and then captured.
 constexpr int kMaxFreeTables = 128;
 
+uint64_t fnv1a(const void* p, size_t n) {
+    const unsigned char* b = static_cast<const unsigned char*>(p);
+    uint64_t h = 1469598103934665603ull;
+    for (size_t i = 0; i < n; ++i) h = (h ^ b[i]) * 1099511628211ull;
+    return h;
+}
+
 const QueueTile* tile_table(octgb_ctx* c, const std::vector<QueueTile>& qt) {
     const size_t bytes = qt.size() * sizeof(QueueTile);
+    const uint64_t hash = fnv1a(qt.data(), bytes);
     ++c->qtable_clock;
     for (QTable* t : c->qtables)
-        if (t->key.size() == qt.size() && memcmp(t->key.data(), qt.data(), bytes) == 0) {
+        if (t->hash == hash && t->key.size() == qt.size() && memcmp(t->key.data(), qt.data(), bytes) == 0) {
             t->last_use = c->qtable_clock;
             if (c->capturing) t->pinned = true;
             return t->buf.as<QueueTile>();
@@ -420,6 +429,7 @@ const QueueTile* tile_table(octgb_ctx* c, const std::vector<QueueTile>& qt) {
     t->key.clear();                       // a failed upload leaves no matching entry
     ck(t->buf.ensure(static_cast<size_t>(kMaxQueueTiles) * sizeof(QueueTile)), "cudaMalloc(tile table)");
     t->key = qt;
+    t->hash = hash;
     t->last_use = c->qtable_clock;
     // from pageable memory: the call returns once the source is staged
     ck(cudaMemcpyAsync(t->buf.p, t->key.data(), bytes, cudaMemcpyHostToDevice, c->stream), "H2D tile table");

@@ -50,6 +50,23 @@ def test_noalloc_matches_magnitude_on_consecutive_calls(spectral_case):
             got = out.cpu().numpy()
             scale = np.abs(ref).max()
             assert np.abs(got - ref).max() / scale < 2e-6
+        # the largest batch the fixed scratch holds (64 B-scans fill it), and the
+        # int16 and float32 raw types
+        full = synthetic.generate_numpy(64, 8, apod, seed=22)
+        for raw, dt in ((full, _lib.U16), (full.astype(np.int16), _lib.I16), (full.astype(np.float32), _lib.F32)):
+            B, interf, N = raw.shape
+            ref = ctx.magnitude(raw, apod)
+            if dt == _lib.U16:
+                dev = synthetic.u16_bits(torch.from_numpy(raw.astype(np.int32)).cuda())
+            else:
+                dev = torch.from_numpy(np.ascontiguousarray(raw)).cuda()
+            out = torch.full((B, interf - apod, N // 2), float("nan"), dtype=torch.float32, device="cuda")
+            torch.cuda.synchronize()
+            rc = lib.octgb_magnitude_noalloc(ctx.h, ctypes.c_void_p(dev.data_ptr()), dt, B, interf, apod,
+                                             ctypes.c_void_p(out.data_ptr()))
+            assert rc == _lib.OK, lib.octgb_last_error(ctx.h)
+            ctx.synchronize()
+            assert np.abs(out.cpu().numpy() - ref).max() / np.abs(ref).max() < 2e-6
         # beyond the fixed scratch: a clear error, no work
         big = torch.zeros((65, interf, N), dtype=torch.int16, device="cuda")
         rc = lib.octgb_magnitude_noalloc(ctx.h, ctypes.c_void_p(big.data_ptr()), _lib.U16, 65, interf, apod,
