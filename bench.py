@@ -53,9 +53,9 @@ sys.path.insert(0, str(ROOT))
 METRIC = "A-scans/s on 1 GB300 (fused vs plain FP32; learned vs search β) at ≤1 LSB"
 APOD = 25
 # DRAM bytes per A-scan of the spectral kernel from one ncu capture
-# (profiles/k_spectral_config1_small.md: (49.46 + 11.17) MB over 12 000 A-scans;
+# (profiles/k_spectral_config1_small.md: (49.45 + 7.74) MB over 12 000 A-scans;
 # caches flushed before the kernel, magnitudes partly still in L2 at its end)
-SPECTRAL_DRAM_BYTES_PER_ASCAN = (49.461504e6 + 11.174144e6) / 12000
+SPECTRAL_DRAM_BYTES_PER_ASCAN = (49.447680e6 + 7.744512e6) / 12000
 
 
 # ------------------------------------------------------------------------ workload description
@@ -440,6 +440,7 @@ def precision_leg(ctx, vol, torch, stream, args, sample_bscans=2):
 
     ms_p = timed(ctx.magnitude_precision)
     ms_f = timed(ctx.magnitude)
+    ms_x = timed(ctx.magnitude_exact, steps=1, warm=1)
     ascans = len(tiles) * B * nxa
     sample = tiles[0][:sample_bscans]
     raw = sample.cpu().numpy().view(np.uint16)
@@ -448,13 +449,17 @@ def precision_leg(ctx, vol, torch, stream, args, sample_bscans=2):
         d64 = 20 * np.log10(O.magnitude_numpy(raw, og, APOD, np.float64))
         dp = 20 * np.log10(np.asarray(ctx.magnitude_precision(sample, APOD, raw_dtype=0), np.float64))
         df = 20 * np.log10(np.asarray(ctx.magnitude(sample, APOD, raw_dtype=0), np.float64))
+        dx = 20 * np.log10(np.asarray(ctx.magnitude_exact(sample, APOD, raw_dtype=0), np.float64))
     fin = np.isfinite(d64)
     clim = (float(d64[fin].min()), float(d64[fin].max()))
-    rp, rf = (O.lsb_levels(d, d64, clim)[-1] for d in (dp, df))
+    rp, rf, rx = (O.lsb_levels(d, d64, clim)[-1] for d in (dp, df, dx))
     return {"value": ascans / (ms_p * 1e-3), "unit": "A-scans/s", "ms_per_volume": ms_p,
             "float32_form": {"value": ascans / (ms_f * 1e-3), "ms_per_volume": ms_f},
+            "float64_form": {"value": ascans / (ms_x * 1e-3), "ms_per_volume": ms_x,
+                             "note": "exact integer background, float64 sinc / window / FFT, |X| to float32"},
             "codes_vs_float64": {"precision_exact": rp["exact_frac"], "precision_max_lsb": rp["max_lsb"],
                                  "float32_exact": rf["exact_frac"], "float32_max_lsb": rf["max_lsb"],
+                                 "float64_form_exact": rx["exact_frac"], "float64_form_max_lsb": rx["max_lsb"],
                                  "voxels": rp["n"], "sample": f"B-scans 0..{sample_bscans - 1} of one tile, "
                                  "all 1024 depth bins, one clim (the float64 oracle's)"},
             "work": "the volume's 12 tiles, spectral stage only (magnitudes out)"}

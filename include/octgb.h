@@ -110,6 +110,18 @@ int octgb_magnitude(octgb_ctx *ctx, const void *raw, int raw_dtype, int raw_loc,
 int octgb_db(octgb_ctx *ctx, const void *raw, int raw_dtype, int raw_loc, int B, int interf, int apod_size,
              int z0, int nz, float *db, int db_loc, double *minmax);
 
+/* Float64 form of SpectralProcessor.magnitude: the reference's NumPy path at
+ * precision "float64" (octrecon/core/spectral.py:91-95,123-165).  The
+ * background is exact (integer apodisation sums; the line mean from the integer
+ * sum of the numerators), the sinc runs in float64 over the float64 band
+ * weights given to octgb_set_geometry, then the float64 window and a float64
+ * inverse FFT; |X| (n/2 bins) is rounded once to float32.  raw must be uint16
+ * or int16.  Several times slower than octgb_magnitude (GB300's float64 rate is
+ * a small fraction of its float32 rate); its codes match the reference's
+ * float64 path to within 1 LSB. */
+int octgb_magnitude_exact(octgb_ctx *ctx, const void *raw, int raw_dtype, int raw_loc, int B, int interf,
+                          int apod_size, float *mag, int mag_loc);
+
 /* Precision form of the spectral stage: the sinc k-linearisation as a banded
  * GEMM on the tensor cores (tcgen05.mma, split-FP16 with three products,
  * float32 accumulation in TMEM; 128 A-scans x 64 output samples x a

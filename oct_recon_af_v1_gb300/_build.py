@@ -17,7 +17,7 @@ CSRC = PKG / "csrc"
 OUT_DIR = PKG / "_lib"
 LIB = OUT_DIR / "liboctgb.so"
 INCLUDE = PKG.parent / "include"
-SOURCES = ["api.cu", "spectral.cu", "stitch.cu", "estimate.cu", "cnn.cu", "precision.cu", "prepare.cu", "encode.cu", "cnn_tc.cu"]
+SOURCES = ["api.cu", "spectral.cu", "stitch.cu", "estimate.cu", "cnn.cu", "precision.cu", "prepare.cu", "encode.cu", "cnn_tc.cu", "exact.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3",
               "--expt-relaxed-constexpr", "-I", str(INCLUDE), "-I", str(CSRC)]

@@ -73,6 +73,7 @@ SIGNATURES = {
                                        c_int, c_int, c_void_p, c_int, c_int]),
     "octgb_linearise_precision": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_int, c_void_p, c_int]),
     "octgb_magnitude_precision": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_int, c_void_p, c_int]),
+    "octgb_magnitude_exact": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_int, c_void_p, c_int]),
     "octgb_disp_images": (c_int, [c_void_p, c_int, c_void_p, c_int, c_int, c_int, c_void_p, c_int]),
     "octgb_cnn_images": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_void_p, c_int]),
     "octgb_cnn_conv3x3": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_int,
@@ -329,6 +330,16 @@ class Context:
             out = np.empty((B, interf - apod_size, self.n // 2), np.float32)
         op, oloc = _ptr(out)
         self._check(self.lib.octgb_magnitude_precision(self.h, p, dt, loc, B, interf, apod_size, op, oloc))
+        return out
+
+    def magnitude_exact(self, raw, apod_size: int, out=None, raw_dtype=None):
+        """Float64 form of magnitude(): exact background, float64 sinc, window
+        and FFT, |X| rounded to float32 (integer raws only)."""
+        raw, p, loc, dt, B, interf = self._raw_args(raw, apod_size, raw_dtype)
+        if out is None:
+            out = np.empty((B, interf - apod_size, self.n // 2), np.float32)
+        op, oloc = _ptr(out)
+        self._check(self.lib.octgb_magnitude_exact(self.h, p, dt, loc, B, interf, apod_size, op, oloc))
         return out
 
     def db(self, raw, apod_size: int, z0: int, nz: int, out=None, minmax: bool = True, raw_dtype=None):

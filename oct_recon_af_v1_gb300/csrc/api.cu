@@ -165,6 +165,8 @@ struct octgb_ctx {
     // precision form (tensor-core sinc)
     bool prec_ok = false;
     DevBuf prec_w, prec_kb, prec_hi, prec_lo, prec_m, prec_x;
+    // float64 form: band weights (tap-major), window / N and twiddles in float64
+    DevBuf ex_w, ex_win, ex_tw;
     // dispersion scorer and focus profiles
     bool win_is_one = false;                 // geometry window is exactly 1 (plain linearisation)
     DevBuf disp_x, disp_hann, disp_phase, disp_a, disp_score, xmed;
@@ -490,7 +492,7 @@ int octgb_destroy(octgb_ctx* c) {
     for (DevBuf* b : {&c->w, &c->start, &c->win, &c->tw, &c->wsh, &c->s0, &c->raw, &c->apod, &c->out, &c->mm, &c->frames, &c->num,
                       &c->den, &c->plan_table, &c->run_mm, &c->magbuf, &c->dbbuf, &c->planemm, &c->segs, &c->qtable,
                       &c->qcounter, &c->disp_x, &c->disp_hann, &c->disp_phase, &c->disp_a, &c->disp_score, &c->xmed,
-                      &c->prec_w, &c->prec_kb, &c->prec_hi, &c->prec_lo, &c->prec_m, &c->prec_x, &c->prep,
+                      &c->prec_w, &c->prec_kb, &c->prec_hi, &c->prec_lo, &c->prec_m, &c->prec_x, &c->ex_w, &c->ex_win, &c->ex_tw, &c->prep,
                       &c->prep_apod, &c->magrep, &c->srr, &c->gemm_part, &c->enc_bits, &c->enc_lut, &c->enc_slots, &c->enc_sizes})
         b->release();
     for (QTable* t : c->qtables) {
@@ -623,6 +625,27 @@ int octgb_set_geometry(octgb_ctx* c, int n, int taps, const int64_t* idx, const 
            "H2D wsh");
         ck(cudaMemcpyAsync(c->s0.p, s0v.data(), s0v.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream),
            "H2D s0");
+        // float64 form: the band weights as given (tap-major), window / N and twiddles in float64
+        {
+            std::vector<double> wd(static_cast<size_t>(taps) * kN, 0.0);
+            std::vector<double2> wind(kN), twd(kN);
+            for (int i = 0; i < kN; ++i) {
+                for (int t = 0; t < len[i]; ++t) wd[static_cast<size_t>(t) * kN + i] = w[static_cast<size_t>(i) * taps + t];
+                wind[i] = make_double2(window[2 * i] * (1.0 / kN), window[2 * i + 1] * (1.0 / kN));
+                const double ang = 2.0 * 3.14159265358979323846 * i / kN;
+                twd[i] = make_double2(cos(ang), sin(ang));
+            }
+            ck(c->ex_w.ensure(wd.size() * sizeof(double)), "cudaMalloc(float64 weights)");
+            ck(c->ex_win.ensure(kN * sizeof(double2)), "cudaMalloc(float64 window)");
+            ck(c->ex_tw.ensure(kN * sizeof(double2)), "cudaMalloc(float64 twiddles)");
+            ck(cudaMemcpyAsync(c->ex_w.p, wd.data(), wd.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream),
+               "H2D float64 weights");
+            ck(cudaMemcpyAsync(c->ex_win.p, wind.data(), kN * sizeof(double2), cudaMemcpyHostToDevice, c->stream),
+               "H2D float64 window");
+            ck(cudaMemcpyAsync(c->ex_tw.p, twd.data(), kN * sizeof(double2), cudaMemcpyHostToDevice, c->stream),
+               "H2D float64 twiddles");
+            ck(cudaStreamSynchronize(c->stream), "sync float64 geometry");
+        }
         // tensor-core sinc tiles of the precision form (when every output block's band fits its window)
         std::vector<uint16_t> ptiles;
         std::vector<int> pkb;
@@ -1833,6 +1856,46 @@ int octgb_linearise_precision(octgb_ctx* c, const void* raw, int dtype, int loc,
         const float* X = precision_linearise(c, raw, dtype, loc, B, interf, apod);
         copy_out(c, x, x_loc, X, static_cast<size_t>(B) * (interf - apod) * kN * sizeof(float));
         check_status(c);
+    });
+}
+
+int octgb_magnitude_exact(octgb_ctx* c, const void* raw, int dtype, int loc, int B, int interf, int apod, float* mag,
+                          int mag_loc) {
+    return guarded(c, [&] {
+        if (!c->has_geom) throw Error(OCTGB_ERR_STATE, "octgb_set_geometry has not been called");
+        if (c->cancel.load()) throw Error(OCTGB_ERR_CANCELLED, "cancelled");
+        validate_raw(raw, dtype, loc, B, interf, apod);
+        require(dtype == OCTGB_U16 || dtype == OCTGB_I16,
+                "the float64 form takes integer raws (its background is formed exactly from integer sums)");
+        require(mag != nullptr, "mag is NULL");
+        if (B == 0) return;
+        const size_t bytes = static_cast<size_t>(B) * interf * kN * raw_elem(dtype);
+        const void* rd = stage_raw(c, raw, dtype, loc, bytes);
+        const int nx = interf - apod;
+        const size_t ob = static_cast<size_t>(B) * nx * kHalf * sizeof(float);
+        float* dst = mag;
+        if (mag_loc != OCTGB_DEVICE) {
+            ck(c->out.ensure(ob), "cudaMalloc(out)");
+            dst = c->out.as<float>();
+        }
+        ck(c->apod.ensure(static_cast<size_t>(B) * kN * sizeof(int)), "cudaMalloc(apodisation sums)");
+        ExactArgs a{};
+        a.raw = rd;
+        a.B = B;
+        a.interf = interf;
+        a.apod = apod;
+        a.nx = nx;
+        a.n_ascans = static_cast<int64_t>(B) * nx;
+        a.start = c->start.as<int>();
+        a.w = c->ex_w.as<double>();
+        a.taps = c->taps;
+        a.win = c->ex_win.as<double2>();
+        a.tw = c->ex_tw.as<double2>();
+        a.mag = dst;
+        ck(launch_exact(a, dtype, c->apod.as<int>(), c->num_sms, c->stream), "float64 spectral kernels");
+        c->launches += 2;
+        if (mag_loc != OCTGB_DEVICE) copy_out(c, mag, OCTGB_HOST, dst, ob);
+        if (mag_loc != OCTGB_DEVICE || loc != OCTGB_DEVICE) check_status(c);
     });
 }
 

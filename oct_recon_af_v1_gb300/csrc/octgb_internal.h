@@ -53,6 +53,21 @@ struct QueueTile {
 };
 constexpr int kMaxQueueTiles = 256;
 
+// float64 form of the spectral stage (exact.cu)
+struct ExactArgs {
+    const void* raw;          // (B, interf, kN) device, uint16 or int16
+    int B, interf, apod, nx;
+    int64_t n_ascans;         // B * nx
+    const int* apod_sum;      // (B, kN) integer sums of the apodisation lines (filled by launch_exact)
+    const int* start;         // [kN] first source sample of each output
+    const double* w;          // [taps][kN] float64 band weights, tap-major (padding 0)
+    int taps;
+    const double2* win;       // [kN] window / kN, float64 complex
+    const double2* tw;        // [kN] exp(+2 pi i k / kN), float64
+    float* mag;               // (n_ascans, kHalf) |X| rounded to float32
+};
+cudaError_t launch_exact(const ExactArgs& a, int dtype, int* sums, int num_sms, cudaStream_t st);
+
 struct SpectralArgs {
     const void* raw;          // (B, interf, kN), segment 0
     const void* seg[kMaxSeg]; // raw batches of n_seg tiles, each (B, interf, kN); seg[0] == raw

@@ -1,0 +1,75 @@
+"""Float64 form of the spectral stage (octgb_magnitude_exact) against the
+reference's float64 NumPy path (core/spectral.py:123-165 at precision
+"float64"), at the full size of the single-tile workload (50 x (25 + 500) x
+2048, 25.6 M codes with one shared clim): legacy codes within 1 LSB
+everywhere and bit-exact on at least 99.9 % of voxels, per dB level.  The
+form's only rounding of consequence is |X| to float32 at the end (~6e-8
+relative, a few 1e-4 of an LSB)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from oracle import numerics as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _db(m):
+    with np.errstate(divide="ignore"):
+        return 20 * np.log10(np.asarray(m, np.float64)[..., :1000])
+
+
+@pytest.fixture(scope="module")
+def case():
+    from oct_recon_af_v1_gb300 import synthetic as S
+    lam, beta = S.lambda_nm(), S.beta_ref_from_px(1e-5)
+    raw = S.generate_numpy(50, 500, 25, seed=0)
+    og = O.spectral_geometry(lam, beta, 1.33)
+    return dict(raw=raw, lam=lam, beta=beta, og=og, fp64=O.magnitude_numpy(raw, og, 25, np.float64))
+
+
+def test_float64_form_reaches_the_bound(gpu_ctx, case):
+    from oct_recon_af_v1_gb300 import geometry as G
+    c = case
+    sg = G.build_spectral_geometry(c["lam"], c["beta"], 1.33)
+    gpu_ctx.set_geometry(sg.sinc_idx, sg.sinc_w, sg.window)
+    mag = gpu_ctx.magnitude_exact(c["raw"], 25)
+    # |X| itself: float32 rounding of the float64 result
+    ref = c["fp64"]
+    rel = np.abs(mag.astype(np.float64) - ref) / np.maximum(np.abs(ref), 1e-300)
+    assert np.quantile(rel, 0.999) < 1e-7
+    d64, dg = _db(ref), _db(mag)
+    fin = np.isfinite(d64)
+    clim = (float(d64[fin].min()), float(d64[fin].max()))
+    rows = O.lsb_levels(dg, d64, clim)
+    print("\n" + O.format_levels("config 0, float64 form vs the reference's float64 path", rows))
+    overall = rows[-1]
+    assert overall["max_lsb"] <= 1, overall
+    assert overall["exact_frac"] >= 0.999, overall
+
+
+@pytest.mark.parametrize("B,nx", [(1, 1), (3, 5), (2, 129)])
+def test_float64_form_ragged_and_int16(gpu_ctx, case, B, nx):
+    from oct_recon_af_v1_gb300 import geometry as G
+    from oct_recon_af_v1_gb300 import synthetic as S
+    c = case
+    sg = G.build_spectral_geometry(c["lam"], c["beta"], 1.33)
+    gpu_ctx.set_geometry(sg.sinc_idx, sg.sinc_w, sg.window)
+    raw = S.generate_numpy(B, nx, 25, seed=B * 10 + nx)
+    ref = O.magnitude_numpy(raw, c["og"], 25, np.float64)
+    for arr in (raw, raw.astype(np.int16)):
+        got = gpu_ctx.magnitude_exact(arr, 25)
+        assert got.shape == (B, nx, 1024)
+        assert np.abs(got - ref).max() / np.abs(ref).max() < 1e-7
+
+
+def test_float64_form_rejects_float_raws(gpu_ctx, case):
+    from oct_recon_af_v1_gb300 import _lib
+    from oct_recon_af_v1_gb300 import geometry as G
+    c = case
+    sg = G.build_spectral_geometry(c["lam"], c["beta"], 1.33)
+    gpu_ctx.set_geometry(sg.sinc_idx, sg.sinc_w, sg.window)
+    with pytest.raises(_lib.OctgbError) as e:
+        gpu_ctx.magnitude_exact(c["raw"][:1].astype(np.float32), 25)
+    assert e.value.code == _lib.ERR_ARG and "integer raws" in str(e.value)
