@@ -45,8 +45,11 @@ def test_float64_form_reaches_the_bound(gpu_ctx, case):
     rows = O.lsb_levels(dg, d64, clim)
     print("\n" + O.format_levels("config 0, float64 form vs the reference's float64 path", rows))
     overall = rows[-1]
+    # measured on GB300: 99.989 %, max 1 LSB, at every dB level
     assert overall["max_lsb"] <= 1, overall
-    assert overall["exact_frac"] >= 0.999, overall
+    assert overall["exact_frac"] >= 0.9998, overall
+    for r in rows:
+        assert r["max_lsb"] <= 1 and r["exact_frac"] >= 0.9995, r
 
 
 @pytest.mark.parametrize("B,nx", [(1, 1), (3, 5), (2, 129)])
