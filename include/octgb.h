@@ -409,6 +409,16 @@ int octgb_cnn_conv3x3_relu_pool_tc(octgb_ctx *ctx, const float *x, const float *
  * w_scratch (cout * cin * 9 floats) for the flipped kernel. */
 int octgb_cnn_conv3x3_bwd(octgb_ctx *ctx, const float *x, const float *w, const float *dy, float *dx, float *dw,
                           float *db, float *w_scratch, int n, int cin, int cout, int h, int wd);
+/* octgb_cnn_conv3x3_bwd on the tensor cores (tcgen05.mma, BF16 operands,
+ * float32 accumulation): dw as nine pixel-contracting GEMMs whose per-CTA
+ * partial sums are added in a fixed order; dx as octgb_cnn_conv3x3_tc of dy
+ * with the flipped kernel (the float32 kernel where that shape is not
+ * supported); db as octgb_cnn_conv3x3_bwd.  Shapes: 1 <= cin <= 48, 1 <= cout
+ * <= 128, and a band of rows dividing h whose staged input fits in shared
+ * memory (wd up to about 1000).  Asynchronous; a bounded device wait that
+ * expires is reported by the next synchronising call (OCTGB_ERR_TIMEOUT). */
+int octgb_cnn_conv3x3_bwd_tc(octgb_ctx *ctx, const float *x, const float *w, const float *dy, float *dx, float *dw,
+                             float *db, float *w_scratch, int n, int cin, int cout, int h, int wd);
 /* p = 2x2 mean of relu(y) over `planes` planes of h x w (even), and its gradient. */
 int octgb_cnn_relu_pool(octgb_ctx *ctx, const float *y, float *p, int64_t planes, int h, int wd);
 int octgb_cnn_relu_pool_bwd(octgb_ctx *ctx, const float *dp, const float *y, float *dy, int64_t planes, int h,

@@ -84,7 +84,9 @@ SIGNATURES = {
                                   c_int]),
     "octgb_cnn_conv3x3_bwd": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                       c_void_p, c_int, c_int, c_int, c_int, c_int]),
-    "octgb_cnn_relu_pool": (c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_int, c_int]),
+    "octgb_cnn_conv3x3_bwd_tc": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                         c_void_p, c_int, c_int, c_int, c_int, c_int]),
+    "octgb_cnn_relu_pool":(c_int, [c_void_p, c_void_p, c_void_p, c_int64, c_int, c_int]),
     "octgb_cnn_relu_pool_bwd": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_int64, c_int, c_int]),
     "octgb_cnn_dense": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, c_int]),
     "octgb_cnn_dense_bwd": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,

@@ -167,6 +167,8 @@ struct octgb_ctx {
     DevBuf prec_w, prec_kb, prec_hi, prec_lo, prec_m, prec_x;
     // float64 form: band weights (tap-major), window / N and twiddles in float64
     DevBuf ex_w, ex_win, ex_tw;
+    DevBuf bias_part;                        // CNN training: per-plane sums of the bias gradient
+    DevBuf wgrad_part;                       // CNN training: per-CTA sums of the tensor-core weight gradient
     // dispersion scorer and focus profiles
     bool win_is_one = false;                 // geometry window is exactly 1 (plain linearisation)
     DevBuf disp_x, disp_hann, disp_phase, disp_a, disp_score, xmed;
@@ -358,7 +360,11 @@ const SlotTable& slot_table(octgb_ctx* c, int n_tiles, const int* plan_ids, int 
                 s.rs = hi - lo + 1;
                 s.off = off;
                 s.opc = p.opc ? 1 : 0;
-                off += s.xs * s.rs * (p.opc ? 2 : 1);
+                // one zero row after each A-scan's rows and one zero A-scan after the
+                // last, so the kernel's 2 x 2 reads need no bounds tests; an odd
+                // stride puts neighbouring A-scans in different banks
+                s.rst = (s.rs + 1) | 1;
+                off += (s.xs + 1) * s.rst * (p.opc ? 2 : 1);
                 slots[static_cast<size_t>(blk) * n_tiles + n++] = s;
             }
             counts[blk] = n;
@@ -492,7 +498,7 @@ int octgb_destroy(octgb_ctx* c) {
     for (DevBuf* b : {&c->w, &c->start, &c->win, &c->tw, &c->wsh, &c->s0, &c->raw, &c->apod, &c->out, &c->mm, &c->frames, &c->num,
                       &c->den, &c->plan_table, &c->run_mm, &c->magbuf, &c->dbbuf, &c->planemm, &c->segs, &c->qtable,
                       &c->qcounter, &c->disp_x, &c->disp_hann, &c->disp_phase, &c->disp_a, &c->disp_score, &c->xmed,
-                      &c->prec_w, &c->prec_kb, &c->prec_hi, &c->prec_lo, &c->prec_m, &c->prec_x, &c->ex_w, &c->ex_win, &c->ex_tw, &c->prep,
+                      &c->prec_w, &c->prec_kb, &c->prec_hi, &c->prec_lo, &c->prec_m, &c->prec_x, &c->ex_w, &c->ex_win, &c->ex_tw, &c->bias_part, &c->wgrad_part, &c->prep,
                       &c->prep_apod, &c->magrep, &c->srr, &c->gemm_part, &c->enc_bits, &c->enc_lut, &c->enc_slots, &c->enc_sizes})
         b->release();
     for (QTable* t : c->qtables) {
@@ -2031,12 +2037,46 @@ int octgb_cnn_conv3x3_bwd(octgb_ctx* c, const float* x, const float* w, const fl
         require(x && w && dy && dw && db, "NULL buffer");
         require(n >= 1 && cin >= 1 && cout >= 1 && h >= 1 && wd >= 1 && n <= 65535, "bad convolution shape");
         ck(launch_conv3x3_wgrad(x, dy, dw, n, cin, cout, h, wd, c->stream), "conv weight-gradient kernel");
-        ck(launch_bias_grad(dy, n, cout, static_cast<int64_t>(h) * wd, db, c->stream), "bias-gradient kernel");
-        c->launches += 2;
+        ck(c->bias_part.ensure(static_cast<size_t>(n) * cout * sizeof(float)), "cudaMalloc(bias partial sums)");
+        ck(launch_bias_grad(dy, n, cout, static_cast<int64_t>(h) * wd, db, c->bias_part.as<float>(), c->stream),
+           "bias-gradient kernel");
+        c->launches += (static_cast<int64_t>(h) * wd) % 4 == 0 ? 3 : 2;
         if (dx != nullptr) {
             require(w_scratch != nullptr, "w_scratch is NULL");
             ck(launch_flip_weights(w, cout, cin, w_scratch, c->stream), "weight flip kernel");
             ck(launch_conv3x3(dy, w_scratch, nullptr, dx, n, cout, cin, h, wd, c->stream), "conv kernel");
+            c->launches += 2;
+        }
+    });
+}
+
+int octgb_cnn_conv3x3_bwd_tc(octgb_ctx* c, const float* x, const float* w, const float* dy, float* dx, float* dw,
+                             float* db, float* w_scratch, int n, int cin, int cout, int h, int wd) {
+    return guarded(c, [&] {
+        require(x && w && dy && dw && db, "NULL buffer");
+        require(n >= 1 && cin >= 1 && cout >= 1 && h >= 1 && wd >= 1, "bad convolution shape");
+        const size_t parts = conv3x3_wgrad_tc_partials(n, cin, cout, h, wd, c->num_sms);
+        require(parts > 0, "tensor-core weight gradient: 1 <= cin <= 48, 1 <= cout <= 128 and a band of rows "
+                           "dividing the height whose staged input fits in shared memory");
+        ck(c->wgrad_part.ensure(parts * sizeof(float)), "cudaMalloc(weight-gradient partial sums)");
+        ck(launch_conv3x3_wgrad_tc(x, dy, dw, n, cin, cout, h, wd, c->wgrad_part.as<float>(), c->num_sms,
+                                   c->status_dev, c->stream),
+           "tensor-core weight-gradient kernel");
+        ck(c->bias_part.ensure(static_cast<size_t>(n) * cout * sizeof(float)), "cudaMalloc(bias partial sums)");
+        ck(launch_bias_grad(dy, n, cout, static_cast<int64_t>(h) * wd, db, c->bias_part.as<float>(), c->stream),
+           "bias-gradient kernel");
+        c->launches += 2 + ((static_cast<int64_t>(h) * wd) % 4 == 0 ? 2 : 1);
+        if (dx != nullptr) {
+            require(w_scratch != nullptr, "w_scratch is NULL");
+            ck(launch_flip_weights(w, cout, cin, w_scratch, c->stream), "weight flip kernel");
+            // the data gradient is the convolution of dy with the flipped kernel
+            // (cout -> cin channels): BF16 tensor cores where the shape allows
+            if (conv3x3_tc_supported(cout, cin, h, wd))
+                ck(launch_conv3x3_tc(dy, w_scratch, nullptr, dx, n, cout, cin, h, wd, 0, c->status_dev, c->stream,
+                                     true),
+                   "tensor-core conv kernel");
+            else
+                ck(launch_conv3x3(dy, w_scratch, nullptr, dx, n, cout, cin, h, wd, c->stream), "conv kernel");
             c->launches += 2;
         }
     });
@@ -2081,7 +2121,7 @@ int octgb_cnn_dense_bwd(octgb_ctx* c, const float* x, const float* w, float* dy,
             c->launches++;
         }
         ck(launch_gemm(dy, 1, out, x, in, 1, dw, in, out, in, m, 0, c->stream), "gemm kernel");
-        ck(launch_bias_grad(dy, m, out, 1, db, c->stream), "bias-gradient kernel");
+        ck(launch_bias_grad(dy, m, out, 1, db, nullptr, c->stream), "bias-gradient kernel");
         c->launches += 2;
         if (dx != nullptr) {
             ck(launch_gemm(dy, out, 1, w, in, 1, dx, in, m, in, out, 0, c->stream), "gemm kernel");

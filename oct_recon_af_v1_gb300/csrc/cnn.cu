@@ -374,6 +374,28 @@ __global__ void __launch_bounds__(256) k_bias_grad(const float* __restrict__ g, 
     }
 }
 
+// part[n * K + k] = sum of the plane g[n][k][0 .. inner) (inner a multiple of
+// 4): one block per plane, 16-byte loads, a fixed reduction order
+__global__ void __launch_bounds__(256) k_plane_sums(const float* __restrict__ g, int K, int64_t inner,
+                                                    float* __restrict__ part) {
+    __shared__ float red[8];
+    const int64_t plane = static_cast<int64_t>(blockIdx.y) * K + blockIdx.x;
+    const float4* p = reinterpret_cast<const float4*>(g + plane * inner);
+    float s = 0.f;
+    for (int64_t e = threadIdx.x; e < inner / 4; e += 256) {
+        const float4 v = p[e];
+        s += (v.x + v.y) + (v.z + v.w);
+    }
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float t = 0.f;
+        for (int w = 0; w < 8; ++w) t += red[w];
+        part[plane] = t;
+    }
+}
+
 // dense gradient through ReLU: g[i] = pre[i] > 0 ? g[i] : 0
 __global__ void k_relu_bwd(float* __restrict__ g, const float* __restrict__ pre, int64_t n) {
     const int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
@@ -509,7 +531,16 @@ cudaError_t launch_bias_relu(float* y, const float* b, int M, int N, float* out,
     return cudaGetLastError();
 }
 
-cudaError_t launch_bias_grad(const float* g, int Nn, int K, int64_t inner, float* db, cudaStream_t st) {
+cudaError_t launch_bias_grad(const float* g, int Nn, int K, int64_t inner, float* db, float* part, cudaStream_t st) {
+    if (inner >= 4 && inner % 4 == 0 && part != nullptr) {
+        // planes of a convolution gradient: one block per (image, channel),
+        // then the Nn plane sums of each channel in order
+        k_plane_sums<<<dim3(K, Nn), 256, 0, st>>>(g, K, inner, part);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        k_bias_grad<<<K, 256, 0, st>>>(part, Nn, K, 1, db);
+        return cudaGetLastError();
+    }
     k_bias_grad<<<K, 256, 0, st>>>(g, Nn, K, inner, db);
     return cudaGetLastError();
 }

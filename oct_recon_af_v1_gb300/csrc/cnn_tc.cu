@@ -24,6 +24,7 @@
 // Persistent over tiles.  Every mbarrier wait is bounded; on expiry the CTA
 // records the status, waits (bounded) for its MMAs, frees its TMEM and
 // returns.
+#include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -67,6 +68,20 @@ __device__ __forceinline__ uint32_t pack_h2(float a, float b) {
     return *reinterpret_cast<const uint32_t*>(&h);
 }
 
+__device__ __forceinline__ uint32_t pack_bf2(float a, float b) {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<const uint32_t*>(&h);
+}
+
+// two operand values in the kernel's 16-bit type, the first in the low half
+template <bool kBf16>
+__device__ __forceinline__ uint32_t pack2(float a, float b) {
+    return kBf16 ? pack_bf2(a, b) : pack_h2(a, b);
+}
+
+// kind::f16 A and B formats: 0 = FP16, 1 = BF16 (both operands the same type)
+constexpr uint32_t kIdescBf16 = (1u << 7) | (1u << 10);
+
 __device__ __forceinline__ bool conv_wait(uint64_t* bar, uint32_t parity, ConvBars& S, int* status) {
     bool ok = true;
     if (*reinterpret_cast<volatile int*>(&S.abort) == 0) {
@@ -101,6 +116,7 @@ __device__ __forceinline__ void unit_tile(const ConvGeom& g, int64_t u, int h, i
     }
 }
 
+template <bool kBf16>
 __global__ void __launch_bounds__(kCThreads, 4)
     k_conv3x3_tc(const float* __restrict__ x, const float* __restrict__ w, const float* __restrict__ bias,
                  float* __restrict__ y, const ConvGeom g, int* status) {
@@ -142,7 +158,8 @@ __global__ void __launch_bounds__(kCThreads, 4)
             v[e] = c < g.cin ? w[((static_cast<int64_t>(co) * g.cin + c) * 3 + dy) * 3 + dx] : 0.f;
         }
         *reinterpret_cast<uint4*>(B + static_cast<uint32_t>(kb) * b_chunk + co * 16) =
-            make_uint4(pack_h2(v[0], v[1]), pack_h2(v[2], v[3]), pack_h2(v[4], v[5]), pack_h2(v[6], v[7]));
+            make_uint4(pack2<kBf16>(v[0], v[1]), pack2<kBf16>(v[2], v[3]), pack2<kBf16>(v[4], v[5]),
+                       pack2<kBf16>(v[6], v[7]));
     }
     // the padding chunks of every staged buffer (never rewritten)
     {
@@ -157,7 +174,7 @@ __global__ void __launch_bounds__(kCThreads, 4)
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = S.tmem;
-    const uint32_t idesc = mma_idesc_f16(kCM, g.cout);
+    const uint32_t idesc = mma_idesc_f16(kCM, g.cout) | (kBf16 ? kIdescBf16 : 0u);
     // the staged source pixels this thread loads: p = tid + 128 k (row, column), -1 past the block
     int prs[kCSlots], pcs[kCSlots];
 #pragma unroll
@@ -258,8 +275,8 @@ __global__ void __launch_bounds__(kCThreads, 4)
                         v[e] = (off[k] >= 0 && e < ne) ? __ldg(pe) : 0.f;
                         pe += hw;
                     }
-                    const uint4 q = make_uint4(pack_h2(v[0], v[1]), pack_h2(v[2], v[3]), pack_h2(v[4], v[5]),
-                                               pack_h2(v[6], v[7]));
+                    const uint4 q = make_uint4(pack2<kBf16>(v[0], v[1]), pack2<kBf16>(v[2], v[3]),
+                                               pack2<kBf16>(v[4], v[5]), pack2<kBf16>(v[6], v[7]));
                     const int p = tid + kCThreads * k;
                     if (g.halo) {
                         X[c8 * g.pix_c + p] = q;
@@ -333,6 +350,273 @@ __global__ void __launch_bounds__(kCThreads, 4)
                      : "memory");
 }
 
+
+// ---------------------------------------------------------------- weight gradient
+// dw[k][c][ty][tx] = sum over the images and output pixels (oy, ox) of
+//   dy[k](oy, ox) * x[c](oy + ty - 1, ox + tx - 1)          (x zero outside the image)
+// as nine GEMMs that contract over pixels: M = 128 rows = the output channels
+// (rows past cout read in-bounds data of the following chunks into
+// accumulator rows that are never read), N = the input channels rounded up to
+// 16, K = 16 pixels per MMA; BF16 operands (gradients span float32's exponent
+// range), float32 accumulation.  A tile is R image rows.  Its input rows
+// y0 - 1 .. y0 + R are staged with one zero column on either side (row pitch
+// Wp = W + 2) channel-contiguous ([channel group][pixel][8 channels x 2 B],
+// the MN-major B operand), and dy on the same pitch pixel-contiguous ([8-pixel
+// chunk][output channel][8 pixels x 2 B], the K-major A operand) with zeros in
+// the two pad columns: output pixel q = r * Wp + ox meets input pixel
+// q + ty * Wp + tx, so tap (ty, tx) is the staged input block seen from that
+// pixel on (a descriptor offset of 16 bytes a pixel, no shifted copies).  The
+// nine accumulators (9 x N TMEM columns) stay in TMEM over all the CTA's
+// tiles; the staged blocks are double-buffered, so one thread issues tile j's
+// MMAs while the CTA stages tile j + 1.  Each CTA then writes its partial sums
+// and k_sum_partials adds them in CTA order (the result does not depend on
+// timing).
+constexpr int kWThreads = 256;
+
+struct WgradGeom {
+    int n, C, K, H, W;
+    int R, Wp, Q;        // rows per tile, staged row pitch, pixels per tile (R x Wp rounded up to 32)
+    int N;               // MMA N: C rounded up to 16
+    int cg, kg;          // channel groups of 8 staged (x: N / 8; dy: ceil(K / 8))
+    int xpix;            // staged input pixels per channel group (Q + 2 Wp + 2, rounded up to 8)
+    int nbuf;            // staged blocks: 2 (tile j + 1 stages while tile j's MMAs run), or 1 for wide rows
+    int tiles_img;
+    int64_t n_units;
+    uint32_t xbytes, stage, smem;
+    int tmem_cols;
+};
+
+struct WgradBars {
+    uint64_t x[2], drain;
+    uint32_t tmem;
+    int abort;
+    int drained;
+};
+
+__device__ __forceinline__ bool wg_wait(uint64_t* bar, uint32_t parity, WgradBars& S, int* status) {
+    bool ok = true;
+    if (*reinterpret_cast<volatile int*>(&S.abort) == 0) {
+        ok = mbar_wait_bounded(bar, parity, status);
+        if (!ok) atomicExch(&S.abort, 1);
+    } else {
+        ok = false;
+    }
+    return __syncthreads_and(ok ? 1 : 0) != 0;
+}
+
+__global__ void __launch_bounds__(kWThreads, 1)
+    k_conv3x3_wgrad_tc(const float* __restrict__ x, const float* __restrict__ dy, float* __restrict__ part,
+                       const WgradGeom g, int* status) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    __shared__ WgradBars S;
+    uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int64_t hw = static_cast<int64_t>(g.H) * g.W;
+    const int kp = 8 * g.kg;
+
+    if (tid == 0) {
+        mbar_init(&S.x[0], 1);
+        mbar_init(&S.x[1], 1);
+        mbar_init(&S.drain, 1);
+        S.abort = 0;
+        S.drained = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&S.tmem)),
+                     "r"(g.tmem_cols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = S.tmem;
+    // BF16 A (K-major) and B (MN-major: bit 16)
+    const uint32_t idesc = mma_idesc_f16(128, g.N) | kIdescBf16 | (1u << 16);
+    const uint32_t lbo_a = static_cast<uint32_t>(kp) * 16;      // next 8-pixel chunk of dy
+    const uint32_t lbo_b = static_cast<uint32_t>(g.xpix) * 16;  // next channel group of x
+    const int ksteps = g.Q / 16;
+    const int dtasks = (g.Q / 32) * g.kg * 32;
+
+    uint32_t j = 0;
+    bool ok = true;
+    for (int64_t u = blockIdx.x; u < g.n_units; u += gridDim.x, ++j) {
+        const int b = g.nbuf == 2 ? static_cast<int>(j & 1u) : 0;
+        if (j >= static_cast<uint32_t>(g.nbuf)) {
+            // the MMAs of the tile staged nbuf tiles ago have read buffer b
+            const uint32_t use = g.nbuf == 2 ? (j - 2) >> 1 : j - 1;
+            ok = wg_wait(&S.x[b], use & 1u, S, status);
+            if (!ok) break;
+        }
+        const int img = static_cast<int>(u / g.tiles_img);
+        const int y0 = static_cast<int>(u - static_cast<int64_t>(img) * g.tiles_img) * g.R;
+        uint8_t* Xs = base + b * g.stage;
+        uint8_t* Ds = Xs + g.xbytes;
+        // input block: pixel i = r * Wp + cc is x(y0 - 1 + r, cc - 1); zero
+        // outside the image and past the R + 2 staged rows
+        const float* xi = x + static_cast<int64_t>(img) * g.C * hw;
+        for (int i = tid; i < g.xpix; i += kWThreads) {
+            const int r = i / g.Wp, cc = i - r * g.Wp;
+            const int iy = y0 - 1 + r, ix = cc - 1;
+            const bool in = r < g.R + 2 && iy >= 0 && iy < g.H && ix >= 0 && ix < g.W;
+            const float* p = xi + (in ? static_cast<int64_t>(iy) * g.W + ix : 0);
+            for (int c8 = 0; c8 < g.cg; ++c8) {
+                float v[8];
+#pragma unroll
+                for (int e = 0; e < 8; ++e) {
+                    const int c = 8 * c8 + e;
+                    v[e] = (in && c < g.C) ? __ldg(p + static_cast<int64_t>(c) * hw) : 0.f;
+                }
+                *reinterpret_cast<uint4*>(Xs + (static_cast<uint32_t>(c8) * g.xpix + i) * 16u) =
+                    make_uint4(pack_bf2(v[0], v[1]), pack_bf2(v[2], v[3]), pack_bf2(v[4], v[5]), pack_bf2(v[6], v[7]));
+            }
+        }
+        // dy block: chunk q8 of channel k holds q = 8 q8 .. 8 q8 + 7, q = r * Wp
+        // + ox is dy(y0 + r, ox), zero for ox >= W and r >= R.  A warp takes 8
+        // channels x 4 chunks, so a quarter-warp stores 128 contiguous bytes.
+        const float* di = dy + static_cast<int64_t>(img) * g.K * hw + static_cast<int64_t>(y0) * g.W;
+        for (int i = tid; i < dtasks; i += kWThreads) {
+            const int l = i & 31, w = i >> 5;
+            const int qb = w / g.kg, kgi = w - qb * g.kg;
+            const int k = 8 * kgi + (l & 7);
+            const int q8 = 4 * qb + (l >> 3);
+            int r = (8 * q8) / g.Wp;
+            int ox = 8 * q8 - r * g.Wp;
+            const float* dk = di + static_cast<int64_t>(k < g.K ? k : 0) * hw;
+            float v[8];
+#pragma unroll
+            for (int e = 0; e < 8; ++e) {
+                v[e] = (k < g.K && r < g.R && ox < g.W) ? __ldg(dk + r * g.W + ox) : 0.f;
+                if (++ox == g.Wp) {
+                    ox = 0;
+                    ++r;
+                }
+            }
+            *reinterpret_cast<uint4*>(Ds + (static_cast<uint32_t>(q8) * kp + k) * 16u) =
+                make_uint4(pack_bf2(v[0], v[1]), pack_bf2(v[2], v[3]), pack_bf2(v[4], v[5]), pack_bf2(v[6], v[7]));
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        tc_fence_before();
+        __syncthreads();
+        if (tid == 0) {
+            tc_fence_after();
+            const uint64_t da0 = smem_desc(Ds, lbo_a, 128);
+            const uint64_t db0 = smem_desc(Xs, lbo_b, 128);
+            for (int tap = 0; tap < 9; ++tap) {
+                const int ty = tap / 3, tx = tap - 3 * ty;
+                // descriptor addresses are in 16-byte units: one unit per staged pixel of x
+                const uint64_t dbt = db0 + static_cast<uint64_t>(ty * g.Wp + tx);
+                const uint32_t d_tmem = tmem + static_cast<uint32_t>(tap * g.N);
+                for (int ks = 0; ks < ksteps; ++ks) {
+                    const uint64_t da = da0 + static_cast<uint64_t>(ks) * (2u * lbo_a >> 4);
+                    const uint64_t db = dbt + static_cast<uint64_t>(16 * ks);
+                    mma_f16_id(d_tmem, da, db, idesc, (j > 0 || ks > 0) ? 1u : 0u);
+                }
+            }
+            mma_commit(&S.x[b]);
+        }
+    }
+    // every MMA this CTA issued has completed before the accumulators are read
+    __syncthreads();
+    if (tid == 0) {
+        mma_commit(&S.drain);
+        S.drained = mbar_wait_bounded(&S.drain, 0, status) ? 1 : 0;
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (ok && S.drained) {
+        // warp w reads TMEM lanes 32 (w % 4) .. + 31 (output channels), 32-column
+        // chunks w / 4, w / 4 + 2, ...; column t * N + c is tap t of channel c
+        const int quarter = warp & 3;
+        const int k = 32 * quarter + lane;
+        const int cols = 9 * g.N;
+        const int64_t kc9 = static_cast<int64_t>(g.K) * g.C * 9;
+        if (32 * quarter < g.K) {
+            for (int ch = warp >> 2; 32 * ch < cols; ch += kWThreads / 128) {
+                float v[32];
+                tmem_ld32(tmem + (static_cast<uint32_t>(32 * quarter) << 16) + static_cast<uint32_t>(32 * ch), v);
+                if (k < g.K) {
+                    float* pk = part + blockIdx.x * kc9 + static_cast<int64_t>(k) * g.C * 9;
+#pragma unroll
+                    for (int i = 0; i < 32; ++i) {
+                        const int col = 32 * ch + i;
+                        const int t = col / g.N, c = col - t * g.N;
+                        if (col < cols && c < g.C) pk[c * 9 + t] = v[i];
+                    }
+                }
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(g.tmem_cols)
+                     : "memory");
+}
+
+// out[i] = sum over b < nb (in order) of part[b * n + i]
+__global__ void k_sum_partials(const float* __restrict__ part, int nb, int64_t n, float* __restrict__ out) {
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        float s = 0.f;
+        for (int b = 0; b < nb; ++b) s += part[b * n + i];
+        out[i] = s;
+    }
+}
+
+// tile geometry: the band of R rows (R dividing H) with at least 512 pixels,
+// or the tallest whose staged blocks fit (two, else one for wide rows)
+bool wgrad_geom(int n, int cin, int cout, int H, int W, WgradGeom& g) {
+    if (n < 1 || cin < 1 || cin > 48 || cout < 1 || cout > 128 || H < 1 || W < 1) return false;
+    g = WgradGeom{};
+    g.n = n;
+    g.C = cin;
+    g.K = cout;
+    g.H = H;
+    g.W = W;
+    g.N = (cin + 15) / 16 * 16;
+    g.cg = g.N / 8;
+    g.kg = (cout + 7) / 8;
+    g.Wp = W + 2;
+    const uint32_t budget = 227u * 1024u;
+    g.R = 0;
+    for (int nbuf = 2; nbuf >= 1 && g.R == 0; --nbuf) {
+        for (int R = 1; R <= H; ++R) {
+            if (H % R != 0) continue;
+            const int Q = (R * g.Wp + 31) / 32 * 32;
+            const int xpix = (Q + 2 * g.Wp + 2 + 7) / 8 * 8;
+            const uint32_t xbytes = static_cast<uint32_t>(g.cg) * xpix * 16u;
+            const uint32_t dbytes = static_cast<uint32_t>(Q / 8) * 8u * g.kg * 16u;
+            const uint32_t stage = (xbytes + dbytes + 127u) & ~127u;
+            // the stages, 2 KB past the last one for the unused A rows, 1 KB alignment
+            const uint32_t smem = static_cast<uint32_t>(nbuf) * stage + 2048u + 1024u;
+            if (smem > budget) break;
+            g.R = R;
+            g.Q = Q;
+            g.xpix = xpix;
+            g.xbytes = xbytes;
+            g.stage = stage;
+            g.smem = smem;
+            g.nbuf = nbuf;
+            if (Q >= 512) break;         // 32+ K steps a tap: enough per tile
+        }
+    }
+    if (g.R == 0) return false;
+    g.tiles_img = H / g.R;
+    g.n_units = static_cast<int64_t>(n) * g.tiles_img;
+    const int cols = 9 * g.N;
+    g.tmem_cols = cols <= 256 ? 256 : 512;
+    return cols <= 512;
+}
+
+int wgrad_grid(const WgradGeom& g, int num_sms) {
+    const int per_sm = g.tmem_cols == 512 || g.smem > 113u * 1024u ? 1 : 2;
+    const int64_t slots = static_cast<int64_t>(per_sm) * num_sms;
+    return static_cast<int>(g.n_units < slots ? g.n_units : slots);
+}
 }  // namespace
 
 bool conv3x3_tc_supported(int cin, int cout, int H, int W) {
@@ -346,7 +630,7 @@ bool conv3x3_tc_pool_supported(int cin, int cout, int H, int W) {
 }
 
 cudaError_t launch_conv3x3_tc(const float* x, const float* w, const float* b, float* y, int n, int cin, int cout,
-                              int H, int W, int pool, int* status, cudaStream_t st) {
+                              int H, int W, int pool, int* status, cudaStream_t st, bool bf16) {
     if (!conv3x3_tc_supported(cin, cout, H, W)) return cudaErrorInvalidValue;
     if (pool && !conv3x3_tc_pool_supported(cin, cout, H, W)) return cudaErrorInvalidValue;
     ConvGeom g{};
@@ -374,8 +658,8 @@ cudaError_t launch_conv3x3_tc(const float* x, const float* w, const float* b, fl
     g.tmem_cols = cols <= 32 ? 32 : (cols <= 64 ? 64 : (cols <= 128 ? 128 : (cols <= 256 ? 256 : 512)));
     if (g.n_units == 0) return cudaSuccess;
     if (g.smem > 227u * 1024u || g.pix_c > kCSlots * kCThreads) return cudaErrorInvalidValue;
-    cudaError_t e = cudaFuncSetAttribute(k_conv3x3_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         static_cast<int>(g.smem));
+    auto kern = bf16 ? k_conv3x3_tc<true> : k_conv3x3_tc<false>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(g.smem));
     if (e != cudaSuccess) return e;
     // CTAs per SM: shared memory, registers and TMEM columns
     int dev = 0, sms = 0, smem_sm = 0;
@@ -383,7 +667,7 @@ cudaError_t launch_conv3x3_tc(const float* x, const float* w, const float* b, fl
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
     cudaFuncAttributes fa{};
-    e = cudaFuncGetAttributes(&fa, k_conv3x3_tc);
+    e = cudaFuncGetAttributes(&fa, kern);
     if (e != cudaSuccess) return e;
     const int by_smem = smem_sm / static_cast<int>(g.smem + fa.sharedSizeBytes + 1024);
     const int regs = (fa.numRegs + 7) / 8 * 8;
@@ -394,7 +678,29 @@ cudaError_t launch_conv3x3_tc(const float* x, const float* w, const float* b, fl
     per_sm = per_sm < 1 ? 1 : per_sm;
     const int64_t slots = static_cast<int64_t>(per_sm) * sms;
     const int64_t grid = g.n_units < slots ? g.n_units : slots;
-    k_conv3x3_tc<<<static_cast<unsigned int>(grid), kCThreads, g.smem, st>>>(x, w, b, y, g, status);
+    kern<<<static_cast<unsigned int>(grid), kCThreads, g.smem, st>>>(x, w, b, y, g, status);
+    return cudaGetLastError();
+}
+
+size_t conv3x3_wgrad_tc_partials(int n, int cin, int cout, int H, int W, int num_sms) {
+    WgradGeom g;
+    if (!wgrad_geom(n, cin, cout, H, W, g)) return 0;
+    return static_cast<size_t>(wgrad_grid(g, num_sms)) * cout * cin * 9;
+}
+
+cudaError_t launch_conv3x3_wgrad_tc(const float* x, const float* dy, float* dw, int n, int cin, int cout, int H,
+                                    int W, float* partials, int num_sms, int* status, cudaStream_t st) {
+    WgradGeom g;
+    if (!wgrad_geom(n, cin, cout, H, W, g) || partials == nullptr) return cudaErrorInvalidValue;
+    const int grid = wgrad_grid(g, num_sms);
+    cudaError_t e = cudaFuncSetAttribute(k_conv3x3_wgrad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(g.smem));
+    if (e != cudaSuccess) return e;
+    k_conv3x3_wgrad_tc<<<grid, kWThreads, g.smem, st>>>(x, dy, partials, g, status);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    const int64_t total = static_cast<int64_t>(cout) * cin * 9;
+    k_sum_partials<<<static_cast<unsigned int>((total + 255) / 256), 256, 0, st>>>(partials, grid, total, dw);
     return cudaGetLastError();
 }
 

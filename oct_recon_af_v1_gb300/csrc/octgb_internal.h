@@ -142,7 +142,7 @@ struct StitchSlot {               // one tile touching one output block
     int r_lo, rs;                 // rows (relative to r0) read
     int off;                      // float offset of the patch in shared memory
     int opc;                      // optical-path correction on (patch of F follows)
-    int pad;
+    int rst;                      // patch stride per A-scan: rs + a zero row, made odd (distinct banks)
 };
 cudaError_t launch_stitch_frames(const StitchDev* plans_dev, const TileList& tiles, const StitchSlot* slots,
                                  const int* slot_count, int ns_max, size_t patch_smem_bytes, const float* mag,
@@ -238,12 +238,20 @@ cudaError_t launch_image_cols(const float* zcol, int n_probe, int nb, int nx, in
                               cudaStream_t st);
 cudaError_t launch_image_norm(float* img, int n_images, int64_t per_image, cudaStream_t st);
 // tensor-core 3x3 convolution (cnn_tc.cu): same contract as launch_conv3x3 for
-// the shapes conv3x3_tc_supported accepts; FP16 operands, float32 accumulation
-// (pool: ReLU + 2x2 mean fused, y is then (n, cout, H/2, W/2))
+// the shapes conv3x3_tc_supported accepts; FP16 operands (BF16 with bf16: the
+// data gradient, whose values span float32's exponent range), float32
+// accumulation (pool: ReLU + 2x2 mean fused, y is then (n, cout, H/2, W/2))
 bool conv3x3_tc_supported(int cin, int cout, int H, int W);
 bool conv3x3_tc_pool_supported(int cin, int cout, int H, int W);
 cudaError_t launch_conv3x3_tc(const float* x, const float* w, const float* b, float* y, int n, int cin, int cout,
-                              int H, int W, int pool, int* status, cudaStream_t st);
+                              int H, int W, int pool, int* status, cudaStream_t st, bool bf16 = false);
+// weight gradient of the 3x3 convolution on the tensor cores (cnn_tc.cu; BF16
+// operands, float32 accumulation): dw (cout, cin, 3, 3) from x (n, cin, H, W)
+// and dy (n, cout, H, W).  conv3x3_wgrad_tc_partials: the float count of the
+// per-CTA partial sums the launch needs (0: shape not supported).
+size_t conv3x3_wgrad_tc_partials(int n, int cin, int cout, int H, int W, int num_sms);
+cudaError_t launch_conv3x3_wgrad_tc(const float* x, const float* dy, float* dw, int n, int cin, int cout, int H,
+                                    int W, float* partials, int num_sms, int* status, cudaStream_t st);
 cudaError_t launch_conv3x3(const float* x, const float* w, const float* b, float* y, int Nn, int C, int K, int H,
                            int W, cudaStream_t st);
 cudaError_t launch_flip_weights(const float* w, int K, int C, float* wf, cudaStream_t st);
@@ -260,7 +268,9 @@ cudaError_t launch_gemm_split(const float* A, int64_t sa0, int64_t sa1, const fl
                               float* C, int64_t ldc, int M, int N, int K, int accumulate, int S, float* partial,
                               cudaStream_t st);
 cudaError_t launch_bias_relu(float* y, const float* b, int M, int N, float* out, cudaStream_t st);
-cudaError_t launch_bias_grad(const float* g, int Nn, int K, int64_t inner, float* db, cudaStream_t st);
+// db[k] = sum over n and inner of g[n][k][inner]; part (Nn * K floats, optional)
+// takes the plane sums of the two-pass form used when inner is a multiple of 4
+cudaError_t launch_bias_grad(const float* g, int Nn, int K, int64_t inner, float* db, float* part, cudaStream_t st);
 cudaError_t launch_relu_bwd(float* g, const float* pre, int64_t n, cudaStream_t st);
 cudaError_t launch_mse(const float* pred, const float* t, int n, float* grad, double* loss, cudaStream_t st);
 cudaError_t launch_adam(float* p, const float* g, float* m, float* v, int64_t n, float lr, float b1, float b2,

@@ -199,16 +199,10 @@ __global__ void __launch_bounds__(kStThreads) k_stitch_frames(const StitchDev* _
     // dynamic shared memory: per-slot row / column parameters, then the patches
     extern __shared__ __align__(16) float smem_all[];
     __shared__ StitchSlot slot[kMaxSeg];
-    int* zr_s = reinterpret_cast<int*>(smem_all);                  // [ns_max][kFZ]
-    float* wz0_s = smem_all + ns_max * kFZ;
-    float* wz1_s = wz0_s + ns_max * kFZ;
-    float* fz0_s = wz1_s + ns_max * kFZ;                          // F of the row's two taps
-    float* fz1_s = fz0_s + ns_max * kFZ;
-    float* dz_s = fz1_s + ns_max * kFZ;                           // depth-interpolated F
-    int* xr_s = reinterpret_cast<int*>(dz_s + ns_max * kFZ);      // [ns_max][kBlk]
-    float* wx0_s = reinterpret_cast<float*>(xr_s + ns_max * kBlk);
-    float* wx1_s = wx0_s + ns_max * kBlk;
-    float* sm = wx1_s + ns_max * kBlk;
+    float4* rowp = reinterpret_cast<float4*>(smem_all);           // [ns_max][kFZ] {zr, w0, w1, F interpolated}
+    float2* rowf = reinterpret_cast<float2*>(rowp + ns_max * kFZ); // [ns_max][kFZ] {F of the row's two taps}
+    float4* colp = reinterpret_cast<float4*>(rowf + ns_max * kFZ); // [ns_max][kBlk] {x0, wx0, wx1 (0 past the patch)}
+    float* sm = reinterpret_cast<float*>(colp + ns_max * kBlk);
     const int f = blockIdx.z;
     const int zb = blockIdx.y * kFZ;
     const int cb = blockIdx.x * kBlk;
@@ -220,7 +214,9 @@ __global__ void __launch_bounds__(kStThreads) k_stitch_frames(const StitchDev* _
 
     // 1. stage each contributing tile's interpolation parameters and its
     //    magnitude patch (a * F, and F when the optical-path correction makes
-    //    it depend on the A-scan); depth fastest in the patch
+    //    it depend on the A-scan); depth fastest in the patch, one zero row
+    //    after each A-scan's rows and one zero A-scan after the last (stride
+    //    s.rst), so every 2 x 2 read below is in the patch
     for (int k = 0; k < ns; ++k) {
         const StitchSlot s = slot[k];
         const StitchDev& p = plans[tl.id[s.t]];
@@ -232,30 +228,37 @@ __global__ void __launch_bounds__(kStThreads) k_stitch_frames(const StitchDev* _
             const float w0 = zr >= 0 ? p.wz0[zo] : 0.f, w1 = zr >= 0 ? p.wz1[zo] : 0.f;
             const bool has_r1 = zr >= 0 && zr - s.r_lo + 1 < s.rs;
             const float fa = zr >= 0 ? p.fz[zr] : 0.f, fb = has_r1 ? p.fz[zr + 1] : 0.f;
-            zr_s[k * kFZ + tid] = zr;
-            wz0_s[k * kFZ + tid] = w0;
-            wz1_s[k * kFZ + tid] = w1;
-            fz0_s[k * kFZ + tid] = fa;
-            fz1_s[k * kFZ + tid] = fb;
-            dz_s[k * kFZ + tid] = fmaf(fb, w1, fa * w0);
+            rowp[k * kFZ + tid] = make_float4(__int_as_float(zr), w0, w1, fmaf(fb, w1, fa * w0));
+            rowf[k * kFZ + tid] = make_float2(fa, fb);
         } else if (tid < kFZ + kBlk) {
             const int cc = cb + tid - kFZ - p.c0;
             const int xr = (cc >= 0 && cc < p.C) ? p.xr[cc] : -1;
-            xr_s[k * kBlk + tid - kFZ] = xr;
-            wx0_s[k * kBlk + tid - kFZ] = xr >= 0 ? p.wx0[cc] : 0.f;
-            wx1_s[k * kBlk + tid - kFZ] = xr >= 0 ? p.wx1[cc] : 0.f;
+            const int x0 = xr - s.x_lo;
+            // the second lateral tap outside the patch contributes nothing
+            // (its column is the zero A-scan): its weight is 0 for the den term too
+            const bool has_x1 = x0 + 1 < s.xs;
+            colp[k * kBlk + tid - kFZ] = make_float4(__int_as_float(xr >= 0 ? x0 : -1), xr >= 0 ? p.wx0[cc] : 0.f,
+                                                     xr >= 0 && has_x1 ? p.wx1[cc] : 0.f, 0.f);
         }
         const float* mag_f = mag + s.t * mag_tile_stride + static_cast<int64_t>(f) * n_tile_x * kHalf;
         float* pa = sm + s.off;
-        float* pf = pa + s.xs * s.rs;
+        float* pf = pa + (s.xs + 1) * s.rst;
         const int fy = f0 + f;
+        // zero rows and the zero A-scan (plain stores, before the barrier)
+        for (int i = tid; i < (s.xs + 1) * s.rst; i += kStThreads) {
+            const int xx = i / s.rst, rr = i - xx * s.rst;
+            if (xx == s.xs || rr >= s.rs) {
+                pa[i] = 0.f;
+                if (s.opc) pf[i] = 0.f;
+            }
+        }
         // the patch is copied as is (asynchronous 4-byte copies, every slot's
         // in flight at once); the focus weight multiplies it when it is read,
         // the same single product a * F.  64 consecutive threads copy 64
         // consecutive rows of one A-scan, four A-scans per pass
         for (int rr = tid & 63; rr < s.rs; rr += 64)
             for (int xx = tid >> 6; xx < s.xs; xx += kStThreads / 64) {
-                const int i = xx * s.rs + rr;
+                const int i = xx * s.rst + rr;
                 const int x = s.x_lo + xx;
                 const int ra = p.r0 + s.r_lo + rr;
                 int src = ra;
@@ -274,53 +277,48 @@ __global__ void __launch_bounds__(kStThreads) k_stitch_frames(const StitchDev* _
     asm volatile("cp.async.wait_all;" ::: "memory");
     __syncthreads();
 
-    // 2. per voxel: tiles in order, depth (Wz) then lateral (WxT) interpolation
+    // 2. per voxel: tiles in order, depth (Wz) then lateral (WxT) interpolation.
+    //    A tap outside the patch reads a zero, so a * F and F of it are the
+    //    zeros the reference's operators give there.
     const int tx = tid & (kBlk - 1), ty = tid / kBlk;
     const int c = cb + tx;
     float an[kFRows], ad[kFRows];
 #pragma unroll
     for (int q = 0; q < kFRows; ++q) an[q] = ad[q] = 0.f;
     for (int k = 0; k < ns; ++k) {
-        const int xr = xr_s[k * kBlk + tx];
-        if (xr < 0) continue;
+        const float4 cp = colp[k * kBlk + tx];
+        const int x0 = __float_as_int(cp.x);
+        if (x0 < 0) continue;
         const StitchSlot s = slot[k];
         const float* pa = sm + s.off;
-        const float* pf = pa + s.xs * s.rs;
+        const float* pf = pa + (s.xs + 1) * s.rst;
         const bool opc = s.opc != 0;
-        const int x0 = xr - s.x_lo;
-        const bool has_x1 = x0 + 1 < s.xs;
-        const float wx0 = wx0_s[k * kBlk + tx], wx1 = wx1_s[k * kBlk + tx];
+        const float wx0 = cp.y, wx1 = cp.z;
 #pragma unroll
         for (int q = 0; q < kFRows; ++q) {
             const int z = ty + 8 * q;
-            const int zr = zr_s[k * kFZ + z];
+            const float4 rp = rowp[k * kFZ + z];
+            const int zr = __float_as_int(rp.x);
             if (zr < 0) continue;
-            const int rr = zr - s.r_lo;
-            const bool has_r1 = rr + 1 < s.rs;
-            const float w0 = wz0_s[k * kFZ + z], w1 = wz1_s[k * kFZ + z];
-            const float* a0p = pa + x0 * s.rs + rr;
+            const int o = x0 * s.rst + zr - s.r_lo;
+            const float w0 = rp.y, w1 = rp.z;
             float f00, f01, f10, f11, d0, d1;
             if (opc) {
-                const float* f0p = pf + x0 * s.rs + rr;
-                f00 = f0p[0];
-                f01 = has_r1 ? f0p[1] : 0.f;
-                f10 = has_x1 ? f0p[s.rs] : 0.f;
-                f11 = has_x1 && has_r1 ? f0p[s.rs + 1] : 0.f;
+                f00 = pf[o];
+                f01 = pf[o + 1];
+                f10 = pf[o + s.rst];
+                f11 = pf[o + s.rst + 1];
                 d0 = fmaf(f01, w1, f00 * w0);
                 d1 = fmaf(f11, w1, f10 * w0);
             } else {
-                // the same values as the general form with F10 = F00, F11 = F01
-                f00 = fz0_s[k * kFZ + z];
-                f01 = fz1_s[k * kFZ + z];
-                f10 = has_x1 ? f00 : 0.f;
-                f11 = has_x1 ? f01 : 0.f;
-                d0 = dz_s[k * kFZ + z];
-                d1 = has_x1 ? d0 : 0.f;
+                const float2 ff = rowf[k * kFZ + z];
+                f00 = f10 = ff.x;
+                f01 = f11 = ff.y;
+                d0 = d1 = rp.w;
             }
             // a = magnitude * F (TileStitcher.contribute, stitching.py:136)
-            const float a00 = a0p[0] * f00, a01 = has_r1 ? a0p[1] * f01 : 0.f;
-            const float a10 = has_x1 ? a0p[s.rs] * f10 : 0.f;
-            const float a11 = has_x1 && has_r1 ? a0p[s.rs + 1] * f11 : 0.f;
+            const float a00 = pa[o] * f00, a01 = pa[o + 1] * f01;
+            const float a10 = pa[o + s.rst] * f10, a11 = pa[o + s.rst + 1] * f11;
             const float u0 = fmaf(a01, w1, a00 * w0), u1 = fmaf(a11, w1, a10 * w0);
             an[q] += fmaf(u1, wx1, u0 * wx0);
             ad[q] += fmaf(d1, wx1, d0 * wx0);
@@ -580,7 +578,7 @@ cudaError_t launch_stitch_frames(const StitchDev* plans_dev, const TileList& til
                                  int64_t mag_tile_stride, int B, int n_tile_x, int f0, int n_out_z, int n_out_x,
                                  float thr, float* db, unsigned int* plane_mm, unsigned int* run_mm, cudaStream_t st) {
     if (B == 0) return cudaSuccess;
-    const size_t smem = patch_smem_bytes + sizeof(float) * static_cast<size_t>(ns_max) * (6 * kFZ + 3 * kBlk) + 16;
+    const size_t smem = patch_smem_bytes + sizeof(float) * static_cast<size_t>(ns_max) * (6 * kFZ + 4 * kBlk) + 16;
     if (smem > 160 * 1024) return cudaErrorInvalidValue;
     cudaError_t e = cudaFuncSetAttribute(k_stitch_frames, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(smem));

@@ -103,9 +103,13 @@ class BetaFocusNet:
     CUDA tensors, every computation a C-ABI call on the context's stream."""
 
     def __init__(self, ctx: Context, in_ch: int = 3, widths=(32, 32, 32, 32), img: int = IMG, hidden: int = 64,
-                 seed: int = 0, device="cuda"):
+                 seed: int = 0, device="cuda", train_tensor_cores: bool = False):
+        """train_tensor_cores: train_step runs the convolutions, their weight
+        and data gradients on the tensor cores (FP16 forward operands, BF16
+        gradient operands, float32 accumulation) where the shape allows."""
         import torch
         self.torch = torch
+        self.train_tensor_cores = bool(train_tensor_cores)
         self.ctx = ctx
         self.lib = ctx.lib
         self.img = img
@@ -161,13 +165,16 @@ class BetaFocusNet:
             return False
         return w % 128 == 0 if w >= 128 else (128 % w == 0 and h % (128 // w) == 0)
 
-    def forward(self, x, tensor_cores: bool = False):
+    def forward(self, x, tensor_cores: bool = False, fuse_pool=None):
         """x: (n, in_ch, img, img) float32 CUDA tensor -> (n, 2) predictions (a
         view of an internal buffer, valid until the next call).  Runs on
         torch's current stream (see Context.follow_torch_stream), after the
         work that produced x.  tensor_cores: the convolutions on the tensor
-        cores (FP16 operands, float32 accumulation) where the shape allows;
-        training keeps the float32 form its gradients are checked against."""
+        cores (FP16 operands, float32 accumulation) where the shape allows.
+        fuse_pool (default: tensor_cores): layers the fused convolution + ReLU
+        + pooling kernel accepts keep no pre-activations (no backward after)."""
+        if fuse_pool is None:
+            fuse_pool = tensor_cores
         self.ctx.follow_torch_stream()
         n = x.shape[0]
         b = self._buffers(n)
@@ -176,7 +183,7 @@ class BetaFocusNet:
         h = self.img
         for i, (cin, cout) in enumerate(zip(self.chans[:-1], self.chans[1:])):
             w, bias = self.params[2 * i], self.params[2 * i + 1]
-            if tensor_cores and self.tc_supported(cin, cout, h, h) and h >= 128 and h % 2 == 0:
+            if fuse_pool and tensor_cores and self.tc_supported(cin, cout, h, h) and h >= 128 and h % 2 == 0:
                 # convolution, ReLU and pooling in one kernel (no pre-activations)
                 self._check(self.lib.octgb_cnn_conv3x3_relu_pool_tc(self.ctx.h, _p(cur), _p(w), _p(bias),
                                                                     _p(b["pooled"][i]), n, cin, cout, h, h))
@@ -221,9 +228,9 @@ class BetaFocusNet:
                                                          n * cout, h, h))
             xin = self._x if i == 0 else b["pooled"][i - 1]
             dx = None if i == 0 else b["dpooled"][i - 1]
-            self._check(self.lib.octgb_cnn_conv3x3_bwd(self.ctx.h, _p(xin), _p(self.params[2 * i]),
-                                                       _p(b["dpre"][i]), _p(dx), _p(g[2 * i]), _p(g[2 * i + 1]),
-                                                       _p(self.wscratch), n, cin, cout, h, h))
+            bwd = self.lib.octgb_cnn_conv3x3_bwd_tc if self.train_tensor_cores else self.lib.octgb_cnn_conv3x3_bwd
+            self._check(bwd(self.ctx.h, _p(xin), _p(self.params[2 * i]), _p(b["dpre"][i]), _p(dx), _p(g[2 * i]),
+                            _p(g[2 * i + 1]), _p(self.wscratch), n, cin, cout, h, h))
             dp = dx
             h *= 2
 
@@ -241,7 +248,7 @@ class BetaFocusNet:
                                                 eps, self.step_count))
 
     def train_step(self, x, target, lr: float):
-        pred = self.forward(x)
+        pred = self.forward(x, tensor_cores=self.train_tensor_cores, fuse_pool=False)
         loss, dout = self.loss_grad(pred, target)
         self.backward(dout)
         self.adam(lr)

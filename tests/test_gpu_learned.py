@@ -97,6 +97,72 @@ def test_conv_relu_pool_tensor_cores(torch_ctx):
         np.testing.assert_allclose(p.cpu().numpy(), ref, rtol=0, atol=1e-5 * np.abs(pre).max() * np.sqrt(cin * 9))
 
 
+def _bf16(a):
+    """float32 -> BF16 (round to nearest even) -> float64."""
+    u = np.ascontiguousarray(a, np.float32).view(np.uint32).astype(np.uint64)
+    u = (u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000
+    return u.astype(np.uint32).view(np.float32).astype(np.float64)
+
+
+def _wgrad_ref(x, dy):
+    """dw (K, C, 3, 3) and sum |dy| |x| per element, float64, as matrix products per tap."""
+    n, C, H, W = x.shape
+    K = dy.shape[1]
+    xp = np.pad(x, ((0, 0), (0, 0), (1, 1), (1, 1)))
+    d2 = dy.transpose(1, 0, 2, 3).reshape(K, -1)
+    dw, mag = np.zeros((K, C, 3, 3)), np.zeros((K, C, 3, 3))
+    for i in range(3):
+        for j in range(3):
+            xs = xp[:, :, i:i + H, j:j + W].transpose(1, 0, 2, 3).reshape(C, -1)
+            dw[:, :, i, j] = d2 @ xs.T
+            mag[:, :, i, j] = np.abs(d2) @ np.abs(xs).T
+    return dw, mag
+
+
+def test_conv_grad_tensor_cores_match_bf16_operands(torch_ctx):
+    """The tcgen05 weight gradient equals the float64 sum of the BF16-rounded
+    operands' products within float32 accumulation (1e-4 of the sum of the
+    products' magnitudes), on the network's shapes and ragged ones (widths not
+    a multiple of 8, channel counts off the MMA sizes, one-row bands); the
+    data gradient (BF16 tensor-core convolution with the flipped kernel) the
+    float64 one of the rounded operands; db the float64 sum of dy."""
+    torch, ctx = torch_ctx
+    from oct_recon_af_v1_gb300.learned import BetaFocusNet, _p
+    rng = np.random.default_rng(8)
+    for n, cin, cout, h, w in ((2, 3, 32, 256, 256), (2, 32, 32, 128, 128), (3, 32, 32, 64, 64),
+                               (4, 32, 32, 32, 32), (1, 11, 21, 20, 37), (2, 5, 7, 9, 13), (1, 48, 128, 16, 16),
+                               (2, 1, 1, 7, 5), (1, 16, 40, 3, 700)):
+        x = rng.standard_normal((n, cin, h, w)).astype(np.float32)
+        wt = (rng.standard_normal((cout, cin, 3, 3)) * 0.3).astype(np.float32)
+        dy = (rng.standard_normal((n, cout, h, w)) * 1e-6).astype(np.float32)   # gradients: small magnitudes
+        ref_dw, mag = _wgrad_ref(_bf16(x), _bf16(dy))
+        xd, wd, dyd = (torch.tensor(a, device="cuda") for a in (x, wt, dy))
+        dw = torch.full((cout, cin, 3, 3), float("nan"), device="cuda")
+        db = torch.empty(cout, device="cuda")
+        dx = torch.empty((n, cin, h, w), device="cuda")
+        scratch = torch.empty(cout * cin * 9, device="cuda")
+        ctx._check(ctx.lib.octgb_cnn_conv3x3_bwd_tc(ctx.h, _p(xd), _p(wd), _p(dyd), _p(dx), _p(dw), _p(db),
+                                                    _p(scratch), n, cin, cout, h, w))
+        ctx.synchronize()
+        got = dw.cpu().numpy().astype(np.float64)
+        assert np.isfinite(got).all(), (cin, cout, h, w)
+        err = np.abs(got - ref_dw)
+        assert (err <= 1e-4 * mag + 1e-30).all(), (cin, cout, h, w, float((err / (mag + 1e-30)).max()))
+        np.testing.assert_allclose(db.cpu().numpy(), dy.astype(np.float64).sum(axis=(0, 2, 3)), rtol=1e-4,
+                                   atol=1e-4 * np.abs(dy).sum(axis=(0, 2, 3)).max())
+        # dx: BF16 tensor cores where the convolution cout -> cin is a supported shape, else float32
+        wf = np.flip(wt, (2, 3)).transpose(1, 0, 2, 3)              # (cin, cout, 3, 3)
+        tc = BetaFocusNet.tc_supported(cout, cin, h, w)
+        ref_dx = C.conv3x3(_bf16(dy) if tc else dy.astype(np.float64), _bf16(wf) if tc else wf.astype(np.float64),
+                           np.zeros(cin))
+        scale = np.abs(ref_dx).max()
+        np.testing.assert_allclose(dx.cpu().numpy(), ref_dx, rtol=0, atol=1e-5 * scale * np.sqrt(cout * 9))
+    from oct_recon_af_v1_gb300._lib import OctgbError
+    with pytest.raises(OctgbError):
+        ctx._check(ctx.lib.octgb_cnn_conv3x3_bwd_tc(ctx.h, _p(xd), _p(wd), _p(dyd), None, _p(dw), _p(db), None,
+                                                    1, 49, 32, 8, 8))
+
+
 def test_network_gradients_match_oracle(torch_ctx):
     torch, ctx = torch_ctx
     from oct_recon_af_v1_gb300.learned import BetaFocusNet
@@ -123,6 +189,37 @@ def test_network_gradients_match_oracle(torch_ctx):
         got = g.cpu().numpy().astype(float)
         err = np.abs(got - r).max() / max(np.abs(r).max(), 1e-12)
         assert err < 2e-4, (i, err)
+
+
+def test_network_gradients_tensor_cores(torch_ctx):
+    """Training on the tensor cores (FP16 forward, BF16 gradients) on a
+    network whose layers take every path (tensor-core forward at widths 64 ..
+    16, float32 forward at 8; tensor-core weight and data gradients): every
+    parameter gradient within 3 % of the largest of the float64 oracle's."""
+    torch, ctx = torch_ctx
+    from oct_recon_af_v1_gb300.learned import BetaFocusNet
+    rng = np.random.default_rng(12)
+    widths, img, hidden = (32, 32, 32, 32), 64, 16
+    params = small_params(rng, widths=widths, img=img, hidden=hidden)
+    net = BetaFocusNet(ctx, in_ch=3, widths=widths, img=img, hidden=hidden, train_tensor_cores=True)
+    for dst, src in zip(net.params, params):
+        dst.copy_(torch.tensor(src, dtype=torch.float32))
+    x = rng.standard_normal((4, 3, img, img))
+    t = rng.standard_normal((4, 2)) * 0.5
+    ref_pred, cache = C.forward(params, x)
+    _, dout = C.mse(ref_pred, t)
+    ref_grads = C.backward(params, cache, dout)
+    xd = torch.tensor(x, dtype=torch.float32, device="cuda")
+    td = torch.tensor(t, dtype=torch.float32, device="cuda")
+    pred = net.forward(xd, tensor_cores=True, fuse_pool=False)
+    _, dout_d = net.loss_grad(pred, td)
+    net.backward(dout_d)
+    torch.cuda.synchronize()
+    np.testing.assert_allclose(pred.cpu().numpy(), ref_pred, rtol=0, atol=1e-2 * np.abs(ref_pred).max())
+    for i, (g, r) in enumerate(zip(net.grads, ref_grads)):
+        got = g.cpu().numpy().astype(float)
+        err = np.abs(got - r).max() / max(np.abs(r).max(), 1e-12)
+        assert err < 3e-2, (i, err)
 
 
 def test_adam_step_matches_formula(torch_ctx):
@@ -178,10 +275,12 @@ def test_probe_images_match_numpy(torch_ctx):
     np.testing.assert_allclose(imgs, ref, rtol=0, atol=2e-4)
 
 
-def test_training_lowers_loss(torch_ctx):
+@pytest.mark.parametrize("tensor_cores", [False, True])
+def test_training_lowers_loss(torch_ctx, tensor_cores):
     torch, ctx = torch_ctx
     from oct_recon_af_v1_gb300.learned import BetaFocusNet
-    net = BetaFocusNet(ctx, in_ch=3, widths=(8, 8, 8, 8), img=64, hidden=16, seed=1)
+    widths = (32, 32, 32, 32) if tensor_cores else (8, 8, 8, 8)
+    net = BetaFocusNet(ctx, in_ch=3, widths=widths, img=64, hidden=16, seed=1, train_tensor_cores=tensor_cores)
     g = torch.Generator(device="cuda").manual_seed(0)
     x = torch.randn((16, 3, 64, 64), device="cuda", generator=g)
     t = torch.stack([x[:, 0].mean((1, 2)) * 3, x[:, 1, :32].mean((1, 2)) * 3], -1).contiguous()
