@@ -483,7 +483,7 @@ def learned_leg(args, torch, stream, dev):
     return {"learned_ms_per_bscan": r["ms_per_step"] / n, "search_ms_per_bscan": r["search"]["seconds"] * 1e3 / n,
             "speedup": r["search"]["learned_speedup"], "learned_a_scans_per_s": r["value"],
             "search_a_scans_per_s": r["search"]["value"], "accuracy": r["accuracy"],
-            "training": {k: r["training"][k] for k in ("train_s", "epochs", "batch")},
+            "training": {k: r["training"][k] for k in ("train_s", "epochs", "batch", "kernels", "loss_per_epoch")},
             "config": r["config"]["workload"]}
 
 
@@ -779,7 +779,8 @@ def gpu_arm_config4(args, rank, world, torch, ctx, stream, dev):
     from oct_recon_af_v1_gb300._lib import Context
     net_ctx = Context(torch.cuda.current_device())
     net_ctx.set_stream(stream.cuda_stream)
-    net = L.BetaFocusNet(net_ctx, seed=0)
+    train_tc = not getattr(args, "train_fp32", False)
+    net = L.BetaFocusNet(net_ctx, seed=0, train_tensor_cores=train_tc)
     Yd = torch.tensor(Y, device=dev)
     bs, epochs = 128, args.epochs4
     steps_per_epoch = n_train // bs
@@ -912,7 +913,9 @@ def gpu_arm_config4(args, rank, world, torch, ctx, stream, dev):
                          "focus_mae_learned_px": float(np.mean(np.abs(focus_l - focus_t))),
                          "focus_mae_plain_px": float(np.mean(np.abs(focus_s - focus_t)))},
             "training": {"images_s": t_data, "train_s": t_train, "epochs": epochs, "batch": bs,
-                         "loss_per_epoch": losses},
+                         "loss_per_epoch": losses,
+                         "kernels": "tensor cores (FP16 forward, BF16 weight and data gradients, float32 "
+                                    "accumulation)" if train_tc else "float32 SIMT"},
             "e2e": {"value": ascans / (ms_e2e * 1e-3), "unit": "A-scans/s", "ms_per_step": ms_e2e,
                     "h2d_bytes_per_step": raw_bytes, "d2h_bytes_per_step": n_test * 2 * 4}}
 
@@ -1284,6 +1287,8 @@ def main():
     ap.add_argument("--config", type=int, default=1, choices=[0, 1, 2, 3, 4])
     ap.add_argument("--train4", type=int, default=20000, help="training images of the learned estimator (config 4)")
     ap.add_argument("--epochs4", type=int, default=8, help="training epochs (config 4)")
+    ap.add_argument("--train-fp32", action="store_true",
+                    help="train the learned estimator with the float32 SIMT kernels instead of the tensor cores")
     ap.add_argument("--tiles3", type=int, default=64, help="tiles of the batched workload (config 3)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")

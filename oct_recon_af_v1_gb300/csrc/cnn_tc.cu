@@ -435,7 +435,10 @@ __global__ void __launch_bounds__(kWThreads, 1)
     // BF16 A (K-major) and B (MN-major: bit 16)
     const uint32_t idesc = mma_idesc_f16(128, g.N) | kIdescBf16 | (1u << 16);
     const uint32_t lbo_a = static_cast<uint32_t>(kp) * 16;      // next 8-pixel chunk of dy
-    const uint32_t lbo_b = static_cast<uint32_t>(g.xpix) * 16;  // next channel group of x
+    // B is MN-major without swizzle: there the descriptor's leading offset is
+    // the step along K (the next 8 pixels, 128 bytes on) and the stride offset
+    // the step along N (the next channel group)
+    const uint32_t sbo_b = static_cast<uint32_t>(g.xpix) * 16;
     const int ksteps = g.Q / 16;
     const int dtasks = (g.Q / 32) * g.kg * 32;
 
@@ -502,7 +505,7 @@ __global__ void __launch_bounds__(kWThreads, 1)
         if (tid == 0) {
             tc_fence_after();
             const uint64_t da0 = smem_desc(Ds, lbo_a, 128);
-            const uint64_t db0 = smem_desc(Xs, lbo_b, 128);
+            const uint64_t db0 = smem_desc(Xs, 128, sbo_b);
             for (int tap = 0; tap < 9; ++tap) {
                 const int ty = tap / 3, tx = tap - 3 * ty;
                 // descriptor addresses are in 16-byte units: one unit per staged pixel of x
