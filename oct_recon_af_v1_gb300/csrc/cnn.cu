@@ -279,6 +279,40 @@ __global__ void k_relu_pool_bwd(const float* __restrict__ dp, const float* __res
     }
 }
 
+// the same two kernels four pixels a thread (16-byte loads and stores) for
+// widths that are a multiple of 4 on aligned buffers, rows = planes x H < 2^31 / (W / 4)
+__global__ void k_relu_pool4(const float* __restrict__ y, int rows_out, int H, int W, float* __restrict__ p) {
+    const int w4 = W / 4, Wo = W / 2, Ho = H / 2;
+    const int total = rows_out * w4;                     // two outputs (four inputs of two rows) a thread
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const int ro = i / w4, c = 4 * (i - ro * w4);
+        const int plane = ro / Ho, oh = ro - plane * Ho;
+        const float* s = y + (static_cast<int64_t>(plane) * H + 2 * oh) * W + c;
+        const float4 a = *reinterpret_cast<const float4*>(s);
+        const float4 b = *reinterpret_cast<const float4*>(s + W);
+        const float p0 = 0.25f * ((fmaxf(a.x, 0.f) + fmaxf(a.y, 0.f)) + (fmaxf(b.x, 0.f) + fmaxf(b.y, 0.f)));
+        const float p1 = 0.25f * ((fmaxf(a.z, 0.f) + fmaxf(a.w, 0.f)) + (fmaxf(b.z, 0.f) + fmaxf(b.w, 0.f)));
+        *reinterpret_cast<float2*>(p + static_cast<int64_t>(ro) * Wo + c / 2) = make_float2(p0, p1);
+    }
+}
+
+__global__ void k_relu_pool_bwd4(const float* __restrict__ dp, const float* __restrict__ y, int rows, int H, int W,
+                                 float* __restrict__ dy) {
+    const int w4 = W / 4, Wo = W / 2;
+    const int total = rows * w4;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const int row = i / w4, c = 4 * (i - row * w4);
+        const int plane = row / H, h = row - plane * H;
+        const float2 g = *reinterpret_cast<const float2*>(dp + (static_cast<int64_t>(plane) * (H / 2) + h / 2) * Wo +
+                                                          c / 2);
+        const int64_t o = static_cast<int64_t>(row) * W + c;
+        const float4 v = *reinterpret_cast<const float4*>(y + o);
+        const float g0 = 0.25f * g.x, g1 = 0.25f * g.y;
+        *reinterpret_cast<float4*>(dy + o) =
+            make_float4(v.x > 0.f ? g0 : 0.f, v.y > 0.f ? g0 : 0.f, v.z > 0.f ? g1 : 0.f, v.w > 0.f ? g1 : 0.f);
+    }
+}
+
 // ---------------------------------------------------------------- dense layers
 constexpr int kGT = 64, kGK = 16;
 
@@ -486,13 +520,26 @@ cudaError_t launch_conv3x3_wgrad(const float* x, const float* dy, float* dw, int
     return cudaGetLastError();
 }
 
+static bool aligned16(const void* p) { return reinterpret_cast<uintptr_t>(p) % 16 == 0; }
+
 cudaError_t launch_relu_pool(const float* y, int64_t nk, int H, int W, float* p, cudaStream_t st) {
+    const int64_t threads4 = nk * (H / 2) * (W / 4);
+    if (W % 4 == 0 && threads4 < (int64_t(1) << 31) && aligned16(y) && reinterpret_cast<uintptr_t>(p) % 8 == 0) {
+        k_relu_pool4<<<grid_for(threads4, 256, 65536), 256, 0, st>>>(y, static_cast<int>(nk * (H / 2)), H, W, p);
+        return cudaGetLastError();
+    }
     k_relu_pool<<<grid_for(nk * (H / 2) * (W / 2), 256, 65536), 256, 0, st>>>(y, nk, H, W, p);
     return cudaGetLastError();
 }
 
 cudaError_t launch_relu_pool_bwd(const float* dp, const float* y, int64_t nk, int H, int W, float* dy,
                                  cudaStream_t st) {
+    const int64_t threads4 = nk * H * (W / 4);
+    if (W % 4 == 0 && threads4 < (int64_t(1) << 31) && aligned16(y) && aligned16(dy) &&
+        reinterpret_cast<uintptr_t>(dp) % 8 == 0) {
+        k_relu_pool_bwd4<<<grid_for(threads4, 256, 65536), 256, 0, st>>>(dp, y, static_cast<int>(nk * H), H, W, dy);
+        return cudaGetLastError();
+    }
     k_relu_pool_bwd<<<grid_for(nk * H * W, 256, 65536), 256, 0, st>>>(dp, y, nk, H, W, dy);
     return cudaGetLastError();
 }

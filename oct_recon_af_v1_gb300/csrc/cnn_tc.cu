@@ -359,27 +359,31 @@ __global__ void __launch_bounds__(kCThreads, 4)
 // accumulator rows that are never read), N = the input channels rounded up to
 // 16, K = 16 pixels per MMA; BF16 operands (gradients span float32's exponent
 // range), float32 accumulation.  A tile is R image rows.  Its input rows
-// y0 - 1 .. y0 + R are staged with one zero column on either side (row pitch
-// Wp = W + 2) channel-contiguous ([channel group][pixel][8 channels x 2 B],
-// the MN-major B operand), and dy on the same pitch pixel-contiguous ([8-pixel
-// chunk][output channel][8 pixels x 2 B], the K-major A operand) with zeros in
-// the two pad columns: output pixel q = r * Wp + ox meets input pixel
-// q + ty * Wp + tx, so tap (ty, tx) is the staged input block seen from that
-// pixel on (a descriptor offset of 16 bytes a pixel, no shifted copies).  The
-// nine accumulators (9 x N TMEM columns) stay in TMEM over all the CTA's
-// tiles; the staged blocks are double-buffered, so one thread issues tile j's
-// MMAs while the CTA stages tile j + 1.  Each CTA then writes its partial sums
-// and k_sum_partials adds them in CTA order (the result does not depend on
-// timing).
-constexpr int kWThreads = 256;
+// y0 - 1 .. y0 + R are staged with a zero column before each row and zeros
+// after it up to the row pitch Wp (W + 2 rounded up to 4), channel-contiguous
+// ([channel group][pixel][8 channels x 2 B], the MN-major B operand), and dy
+// on the same pitch pixel-contiguous ([8-pixel chunk][output channel][8 pixels
+// x 2 B], the K-major A operand) with zeros past each row's W pixels: output
+// pixel q = r * Wp + ox meets input pixel q + ty * Wp + tx, so tap (ty, tx) is
+// the staged input block seen from that pixel on (a descriptor offset of 16
+// bytes a pixel, no shifted copies).  The pitch being a multiple of 4, dy's
+// rows arrive as 16-byte loads, four pixels per half chunk.  The nine
+// accumulators (9 x N TMEM columns) stay in TMEM over all the CTA's tiles; the
+// staged blocks are double-buffered.  Warp 0 only issues the MMAs (one
+// thread), so tile j's MMAs are issued while warps 1.. stage tile j + 1.  Each
+// CTA then writes its partial sums and k_sum_partials adds them in CTA order
+// (the result does not depend on timing).
+constexpr int kWThreads = 512;
+constexpr int kWStage = kWThreads - 32;       // staging threads (warps 1..)
 
 struct WgradGeom {
     int n, C, K, H, W;
-    int R, Wp, Q;        // rows per tile, staged row pitch, pixels per tile (R x Wp rounded up to 32)
+    int R, Wp, Q;        // rows per tile, staged row pitch (W + 2 rounded up to 4), pixels per tile (R Wp rounded up to 32)
     int N;               // MMA N: C rounded up to 16
     int cg, kg;          // channel groups of 8 staged (x: N / 8; dy: ceil(K / 8))
     int xpix;            // staged input pixels per channel group (Q + 2 Wp + 2, rounded up to 8)
     int nbuf;            // staged blocks: 2 (tile j + 1 stages while tile j's MMAs run), or 1 for wide rows
+    int vec4;            // dy rows load as float4 (W a multiple of 4)
     int tiles_img;
     int64_t n_units;
     uint32_t xbytes, stage, smem;
@@ -411,6 +415,7 @@ __global__ void __launch_bounds__(kWThreads, 1)
     __shared__ WgradBars S;
     uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int st = tid - 32;                       // staging thread index (warps 1..)
     const int64_t hw = static_cast<int64_t>(g.H) * g.W;
     const int kp = 8 * g.kg;
 
@@ -440,7 +445,8 @@ __global__ void __launch_bounds__(kWThreads, 1)
     // the step along N (the next channel group)
     const uint32_t sbo_b = static_cast<uint32_t>(g.xpix) * 16;
     const int ksteps = g.Q / 16;
-    const int dtasks = (g.Q / 32) * g.kg * 32;
+    const int qw = g.Wp / 4;                       // half chunks (4 pixels) a staged row
+    const int dtasks = g.Q / 4 * kp;               // (output channel, half chunk) pairs
 
     uint32_t j = 0;
     bool ok = true;
@@ -456,65 +462,106 @@ __global__ void __launch_bounds__(kWThreads, 1)
         const int y0 = static_cast<int>(u - static_cast<int64_t>(img) * g.tiles_img) * g.R;
         uint8_t* Xs = base + b * g.stage;
         uint8_t* Ds = Xs + g.xbytes;
-        // input block: pixel i = r * Wp + cc is x(y0 - 1 + r, cc - 1); zero
-        // outside the image and past the R + 2 staged rows
-        const float* xi = x + static_cast<int64_t>(img) * g.C * hw;
-        for (int i = tid; i < g.xpix; i += kWThreads) {
-            const int r = i / g.Wp, cc = i - r * g.Wp;
-            const int iy = y0 - 1 + r, ix = cc - 1;
-            const bool in = r < g.R + 2 && iy >= 0 && iy < g.H && ix >= 0 && ix < g.W;
-            const float* p = xi + (in ? static_cast<int64_t>(iy) * g.W + ix : 0);
-            for (int c8 = 0; c8 < g.cg; ++c8) {
-                float v[8];
+        if (warp > 0) {
+            // input block: pixel i = r * Wp + cc is x(y0 - 1 + r, cc - 1); zero
+            // outside the image, past each row's W + 1 columns and past the R + 2
+            // staged rows.  Two channel groups (16 loads) in flight per pass.
+            const float* xi = x + static_cast<int64_t>(img) * g.C * hw;
+            for (int i0 = st; i0 < g.xpix; i0 += 2 * kWStage) {
+                // two pixels a pass, each with two channel groups: 32 loads in flight
+                const float* px[2];
+                bool in[2];
 #pragma unroll
-                for (int e = 0; e < 8; ++e) {
-                    const int c = 8 * c8 + e;
-                    v[e] = (in && c < g.C) ? __ldg(p + static_cast<int64_t>(c) * hw) : 0.f;
+                for (int h = 0; h < 2; ++h) {
+                    const int i = i0 + h * kWStage;
+                    const int r = i / g.Wp, cc = i - r * g.Wp;
+                    const int iy = y0 - 1 + r, ix = cc - 1;
+                    in[h] = i < g.xpix && r < g.R + 2 && iy >= 0 && iy < g.H && ix >= 0 && ix < g.W;
+                    px[h] = xi + (in[h] ? static_cast<int64_t>(iy) * g.W + ix : 0);
                 }
-                *reinterpret_cast<uint4*>(Xs + (static_cast<uint32_t>(c8) * g.xpix + i) * 16u) =
-                    make_uint4(pack_bf2(v[0], v[1]), pack_bf2(v[2], v[3]), pack_bf2(v[4], v[5]), pack_bf2(v[6], v[7]));
-            }
-        }
-        // dy block: chunk q8 of channel k holds q = 8 q8 .. 8 q8 + 7, q = r * Wp
-        // + ox is dy(y0 + r, ox), zero for ox >= W and r >= R.  A warp takes 8
-        // channels x 4 chunks, so a quarter-warp stores 128 contiguous bytes.
-        const float* di = dy + static_cast<int64_t>(img) * g.K * hw + static_cast<int64_t>(y0) * g.W;
-        for (int i = tid; i < dtasks; i += kWThreads) {
-            const int l = i & 31, w = i >> 5;
-            const int qb = w / g.kg, kgi = w - qb * g.kg;
-            const int k = 8 * kgi + (l & 7);
-            const int q8 = 4 * qb + (l >> 3);
-            int r = (8 * q8) / g.Wp;
-            int ox = 8 * q8 - r * g.Wp;
-            const float* dk = di + static_cast<int64_t>(k < g.K ? k : 0) * hw;
-            float v[8];
+                for (int c8 = 0; c8 < g.cg; c8 += 2) {
+                    float v[2][16];
 #pragma unroll
-            for (int e = 0; e < 8; ++e) {
-                v[e] = (k < g.K && r < g.R && ox < g.W) ? __ldg(dk + r * g.W + ox) : 0.f;
-                if (++ox == g.Wp) {
-                    ox = 0;
-                    ++r;
+                    for (int h = 0; h < 2; ++h)
+#pragma unroll
+                        for (int e = 0; e < 16; ++e) {
+                            const int c = 8 * c8 + e;
+                            v[h][e] = (in[h] && c < g.C) ? __ldg(px[h] + static_cast<int64_t>(c) * hw) : 0.f;
+                        }
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const int i = i0 + h * kWStage;
+                        if (i >= g.xpix) continue;
+#pragma unroll
+                        for (int q = 0; q < 2; ++q)
+                            *reinterpret_cast<uint4*>(Xs + (static_cast<uint32_t>(c8 + q) * g.xpix + i) * 16u) =
+                                make_uint4(pack_bf2(v[h][8 * q], v[h][8 * q + 1]), pack_bf2(v[h][8 * q + 2], v[h][8 * q + 3]),
+                                           pack_bf2(v[h][8 * q + 4], v[h][8 * q + 5]),
+                                           pack_bf2(v[h][8 * q + 6], v[h][8 * q + 7]));
+                    }
                 }
             }
-            *reinterpret_cast<uint4*>(Ds + (static_cast<uint32_t>(q8) * kp + k) * 16u) =
-                make_uint4(pack_bf2(v[0], v[1]), pack_bf2(v[2], v[3]), pack_bf2(v[4], v[5]), pack_bf2(v[6], v[7]));
+            // dy block: half chunk h4 (q = 4 h4 .. 4 h4 + 3, one row: the pitch is a
+            // multiple of 4) of channel k.  A warp takes 8 channels x 4 half
+            // chunks: each channel's 16 pixels are one 64-byte read, and the
+            // 8-byte stores of two chunks fill two 128-byte rows of banks.
+            const float* di = dy + static_cast<int64_t>(img) * g.K * hw + static_cast<int64_t>(y0) * g.W;
+            constexpr int kDU = 4;                 // tasks a pass: four 16-byte loads in flight
+            for (int i0 = st; i0 < dtasks; i0 += kDU * kWStage) {
+                float v[kDU][4];
+                uint32_t so[kDU];
+#pragma unroll
+                for (int t = 0; t < kDU; ++t) {
+                    const int i = i0 + t * kWStage;
+                    const int l = i & 31, w = i >> 5;
+                    const int hb = w / g.kg, kgi = w - hb * g.kg;
+                    const int k = 8 * kgi + (l >> 2);
+                    const int h4 = 4 * hb + (l & 3);
+                    const int r = h4 / qw;
+                    const int ox = 4 * (h4 - r * qw);
+                    so[t] = i < dtasks ? (static_cast<uint32_t>(h4 >> 1) * kp + k) * 16u + (h4 & 1) * 8u : ~0u;
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) v[t][e] = 0.f;
+                    if (i < dtasks && k < g.K && r < g.R && ox < g.W) {
+                        const float* pr = di + static_cast<int64_t>(k) * hw + r * g.W + ox;
+                        if (g.vec4) {
+                            const float4 f = __ldg(reinterpret_cast<const float4*>(pr));
+                            v[t][0] = f.x;
+                            v[t][1] = f.y;
+                            v[t][2] = f.z;
+                            v[t][3] = f.w;
+                        } else {
+#pragma unroll
+                            for (int e = 0; e < 4; ++e) v[t][e] = ox + e < g.W ? __ldg(pr + e) : 0.f;
+                        }
+                    }
+                }
+#pragma unroll
+                for (int t = 0; t < kDU; ++t)
+                    if (so[t] != ~0u)
+                        *reinterpret_cast<uint2*>(Ds + so[t]) =
+                            make_uint2(pack_bf2(v[t][0], v[t][1]), pack_bf2(v[t][2], v[t][3]));
+            }
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         }
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         tc_fence_before();
         __syncthreads();
         if (tid == 0) {
             tc_fence_after();
             const uint64_t da0 = smem_desc(Ds, lbo_a, 128);
             const uint64_t db0 = smem_desc(Xs, 128, sbo_b);
-            for (int tap = 0; tap < 9; ++tap) {
-                const int ty = tap / 3, tx = tap - 3 * ty;
+            // K steps outer, taps inner: consecutive MMAs go to different
+            // accumulators, so no MMA waits for the previous one's sum
+            for (int ks = 0; ks < ksteps; ++ks) {
+                const uint64_t da = da0 + static_cast<uint64_t>(ks) * (2u * lbo_a >> 4);
                 // descriptor addresses are in 16-byte units: one unit per staged pixel of x
-                const uint64_t dbt = db0 + static_cast<uint64_t>(ty * g.Wp + tx);
-                const uint32_t d_tmem = tmem + static_cast<uint32_t>(tap * g.N);
-                for (int ks = 0; ks < ksteps; ++ks) {
-                    const uint64_t da = da0 + static_cast<uint64_t>(ks) * (2u * lbo_a >> 4);
-                    const uint64_t db = dbt + static_cast<uint64_t>(16 * ks);
-                    mma_f16_id(d_tmem, da, db, idesc, (j > 0 || ks > 0) ? 1u : 0u);
+                const uint64_t dbk = db0 + static_cast<uint64_t>(16 * ks);
+                const uint32_t acc = (j > 0 || ks > 0) ? 1u : 0u;
+#pragma unroll
+                for (int tap = 0; tap < 9; ++tap) {
+                    const int ty = tap / 3, tx = tap - 3 * ty;
+                    mma_f16_id(tmem + static_cast<uint32_t>(tap * g.N), da,
+                               dbk + static_cast<uint64_t>(ty * g.Wp + tx), idesc, acc);
                 }
             }
             mma_commit(&S.x[b]);
@@ -531,7 +578,7 @@ __global__ void __launch_bounds__(kWThreads, 1)
     tc_fence_after();
     if (ok && S.drained) {
         // warp w reads TMEM lanes 32 (w % 4) .. + 31 (output channels), 32-column
-        // chunks w / 4, w / 4 + 2, ...; column t * N + c is tap t of channel c
+        // chunks w / 4, w / 4 + 4, ...; column t * N + c is tap t of channel c
         const int quarter = warp & 3;
         const int k = 32 * quarter + lane;
         const int cols = 9 * g.N;
@@ -583,7 +630,8 @@ bool wgrad_geom(int n, int cin, int cout, int H, int W, WgradGeom& g) {
     g.N = (cin + 15) / 16 * 16;
     g.cg = g.N / 8;
     g.kg = (cout + 7) / 8;
-    g.Wp = W + 2;
+    g.Wp = (W + 2 + 3) / 4 * 4;
+    g.vec4 = W % 4 == 0 ? 1 : 0;
     const uint32_t budget = 227u * 1024u;
     g.R = 0;
     for (int nbuf = 2; nbuf >= 1 && g.R == 0; --nbuf) {
@@ -695,6 +743,7 @@ cudaError_t launch_conv3x3_wgrad_tc(const float* x, const float* dy, float* dw, 
                                     int W, float* partials, int num_sms, int* status, cudaStream_t st) {
     WgradGeom g;
     if (!wgrad_geom(n, cin, cout, H, W, g) || partials == nullptr) return cudaErrorInvalidValue;
+    if (reinterpret_cast<uintptr_t>(dy) % 16 != 0) g.vec4 = 0;          // 16-byte loads need an aligned base
     const int grid = wgrad_grid(g, num_sms);
     cudaError_t e = cudaFuncSetAttribute(k_conv3x3_wgrad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(g.smem));

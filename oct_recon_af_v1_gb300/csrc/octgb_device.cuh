@@ -165,9 +165,11 @@ inline cudaError_t set_wait_test_here(unsigned long long limit_ns, int starve, c
 }
 
 // ---- tcgen05 (5th-generation tensor cores) helpers
-// shared-memory matrix descriptor: no swizzle, K-major; lbo = byte stride
-// between core matrices (8 rows x 16 bytes) along K, sbo = along M/N (8-row
-// groups); bit 46 is the descriptor version of sm_100-family tensor cores
+// shared-memory matrix descriptor without swizzle: lbo = byte step between
+// core matrices (8 rows x 16 bytes) along K, sbo = along M/N; without swizzle
+// this holds for K-major operands (a core matrix row = 8 K values) and
+// MN-major ones (a row = 8 M/N values) alike.  Bit 46 is the descriptor
+// version of sm_100-family tensor cores.
 __device__ __forceinline__ uint64_t smem_desc(const void* p, uint32_t lbo, uint32_t sbo) {
     const uint64_t a = smem_u32(p);
     return ((a >> 4) & 0x3fffull) | (static_cast<uint64_t>((lbo >> 4) & 0x3fff) << 16) |

@@ -244,35 +244,56 @@ __global__ void __launch_bounds__(kStThreads) k_stitch_frames(const StitchDev* _
         float* pa = sm + s.off;
         float* pf = pa + (s.xs + 1) * s.rst;
         const int fy = f0 + f;
-        // zero rows and the zero A-scan (plain stores, before the barrier)
-        for (int i = tid; i < (s.xs + 1) * s.rst; i += kStThreads) {
-            const int xx = i / s.rst, rr = i - xx * s.rst;
-            if (xx == s.xs || rr >= s.rs) {
-                pa[i] = 0.f;
-                if (s.opc) pf[i] = 0.f;
+        // zero rows (rst - rs of them after each A-scan's rows) and the zero
+        // A-scan after the last (plain stores, before the barrier)
+        {
+            const int zr = s.rst - s.rs;                     // 1 or 2
+            const int nz = s.xs * zr;
+            for (int i = tid; i < nz + s.rst; i += kStThreads) {
+                int o;
+                if (i < nz) {
+                    const int xx = zr == 1 ? i : i >> 1;
+                    o = xx * s.rst + s.rs + (i - xx * zr);
+                } else {
+                    o = s.xs * s.rst + (i - nz);
+                }
+                pa[o] = 0.f;
+                if (s.opc) pf[o] = 0.f;
             }
         }
         // the patch is copied as is (asynchronous 4-byte copies, every slot's
         // in flight at once); the focus weight multiplies it when it is read,
         // the same single product a * F.  64 consecutive threads copy 64
         // consecutive rows of one A-scan, four A-scans per pass
-        for (int rr = tid & 63; rr < s.rs; rr += 64)
-            for (int xx = tid >> 6; xx < s.xs; xx += kStThreads / 64) {
-                const int i = xx * s.rst + rr;
-                const int x = s.x_lo + xx;
-                const int ra = p.r0 + s.r_lo + rr;
-                int src = ra;
-                if (p.shift != nullptr) {
+        if (p.shift == nullptr) {
+            // source and destination advance by four A-scans a pass
+            for (int rr = tid & 63; rr < s.rs; rr += 64) {
+                const int xx0 = tid >> 6;
+                const float* src = mag_f + static_cast<int64_t>(s.x_lo + xx0) * kHalf + p.r0 + s.r_lo + rr;
+                uint32_t dst = static_cast<uint32_t>(__cvta_generic_to_shared(pa + xx0 * s.rst + rr));
+                const uint32_t dstep = static_cast<uint32_t>(kStThreads / 64 * s.rst) * 4u;
+                for (int xx = xx0; xx < s.xs; xx += kStThreads / 64) {
+                    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(dst), "l"(src) : "memory");
+                    src += kStThreads / 64 * kHalf;
+                    dst += dstep;
+                }
+            }
+        } else {
+            for (int rr = tid & 63; rr < s.rs; rr += 64)
+                for (int xx = tid >> 6; xx < s.xs; xx += kStThreads / 64) {
+                    const int i = xx * s.rst + rr;
+                    const int x = s.x_lo + xx;
+                    const int ra = p.r0 + s.r_lo + rr;
                     const int64_t o = static_cast<int64_t>(fy) * p.n_tile_x + x;
                     pf[i] = (ra < p.lo[o] || ra > p.hi[o]) ? 0.f : p.fz[s.r_lo + rr];
-                    src = ra + p.shift[o];
+                    int src = ra + p.shift[o];
                     src = src < 0 ? 0 : (src > p.n_rows - 1 ? p.n_rows - 1 : src);
+                    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(
+                                     static_cast<uint32_t>(__cvta_generic_to_shared(pa + i))),
+                                 "l"(mag_f + static_cast<int64_t>(x) * kHalf + src)
+                                 : "memory");
                 }
-                asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(
-                                 static_cast<uint32_t>(__cvta_generic_to_shared(pa + i))),
-                             "l"(mag_f + static_cast<int64_t>(x) * kHalf + src)
-                             : "memory");
-            }
+        }
     }
     asm volatile("cp.async.wait_all;" ::: "memory");
     __syncthreads();

@@ -131,7 +131,7 @@ def test_conv_grad_tensor_cores_match_bf16_operands(torch_ctx):
     rng = np.random.default_rng(8)
     for n, cin, cout, h, w in ((2, 3, 32, 256, 256), (2, 32, 32, 128, 128), (3, 32, 32, 64, 64),
                                (4, 32, 32, 32, 32), (1, 11, 21, 20, 37), (2, 5, 7, 9, 13), (1, 48, 128, 16, 16),
-                               (2, 1, 1, 7, 5), (1, 16, 40, 3, 700)):
+                               (2, 1, 1, 7, 5), (1, 16, 40, 3, 700), (2, 8, 16, 6, 30)):
         x = rng.standard_normal((n, cin, h, w)).astype(np.float32)
         wt = (rng.standard_normal((cout, cin, 3, 3)) * 0.3).astype(np.float32)
         dy = (rng.standard_normal((n, cout, h, w)) * 1e-6).astype(np.float32)   # gradients: small magnitudes
