@@ -1065,14 +1065,22 @@ def plugin_arm(vol, torch, dev, batch=30, io_threads=16):
     for yi in range(2):                                         # warm-up: rings, plans, pinned results
         R.process_row(yi)
     torch.cuda.synchronize()
+    for key in R.timers:
+        R.timers[key] = 0.0
     t0 = time.perf_counter()
     rows = [R.process_row(yi) for yi in range(2)]
     dt = time.perf_counter() - t0
     n_out = sum(int(r.size) for r in rows)
     del rows
     ascans = 12 * vol.ny * vol.lay.n_x_px
+    # host memory traffic of the drop-in path per volume: the reader's copy into
+    # the pinned slots (read + write), the DMA reads of those slots and the DMA
+    # writes of the float32 planes
+    host_bytes = 3 * vol.raw_bytes() + 4 * n_out
     return {"value": ascans / dt, "unit": "A-scans/s", "ms_per_volume": dt * 1e3,
             "h2d_bytes_per_volume": vol.raw_bytes(), "d2h_bytes_per_volume": 4 * n_out,
+            "host_memory_bytes_per_volume": host_bytes,
+            "timers_ms": {k: round(v * 1e3, 2) for k, v in R.timers.items()},
             "batch_frames": batch, "io_threads": io_threads,
             "source": "octrecon Reconstructor.process_row on device gb300 (reference pipeline, plug-in "
                       "registered), both y-rows; reader serves the B-scans from host memory; float32 dB out"}
