@@ -288,6 +288,11 @@ def gpu_arm(args, rank, world):
     bits = torch.empty(n_out, dtype=torch.int16, device=dev)
     ascans = 12 * vol.ny * vol.lay.n_x_px
 
+    # the stitch kernel's tile shape (output rows per block), autotuned on this volume
+    from oct_recon_af_v1_gb300 import autotune
+    stitch_rows, stitch_ms = autotune.tune_stitch_rows(
+        ctx, lambda: run_step(ctx, vol, vol.raw, db_vol, bits, args.batch), stream,
+        key=("config1", vol.ny, vol.nz, vol.nx, args.batch))
     graph = None
     if not args.no_graph:
         run_step(ctx, vol, vol.raw, db_vol, bits, args.batch)      # sizes every buffer
@@ -367,7 +372,8 @@ def gpu_arm(args, rank, world):
         "vs_baseline": None, "dtype": "f32 (uint16 in, uint16 out)", "data": "synthetic (seeded, generated on device)",
         "config": config1_desc(vol.ny),
         "execution": {"parallelism": f"replicas x{world} (independent volumes)", "frame_batch": args.batch,
-                      "cuda_graph": graph is not None, "a_scans_per_step": ascans},
+                      "cuda_graph": graph is not None, "a_scans_per_step": ascans,
+                      "stitch_rows": stitch_rows, "stitch_rows_ms": stitch_ms},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": SPECTRAL_DRAM_BYTES_PER_ASCAN * kascans,

@@ -300,6 +300,12 @@ int octgb_selftest_wait_expiry(octgb_ctx *ctx, int which, int wait_limit_us);
  * launched has completed); their ids become invalid and octgb_set_geometry is
  * accepted again.  No counterpart in the reference (its loop has no graphs). */
 int octgb_graphs_release(octgb_ctx *ctx);
+/* Tile shape of octgb_frames_process's stitch kernel: output rows per block
+ * (32, 64 or 128; each block is 32 columns wide; default 64).  Results do not
+ * depend on it (every voxel sums its tiles in the same order); the
+ * autotuner picks the fastest for a workload.  Graphs already captured keep
+ * the shape they were captured with.  Not during graph capture. */
+int octgb_set_stitch_rows(octgb_ctx *ctx, int rows);
 
 /* ---------------------------------------------------------------- batched form */
 

@@ -50,6 +50,7 @@ SIGNATURES = {
     "octgb_graph_end": (c_int, [c_void_p, POINTER(c_int)]),
     "octgb_graph_launch": (c_int, [c_void_p, c_int]),
     "octgb_graphs_release": (c_int, [c_void_p]),
+    "octgb_set_stitch_rows": (c_int, [c_void_p, c_int]),
     "octgb_selftest_wait_expiry": (c_int, [c_void_p, c_int, c_int]),
     "octgb_magnitude_noalloc": (c_int, [c_void_p, c_void_p, c_int, c_int, c_int, c_int, c_void_p]),
     "octgb_batch_process": (c_int, [c_void_p, c_int, c_void_p, c_int, c_float, c_int]),
@@ -560,6 +561,10 @@ class Context:
     def graphs_release(self):
         """Destroy the context's captured graphs (a new geometry is refused while any exist)."""
         self._check(self.lib.octgb_graphs_release(self.h))
+
+    def set_stitch_rows(self, rows: int):
+        """Output rows per block of frames_process's stitch kernel (32, 64 or 128; results do not depend on it)."""
+        self._check(self.lib.octgb_set_stitch_rows(self.h, int(rows)))
 
     # -------------------------------------------------------------- batched form
     def batch_process(self, tiles, threshold: float, grab: int = 4, raw_dtype: int = U16):

@@ -1,4 +1,5 @@
-"""Launch-shape autotuner for the batched form (octgb_batch_process).
+"""Launch-shape autotuners: the batched form's work queue (octgb_batch_process)
+and the frame API's stitch tile shape (octgb_set_stitch_rows).
 
 The persistent spectral kernel takes `grab` groups of 4 A-scans per atomic
 operation on the work queue: small grabs balance load across SMs at the end
@@ -51,3 +52,40 @@ def tune_batch(ctx, tiles, threshold: float, stream, reps: int = 2, grabs=GRABS,
     best = min(timings, key=timings.get)
     _CACHE[sig] = (best[0], best[1], {f"{g}/{o}": round(t, 3) for (g, o), t in timings.items()})
     return _CACHE[sig]
+
+
+STITCH_ROWS = (32, 64, 128)
+
+
+def tune_stitch_rows(ctx, step, stream, key, reps: int = 3, rows=STITCH_ROWS):
+    """Output rows per stitch block of octgb_frames_process (its tile shape:
+    32, 64 or 128 rows x 32 columns).  `step` runs one whole workload through
+    the frame API (not under graph capture); each candidate is run once to
+    build its slot tables, then timed over `reps` runs with CUDA events on the
+    launching stream.  Every voxel sums its tiles in the same order for every
+    shape, so the choice changes the time only.  Leaves the fastest set on the
+    context and returns (rows, {rows: ms}); cached per `key`."""
+    import torch
+    if key in _CACHE:
+        best, table = _CACHE[key]
+        ctx.set_stitch_rows(best)
+        return best, table
+    table = {}
+    for r in rows:
+        try:
+            ctx.set_stitch_rows(r)
+            step()
+        except Exception:                                   # a shape whose patches exceed shared memory
+            continue
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(reps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        table[r] = round(e0.elapsed_time(e1) / reps, 3)
+    best = min(table, key=table.get)
+    ctx.set_stitch_rows(best)
+    _CACHE[key] = (best, table)
+    return best, table

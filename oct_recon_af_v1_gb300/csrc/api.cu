@@ -99,7 +99,7 @@ struct Plan {
 // Which tiles touch each output block of the frame-batch stitch kernel, with
 // their patch extents and shared-memory offsets; built once per tile list.
 struct SlotTable {
-    std::vector<int> key;        // plan ids, n_out_z, n_out_x
+    std::vector<int> key;        // plan ids, n_out_z, n_out_x, rows per block
     DevBuf slots, counts;
     size_t smem = 0;             // largest patch footprint of a block (bytes)
     int ns_max = 1;              // most tiles touching one block
@@ -133,6 +133,7 @@ std::string g_create_error;
 struct octgb_ctx {
     int device = 0;
     int num_sms = 0;
+    int stitch_rows = kStitchRows;           // frame-batch stitch block height (octgb_set_stitch_rows)
     cudaStream_t own = nullptr;
     cudaStream_t stream = nullptr;
     std::string err;
@@ -325,14 +326,15 @@ void read_minmax(octgb_ctx* c, const unsigned int* mm_dev, double* out2) {
     }
 }
 
-const SlotTable& slot_table(octgb_ctx* c, int n_tiles, const int* plan_ids, int n_out_z, int n_out_x) {
+const SlotTable& slot_table(octgb_ctx* c, int n_tiles, const int* plan_ids, int n_out_z, int n_out_x, int rows) {
     std::vector<int> key(plan_ids, plan_ids + n_tiles);
     key.push_back(n_out_z);
     key.push_back(n_out_x);
+    key.push_back(rows);
     for (SlotTable* t : c->slot_tables)
         if (t->key == key) return *t;
     require(!c->capturing, "first use of a tile list during graph capture: run the sequence once before capturing");
-    const int nxb = (n_out_x + kBlk - 1) / kBlk, nzb = (n_out_z + kStitchRows - 1) / kStitchRows;
+    const int nxb = (n_out_x + kBlk - 1) / kBlk, nzb = (n_out_z + rows - 1) / rows;
     std::vector<StitchSlot> slots(static_cast<size_t>(nxb) * nzb * n_tiles);
     std::vector<int> counts(static_cast<size_t>(nxb) * nzb, 0);
     size_t smem = 0;
@@ -346,7 +348,7 @@ const SlotTable& slot_table(octgb_ctx* c, int n_tiles, const int* plan_ids, int 
                 const int cbi = bx - p.cblk_first;
                 if (cbi < 0 || cbi >= p.n_cblk || p.cblk_h[cbi].x < 0) continue;
                 int lo = 1 << 30, hi = -1;
-                for (int k = bz * (kStitchRows / kBlk); k < (bz + 1) * (kStitchRows / kBlk); ++k) {
+                for (int k = bz * (rows / kBlk); k < (bz + 1) * (rows / kBlk); ++k) {
                     if (k >= static_cast<int>(p.zblk_h.size()) || p.zblk_h[k].x < 0) continue;
                     lo = lo < p.zblk_h[k].x ? lo : p.zblk_h[k].x;
                     hi = hi > p.zblk_h[k].y ? hi : p.zblk_h[k].y;
@@ -1178,10 +1180,10 @@ int octgb_frames_process(octgb_ctx* c, int n_tiles, const int* plan_ids, const v
             c->launches++;
         }
         ck(c->run_mm.ensure(2 * sizeof(unsigned int)), "cudaMalloc(run mm)");
-        const SlotTable& stab = slot_table(c, n_tiles, plan_ids, n_out_z, n_out_x);
+        const SlotTable& stab = slot_table(c, n_tiles, plan_ids, n_out_z, n_out_x, c->stitch_rows);
         ck(launch_stitch_frames(c->plan_table.as<StitchDev>(), tl, stab.slots.as<StitchSlot>(), stab.counts.as<int>(),
                                 stab.ns_max, stab.smem, c->magbuf.as<float>(), tile_stride, B, nx, f0, n_out_z, n_out_x, thr, dst,
-                                pmm, c->run_mm.as<unsigned int>(), c->stream),
+                                pmm, c->run_mm.as<unsigned int>(), c->stitch_rows, c->stream),
            "stitch frames kernel");
         c->launches++;
         if (db_loc != OCTGB_DEVICE) copy_out(c, db, OCTGB_HOST, dst, db_bytes);
@@ -1285,6 +1287,14 @@ int octgb_graphs_release(octgb_ctx* c) {
         c->graphs.clear();
         c->graph_kernels.clear();
         for (QTable* t : c->qtables) t->pinned = false;
+    });
+}
+
+int octgb_set_stitch_rows(octgb_ctx* c, int rows) {
+    return guarded(c, [&] {
+        if (c->capturing) throw Error(OCTGB_ERR_STATE, "octgb_set_stitch_rows during graph capture");
+        require(rows == 32 || rows == 64 || rows == 128, "stitch rows must be 32, 64 or 128");
+        c->stitch_rows = rows;
     });
 }
 

@@ -135,7 +135,7 @@ struct TileList {
 cudaError_t launch_stitch(const StitchDev& p, const float* mag, const int* frame_y, int f0, int B, float* num,
                           float* den, int frame_offset, int n_out_x, int xs_max, int rs_max, cudaStream_t st);
 // frames API: all tiles of a frame batch, num/den kept on chip, dB + clim written
-constexpr int kStitchRows = 64;   // output rows per frame-batch stitch block (x 32 columns)
+constexpr int kStitchRows = 64;   // default output rows per frame-batch stitch block (x 32 columns; 32, 64 or 128)
 struct StitchSlot {               // one tile touching one output block
     int t;                        // index into the TileList
     int x_lo, xs;                 // A-scans read
@@ -147,7 +147,8 @@ struct StitchSlot {               // one tile touching one output block
 cudaError_t launch_stitch_frames(const StitchDev* plans_dev, const TileList& tiles, const StitchSlot* slots,
                                  const int* slot_count, int ns_max, size_t patch_smem_bytes, const float* mag,
                                  int64_t mag_tile_stride, int B, int n_tile_x, int f0, int n_out_z, int n_out_x,
-                                 float thr, float* db, unsigned int* plane_mm, unsigned int* run_mm, cudaStream_t st);
+                                 float thr, float* db, unsigned int* plane_mm, unsigned int* run_mm, int rows,
+                                 cudaStream_t st);
 cudaError_t launch_finalise(const float* num, const float* den, int64_t n_per_plane, int n_planes, float thr,
                             float* db, unsigned int* plane_minmax, cudaStream_t st);
 // quantisation: `table` is scratch of kQuantTable floats (the code thresholds of the clim)

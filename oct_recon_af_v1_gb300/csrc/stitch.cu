@@ -185,9 +185,8 @@ __device__ __forceinline__ void warp_minmax(float& mn, float& mx) {
 // with a few parallel loads.  All contributing patches and the tiles' row /
 // column interpolation parameters are staged in shared memory first (one
 // barrier, many loads in flight), then every voxel sums the tiles in order.
-constexpr int kFZ = kStitchRows;             // output rows per CTA
-constexpr int kFRows = kFZ / 8;              // rows per thread
-
+// kFZ output rows per CTA (the tile shape the autotuner picks: 32, 64 or 128)
+template <int kFZ>
 __global__ void __launch_bounds__(kStThreads) k_stitch_frames(const StitchDev* __restrict__ plans, const TileList tl,
                                                               const StitchSlot* __restrict__ slots,
                                                               const int* __restrict__ slot_count,
@@ -196,6 +195,7 @@ __global__ void __launch_bounds__(kStThreads) k_stitch_frames(const StitchDev* _
                                                               float thr, float* __restrict__ db,
                                                               unsigned int* __restrict__ plane_mm,
                                                               unsigned int* __restrict__ run_mm, int ns_max) {
+    constexpr int kFRows = kFZ / 8;          // rows per thread
     // dynamic shared memory: per-slot row / column parameters, then the patches
     extern __shared__ __align__(16) float smem_all[];
     __shared__ StitchSlot slot[kMaxSeg];
@@ -597,17 +597,18 @@ cudaError_t launch_stitch(const StitchDev& p, const float* mag, const int* frame
 cudaError_t launch_stitch_frames(const StitchDev* plans_dev, const TileList& tiles, const StitchSlot* slots,
                                  const int* slot_count, int ns_max, size_t patch_smem_bytes, const float* mag,
                                  int64_t mag_tile_stride, int B, int n_tile_x, int f0, int n_out_z, int n_out_x,
-                                 float thr, float* db, unsigned int* plane_mm, unsigned int* run_mm, cudaStream_t st) {
+                                 float thr, float* db, unsigned int* plane_mm, unsigned int* run_mm, int rows,
+                                 cudaStream_t st) {
     if (B == 0) return cudaSuccess;
-    const size_t smem = patch_smem_bytes + sizeof(float) * static_cast<size_t>(ns_max) * (6 * kFZ + 4 * kBlk) + 16;
+    if (rows != 32 && rows != 64 && rows != 128) return cudaErrorInvalidValue;
+    const size_t smem = patch_smem_bytes + sizeof(float) * static_cast<size_t>(ns_max) * (6 * rows + 4 * kBlk) + 16;
     if (smem > 160 * 1024) return cudaErrorInvalidValue;
-    cudaError_t e = cudaFuncSetAttribute(k_stitch_frames, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         static_cast<int>(smem));
+    auto kern = rows == 32 ? k_stitch_frames<32> : (rows == 64 ? k_stitch_frames<64> : k_stitch_frames<128>);
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     if (e != cudaSuccess) return e;
-    const dim3 grid((n_out_x + kBlk - 1) / kBlk, (n_out_z + kFZ - 1) / kFZ, B);
-    k_stitch_frames<<<grid, kStThreads, smem, st>>>(plans_dev, tiles, slots, slot_count, mag, mag_tile_stride,
-                                                     n_tile_x, f0, n_out_z, n_out_x, thr, db, plane_mm, run_mm,
-                                                     ns_max);
+    const dim3 grid((n_out_x + kBlk - 1) / kBlk, (n_out_z + rows - 1) / rows, B);
+    kern<<<grid, kStThreads, smem, st>>>(plans_dev, tiles, slots, slot_count, mag, mag_tile_stride, n_tile_x, f0,
+                                         n_out_z, n_out_x, thr, db, plane_mm, run_mm, ns_max);
     return cudaGetLastError();
 }
 

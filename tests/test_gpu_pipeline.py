@@ -172,3 +172,43 @@ def test_frames_host_input_ring_matches_device_input(gpu_ctx):
     a, b = out_h.cpu().numpy(), out_d.cpu().numpy()
     assert np.isfinite(a).any()
     np.testing.assert_array_equal(a, b)
+
+
+def test_frames_stitch_rows_do_not_change_result(gpu_ctx):
+    """The stitch kernel's tile shape (32, 64 or 128 output rows per block, the
+    autotuner's choice) changes no voxel and no clim: every voxel sums the same
+    tiles in the same order."""
+    torch = pytest.importorskip("torch")
+    from oct_recon_af_v1_gb300 import geometry as G
+    from oct_recon_af_v1_gb300 import stitching as S
+    from oct_recon_af_v1_gb300 import synthetic
+    from oct_recon_af_v1_gb300._lib import OctgbError
+    sg = G.build_spectral_geometry(synthetic.lambda_nm(), synthetic.beta_ref_from_px(1e-5), 1.33)
+    gpu_ctx.set_geometry(sg.sinc_idx, sg.sinc_w, sg.window)
+    lay = S.ScanLayout(np.array([-0.0225, 0.0225]), np.array([0.0]), np.array([0.0, 0.05]), 50, 4, 0.05, 0.004)
+    tg = S.tiled_geometry(lay, sg.z_um, [300.0, 320.0], 1.0)
+    order = [(xi, zi) for xi in range(2) for zi in range(2)]
+    ids = []
+    for xi, zi in order:
+        st = S.TileStitcher.build(tg, lay.x_centers_mm[xi], lay.z_depths_mm[zi], [300.0, 320.0][zi], 80.0)
+        ids.append(st.upload(gpu_ctx))
+    dev = [synthetic.u16_bits(synthetic.generate(4, 50, 25, seed=60 + k)).cuda() for k in range(len(order))]
+    nz, nx = len(tg.out_z_mm), len(tg.out_x_mm)
+    thr = S.min_weight_threshold(np.float32)
+    outs, clims = {}, {}
+    try:
+        for rows in (64, 32, 128):
+            gpu_ctx.set_stitch_rows(rows)
+            out = torch.empty((4, nz, nx), dtype=torch.float32, device="cuda")
+            gpu_ctx.clim_reset()
+            gpu_ctx.frames_process(ids, dev, 25, 0, nz, nx, thr, out=out, raw_dtype=0)
+            gpu_ctx.synchronize()
+            outs[rows], clims[rows] = out.cpu().numpy(), gpu_ctx.clim_get()
+        assert np.isfinite(outs[64]).any()
+        for rows in (32, 128):
+            np.testing.assert_array_equal(outs[rows], outs[64])
+            assert clims[rows] == clims[64]
+        with pytest.raises(OctgbError):
+            gpu_ctx.set_stitch_rows(48)
+    finally:
+        gpu_ctx.set_stitch_rows(64)
