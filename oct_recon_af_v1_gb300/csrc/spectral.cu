@@ -84,9 +84,22 @@ __device__ __forceinline__ float mul_window(float x, float2 h2, bool& safe) {
     return o;
 }
 
+// Where slot s of quad q reads its raw row and apodisation row and writes
+// its result.  Static mode: quads of one batch (n_seg segments of B x nx
+// A-scans).  Queue mode: quads of the tile table (quad0 prefix in shared
+// memory, binary search).
+struct SlotRef {
+    const void* row;     // raw row (kN samples)
+    int64_t apod_row;    // row of the apodisation-mean buffer
+    int64_t as;          // static: global A-scan index; queue: A-scan index within the tile
+    int tile;            // queue: tile index
+    bool valid;
+};
+
 template <typename RawT>
 struct Smem {
     uint64_t bar[2];
+    SlotRef slot[2][kPerCta];                       // the quad of each stage buffer (thread 0 fills it)
     float red[kPerCta][4];
     float mval[kPerCta];
     unsigned int mm[2];
@@ -106,42 +119,43 @@ static_assert(sizeof(Smem<uint16_t>) + 2 * sizeof(int64_t) + kMaxQueueTiles * si
 static_assert(sizeof(Smem<float>) + 2 * sizeof(int64_t) + kMaxQueueTiles * sizeof(unsigned) <= 232448,
               "spectral kernel shared memory (float32 raws) exceeds 227 KB");
 
-// Where slot s of quad q reads its raw row and apodisation row and writes
-// its result.  Static mode: quads of one batch (n_seg segments of B x nx
-// A-scans).  Queue mode: quads of the tile table (quad0 prefix in shared
-// memory, binary search).
-struct SlotRef {
-    const void* row;     // raw row (kN samples)
-    int64_t apod_row;    // row of the apodisation-mean buffer
-    int64_t as;          // static: global A-scan index; queue: A-scan index within the tile
-    int tile;            // queue: tile index
-    bool valid;
-};
-
+// A launch holds fewer than 2^31 A-scans (the host checks), so the index
+// arithmetic is 32-bit.  Queue mode: a CTA takes its quads in increasing
+// order, so the tile holding quad q is found by stepping forward from the
+// previous one (`hint`); a binary search is the fallback.
 template <typename RawT, bool Queue>
-__device__ __forceinline__ SlotRef slot_ref(const SpectralArgs& a, const unsigned int* quad0_s, int64_t q, int s) {
+__device__ __forceinline__ SlotRef slot_ref(const SpectralArgs& a, const unsigned int* quad0_s, int64_t q, int s,
+                                            int& hint) {
     SlotRef r;
     if (!Queue) {
-        const int64_t as = q * kPerCta + s;
-        r.valid = as < a.n_ascans;
-        const int64_t asc = r.valid ? as : 0;
-        const int64_t bt = asc / a.nx, x = asc - bt * a.nx;   // bt = segment * B + b
-        const int sg = static_cast<int>(bt / a.B);
-        const int64_t b = bt - static_cast<int64_t>(sg) * a.B;
-        r.row = static_cast<const RawT*>(a.seg[sg]) + ((b * a.interf + a.apod + x) * kN);
+        const unsigned int as = static_cast<unsigned int>(q) * kPerCta + static_cast<unsigned int>(s);
+        r.valid = static_cast<int64_t>(as) < a.n_ascans;
+        const unsigned int asc = r.valid ? as : 0u;
+        const unsigned int nx = static_cast<unsigned int>(a.nx);
+        const unsigned int bt = asc / nx, x = asc - bt * nx;   // bt = segment * B + b
+        const unsigned int sg = bt / static_cast<unsigned int>(a.B);
+        const unsigned int b = bt - sg * static_cast<unsigned int>(a.B);
+        r.row = static_cast<const RawT*>(a.seg[sg]) + ((static_cast<int64_t>(b) * a.interf + a.apod + x) * kN);
         r.apod_row = bt;
         r.as = as;
         r.tile = 0;
     } else {
-        int lo = 0, hi = a.n_qt - 1;                // last tile with quad0 <= q
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (quad0_s[mid] <= static_cast<unsigned int>(q)) lo = mid; else hi = mid - 1;
+        const unsigned int uq = static_cast<unsigned int>(q);
+        int lo = hint;                               // last tile with quad0 <= q
+        if (quad0_s[lo] > uq) {
+            int hi = lo;
+            lo = 0;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (quad0_s[mid] <= uq) lo = mid; else hi = mid - 1;
+            }
         }
+        while (lo + 1 < a.n_qt && quad0_s[lo + 1] <= uq) ++lo;
+        hint = lo;
         const QueueTile& t = a.qt[lo];
-        const int64_t lq = q - t.quad0;
-        const int64_t b = lq / t.qpb;                  // quads are aligned to B-scans
-        const int qb = static_cast<int>(lq - b * t.qpb);
+        const unsigned int lq = uq - t.quad0;
+        const unsigned int b = lq / static_cast<unsigned int>(t.qpb);   // quads are aligned to B-scans
+        const int qb = static_cast<int>(lq - b * static_cast<unsigned int>(t.qpb));
         // the last quad of a B-scan ends on its last A-scan (it may repeat up
         // to three A-scans of the previous quad), so both edge columns find
         // their lateral neighbour in the same quad
@@ -149,7 +163,7 @@ __device__ __forceinline__ SlotRef slot_ref(const SpectralArgs& a, const unsigne
         const int64_t x = xs + s;
         // a quad outside this tile's range (only possible with a table that
         // does not match total_quads) reads and writes nothing
-        r.valid = x < t.nx && lq >= 0 && lq < static_cast<int64_t>(t.nquads);
+        r.valid = x < t.nx && lq < t.nquads;
         const int64_t xc = r.valid ? x : 0;
         const int64_t bc = r.valid ? b : 0;
         r.row = static_cast<const RawT*>(t.raw) + ((bc * t.interf + t.apod + xc) * kN);
@@ -252,13 +266,15 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
         item_end = base + a.grab < nquads ? base + a.grab : nquads;
         return base;
     };
+    int tile_hint = 0;                                 // thread 0: tile of the last quad issued
     auto issue = [&](int64_t quad, int buf, bool first) {
         int nvalid = 0;
         SlotRef r[kPerCta];
 #pragma unroll
         for (int k = 0; k < kPerCta; ++k) {
-            r[k] = slot_ref<RawT, kQueue>(a, quad0_s, quad, k);
+            r[k] = slot_ref<RawT, kQueue>(a, quad0_s, quad, k, tile_hint);
             nvalid += r[k].valid ? 1 : 0;
+            S.slot[buf][k] = r[k];                     // read by every thread once the buffer is current
         }
         mbar_expect_tx(&S.bar[buf], static_cast<uint32_t>(nvalid) * kN * sizeof(RawT) + starved_bytes(first));
 #pragma unroll
@@ -293,7 +309,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
         }
 
         // ---- (b) background: d = raw - apod, line mean (group g, A-scan g) ----
-        const SlotRef me = slot_ref<RawT, kQueue>(a, quad0_s, quad, g);
+        const SlotRef me = S.slot[buf][g];
         const bool valid = me.valid;
         const float* apod = a.apod_mean + me.apod_row * kN;
         // d = raw - apod stays in registers until the line mean m is known;
@@ -605,6 +621,8 @@ cudaError_t launch_apod_mean_tiles(const QueueTile* tiles_dev, int n_tiles, int 
 }
 
 cudaError_t launch_spectral(const SpectralArgs& a, int dtype, int mode, int grid, cudaStream_t st) {
+    // the kernel's slot arithmetic is 32-bit (q * 4 + s, quads of a tile)
+    if (a.n_ascans >= (int64_t(1) << 31) || a.total_quads >= (1u << 31)) return cudaErrorInvalidValue;
     if (dtype == 0) return launch_mode<uint16_t>(a, mode, grid, st);
     if (dtype == 1) return launch_mode<int16_t>(a, mode, grid, st);
     return launch_mode<float>(a, mode, grid, st);
