@@ -252,7 +252,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
     float run_min = __int_as_float(0x7f800000), run_max = -__int_as_float(0x7f800000);
     __syncthreads();
 
-    // thread 0 owns the schedule: the next quad after `cur`
+    // the next quad after `cur` (lane 0 of warp 0)
     int64_t item_next = 0, item_end = 0;               // queue mode: current grab [next, end)
     auto next_quad = [&](int64_t cur) -> int64_t {
         if (!kQueue) {
@@ -266,25 +266,32 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
         item_end = base + a.grab < nquads ? base + a.grab : nquads;
         return base;
     };
-    int tile_hint = 0;                                 // thread 0: tile of the last quad issued
+    // warp 0 issues a quad: lane k < 4 resolves slot k (in parallel) and copies
+    // its row; lane 0 arms the buffer's barrier first
+    int tile_hint = 0;                                 // lanes 0-3: tile of the last quad issued
     auto issue = [&](int64_t quad, int buf, bool first) {
-        int nvalid = 0;
-        SlotRef r[kPerCta];
-#pragma unroll
-        for (int k = 0; k < kPerCta; ++k) {
-            r[k] = slot_ref<RawT, kQueue>(a, quad0_s, quad, k, tile_hint);
-            nvalid += r[k].valid ? 1 : 0;
-            S.slot[buf][k] = r[k];                     // read by every thread once the buffer is current
+        SlotRef r{};
+        bool v = false;
+        if (lane < kPerCta) {
+            r = slot_ref<RawT, kQueue>(a, quad0_s, quad, lane, tile_hint);
+            v = r.valid;
+            S.slot[buf][lane] = r;                     // read by every thread once the buffer is current
         }
-        mbar_expect_tx(&S.bar[buf], static_cast<uint32_t>(nvalid) * kN * sizeof(RawT) + starved_bytes(first));
-#pragma unroll
-        for (int k = 0; k < kPerCta; ++k)
-            if (r[k].valid) tma_bulk_g2s(&S.stage[buf][k][0], r[k].row, kN * sizeof(RawT), &S.bar[buf]);
+        const uint32_t nvalid = static_cast<uint32_t>(__popc(__ballot_sync(0xffffffffu, v)));
+        if (lane == 0) mbar_expect_tx(&S.bar[buf], nvalid * kN * sizeof(RawT) + starved_bytes(first));
+        __syncwarp();
+        if (v) tma_bulk_g2s(&S.stage[buf][lane][0], r.row, kN * sizeof(RawT), &S.bar[buf]);
+    };
+    // lane 0 of warp 0 owns the schedule; the quad is shared with the warp
+    auto warp_next = [&](int64_t cur) -> int64_t {
+        int64_t n = 0;
+        if (lane == 0) n = next_quad(cur);
+        return static_cast<int64_t>(__shfl_sync(0xffffffffu, static_cast<long long>(n), 0));
     };
 
-    if (tid == 0) {
-        const int64_t q0 = next_quad(-1);
-        qbuf[0] = q0;
+    if (warp == 0) {
+        const int64_t q0 = warp_next(-1);
+        if (lane == 0) qbuf[0] = q0;
         if (q0 >= 0) issue(q0, 0, true);
     }
     __syncthreads();
@@ -293,11 +300,20 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
         const int buf = it & 1;
         const int64_t quad = qbuf[buf];
         if (quad < 0) break;
-        if (tid == 0) {
-            const int64_t nq = next_quad(quad);
-            qbuf[buf ^ 1] = nq;
+        if (warp == 0) {
+            const int64_t nq = warp_next(quad);
+            if (lane == 0) qbuf[buf ^ 1] = nq;
             if (nq >= 0) issue(nq, buf ^ 1, false);
         }
+
+        // this group's apodisation row does not depend on the raw copy: its
+        // loads are in flight while the copy is awaited
+        const SlotRef me = S.slot[buf][g];
+        const bool valid = me.valid;
+        const float* apod = a.apod_mean + me.apod_row * kN;
+        float4 apv[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) apv[q] = __ldg(reinterpret_cast<const float4*>(apod + 4 * lt + 512 * q));
 
         const bool ok = mbar_wait_bounded(&S.bar[buf], (it >> 1) & 1, a.status);
         if (__syncthreads_or(!ok)) {
@@ -309,9 +325,6 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
         }
 
         // ---- (b) background: d = raw - apod, line mean (group g, A-scan g) ----
-        const SlotRef me = S.slot[buf][g];
-        const bool valid = me.valid;
-        const float* apod = a.apod_mean + me.apod_row * kN;
         // d = raw - apod stays in registers until the line mean m is known;
         // shared memory receives d - m (the float32 value the reference
         // stores, cpu_kernels.py:35-36), so the sinc reads its window as is
@@ -322,7 +335,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
             const int j = 4 * lt + 512 * q;
             float rv[4];
             RawLoad<RawT>::load4(&S.stage[buf][g][j], rv);
-            const float4 ap = __ldg(reinterpret_cast<const float4*>(apod + j));
+            const float4 ap = apv[q];
             dv[4 * q] = rv[0] - ap.x;
             dv[4 * q + 1] = rv[1] - ap.y;
             dv[4 * q + 2] = rv[2] - ap.z;
