@@ -53,9 +53,9 @@ sys.path.insert(0, str(ROOT))
 METRIC = "A-scans/s on 1 GB300 (fused vs plain FP32; learned vs search β) at ≤1 LSB"
 APOD = 25
 # DRAM bytes per A-scan of the spectral kernel from one ncu capture
-# (profiles/k_spectral_config1_small.md: (49.45 + 7.74) MB over 12 000 A-scans;
+# (profiles/k_spectral_config1_small.md: (49.44 + 7.31) MB over 12 000 A-scans;
 # caches flushed before the kernel, magnitudes partly still in L2 at its end)
-SPECTRAL_DRAM_BYTES_PER_ASCAN = (49.447680e6 + 7.744512e6) / 12000
+SPECTRAL_DRAM_BYTES_PER_ASCAN = (49.435136e6 + 7.309824e6) / 12000
 
 
 # ------------------------------------------------------------------------ workload description
@@ -290,9 +290,13 @@ def gpu_arm(args, rank, world):
 
     # the stitch kernel's tile shape (output rows per block), autotuned on this volume
     from oct_recon_af_v1_gb300 import autotune
-    stitch_rows, stitch_ms = autotune.tune_stitch_rows(
-        ctx, lambda: run_step(ctx, vol, vol.raw, db_vol, bits, args.batch), stream,
-        key=("config1", vol.ny, vol.nz, vol.nx, args.batch))
+    if args.stitch_rows:
+        stitch_rows, stitch_ms = args.stitch_rows, None
+        ctx.set_stitch_rows(stitch_rows)
+    else:
+        stitch_rows, stitch_ms = autotune.tune_stitch_rows(
+            ctx, lambda: run_step(ctx, vol, vol.raw, db_vol, bits, args.batch), stream,
+            key=("config1", vol.ny, vol.nz, vol.nx, args.batch))
     graph = None
     if not args.no_graph:
         run_step(ctx, vol, vol.raw, db_vol, bits, args.batch)      # sizes every buffer
@@ -1301,6 +1305,8 @@ def main():
     ap.add_argument("--config", type=int, default=1, choices=[0, 1, 2, 3, 4])
     ap.add_argument("--train4", type=int, default=20000, help="training images of the learned estimator (config 4)")
     ap.add_argument("--epochs4", type=int, default=8, help="training epochs (config 4)")
+    ap.add_argument("--stitch-rows", type=int, default=0, choices=[0, 32, 64, 128],
+                    help="fix the stitch kernel's rows per block instead of autotuning them (config 1)")
     ap.add_argument("--train-fp32", action="store_true",
                     help="train the learned estimator with the float32 SIMT kernels instead of the tensor cores")
     ap.add_argument("--tiles3", type=int, default=64, help="tiles of the batched workload (config 3)")

@@ -52,21 +52,24 @@ __global__ void __launch_bounds__(kThreads, 2) k_disp_mag(const DispArgs a) {
         S.tw3[r][j] = __ldg(a.tw + (r * j) % kN);
     }
     __syncthreads();
-    const int64_t n_items = static_cast<int64_t>(a.n_beta) * a.nb * a.nx;
-    for (int64_t item = static_cast<int64_t>(blockIdx.x) * kPerCta + g; item < n_items;
-         item += static_cast<int64_t>(gridDim.x) * kPerCta) {
-        const int64_t bx = item % (static_cast<int64_t>(a.nb) * a.nx);
-        const int gi = static_cast<int>(item / (static_cast<int64_t>(a.nb) * a.nx));
-        const int bi = static_cast<int>(bx / a.nx);
-        const int x = static_cast<int>(bx - static_cast<int64_t>(bi) * a.nx);
-        const float2* ph = a.phase + static_cast<int64_t>(gi) * kN;
+    // items < 2^32 - 2 kPerCta gridDim (the launcher checks): 32-bit item arithmetic
+    const unsigned int nbx = static_cast<unsigned int>(a.nb) * static_cast<unsigned int>(a.nx);
+    const unsigned int n_items = static_cast<unsigned int>(a.n_beta) * nbx;
+    for (unsigned int item = blockIdx.x * kPerCta + g; item < n_items; item += gridDim.x * kPerCta) {
+        const unsigned int gu = item / nbx, bx = item - gu * nbx;
+        const unsigned int bu = bx / static_cast<unsigned int>(a.nx);
+        const unsigned int x = bx - bu * static_cast<unsigned int>(a.nx);
+        const float2* ph = a.phase + static_cast<int64_t>(gu) * kN;
+        // repeat rp of A-scan x of B-scan b0 + bu: line0 + rp * nx * kN
+        const float* line0 =
+            a.X + ((static_cast<int64_t>(a.b0 + static_cast<int>(bu)) * a.rep) * a.nx + x) * kN;
         float acc[2][4];
 #pragma unroll
         for (int h = 0; h < 2; ++h)
 #pragma unroll
             for (int r = 0; r < 4; ++r) acc[h][r] = 0.f;
         for (int rp = 0; rp < a.rep; ++rp) {
-            const float* line = a.X + ((static_cast<int64_t>(a.b0 + bi) * a.rep + rp) * a.nx + x) * kN;
+            const float* line = line0 + static_cast<int64_t>(rp) * a.nx * kN;
             float2 v[16];
 #pragma unroll
             for (int r = 0; r < 16; ++r) {
@@ -98,11 +101,11 @@ __global__ void __launch_bounds__(kThreads, 2) k_disp_mag(const DispArgs a) {
                 const int z0 = zi * a.z_keep / 256, z1 = ((zi + 1) * a.z_keep + 255) / 256;
                 float sum = 0.f;
                 for (int z = z0; z < z1; ++z) sum += M[z];
-                a.zcol[item * 256 + zi] = sum;
+                a.zcol[static_cast<int64_t>(item) * 256 + zi] = sum;
             }
             continue;                                   // the next transform writes the line after a group barrier
         }
-        float* out = a.A + item * kHalf;
+        float* out = a.A + static_cast<int64_t>(item) * kHalf;
 #pragma unroll
         for (int h = 0; h < 2; ++h)
 #pragma unroll
@@ -397,6 +400,7 @@ cudaError_t launch_disp_mag(const DispArgs& a, int num_sms, cudaStream_t st) {
                                          static_cast<int>(smem));
     if (e != cudaSuccess) return e;
     const int64_t items = static_cast<int64_t>(a.n_beta) * a.nb * a.nx;
+    if (items >= (int64_t(1) << 32) - 2 * kPerCta * num_sms) return cudaErrorInvalidValue;   // 32-bit item index
     int64_t grid = (items + kPerCta - 1) / kPerCta;
     if (grid > 2 * num_sms) grid = 2 * num_sms;
     k_disp_mag<<<static_cast<int>(grid), kThreads, smem, st>>>(a);

@@ -354,13 +354,14 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
                 *reinterpret_cast<float4*>(&S.d[g][4 * lt + 512 * q]) =
                     make_float4(dv[4 * q] - m, dv[4 * q + 1] - m, dv[4 * q + 2] - m, dv[4 * q + 3] - m);
         }
+        // the window of this thread's four outputs: in flight across the barrier
+        const float4 wa = __ldg(reinterpret_cast<const float4*>(a.g.win + 4 * tid));
+        const float4 wb = __ldg(reinterpret_cast<const float4*>(a.g.win + 4 * tid + 2));
         __syncthreads();
 
         // ---- (c)+(d) sinc k-linearisation and window, four A-scans ----
         {
             const int i0 = 4 * tid;
-            const float4 wa = __ldg(reinterpret_cast<const float4*>(a.g.win + i0));
-            const float4 wb = __ldg(reinterpret_cast<const float4*>(a.g.win + i0 + 2));
             const float wre[4] = {wa.x, wa.z, wb.x, wb.z}, wim[4] = {wa.y, wa.w, wb.y, wb.w};
             const int64_t a0 = quad * kPerCta;
 #pragma unroll 1
