@@ -384,6 +384,9 @@ struct WgradGeom {
     int xpix;            // staged input pixels per channel group (Q + 2 Wp + 2, rounded up to 8)
     int nbuf;            // staged blocks: 2 (tile j + 1 stages while tile j's MMAs run), or 1 for wide rows
     int vec4;            // dy rows load as float4 (W a multiple of 4)
+    int fold;            // C <= 8: the three column taps are one MMA (N = 32: copies of the block shifted by
+                         // tx = 0, 1, 2 pixels as channel groups 0-2, group 3 zero): 3 MMAs a K step, not 9
+    int acc_cols;        // TMEM columns of the accumulators (9 N, or 3 x 32 folded)
     int tiles_img;
     int64_t n_units;
     uint32_t xbytes, stage, smem;
@@ -438,7 +441,7 @@ __global__ void __launch_bounds__(kWThreads, 1)
     tc_fence_after();
     const uint32_t tmem = S.tmem;
     // BF16 A (K-major) and B (MN-major: bit 16)
-    const uint32_t idesc = mma_idesc_f16(128, g.N) | kIdescBf16 | (1u << 16);
+    const uint32_t idesc = mma_idesc_f16(128, g.fold ? 32 : g.N) | kIdescBf16 | (1u << 16);
     const uint32_t lbo_a = static_cast<uint32_t>(kp) * 16;      // next 8-pixel chunk of dy
     // B is MN-major without swizzle: there the descriptor's leading offset is
     // the step along K (the next 8 pixels, 128 bytes on) and the stride offset
@@ -446,6 +449,11 @@ __global__ void __launch_bounds__(kWThreads, 1)
     const uint32_t sbo_b = static_cast<uint32_t>(g.xpix) * 16;
     const int ksteps = g.Q / 16;
     const int qw = g.Wp / 4;                       // half chunks (4 pixels) a staged row
+    if (g.fold && warp > 0)                        // channel group 3 of every stage stays zero
+        for (int i = st; i < g.nbuf * g.xpix; i += kWStage) {
+            const int bb = i / g.xpix, p = i - bb * g.xpix;
+            *reinterpret_cast<uint4*>(base + bb * g.stage + (3u * g.xpix + p) * 16u) = make_uint4(0, 0, 0, 0);
+        }
     const int dtasks = g.Q / 4 * kp;               // (output channel, half chunk) pairs
 
     uint32_t j = 0;
@@ -467,6 +475,33 @@ __global__ void __launch_bounds__(kWThreads, 1)
             // outside the image, past each row's W + 1 columns and past the R + 2
             // staged rows.  Two channel groups (16 loads) in flight per pass.
             const float* xi = x + static_cast<int64_t>(img) * g.C * hw;
+            if (g.fold) {
+                // C <= 8: pixel i of the block goes to copy tx at pixel i - tx
+                for (int i0 = st; i0 < g.xpix; i0 += 2 * kWStage) {
+                    float v[2][8];
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const int i = i0 + h * kWStage;
+                        const int r = i / g.Wp, cc = i - r * g.Wp;
+                        const int iy = y0 - 1 + r, ix = cc - 1;
+                        const bool in = i < g.xpix && r < g.R + 2 && iy >= 0 && iy < g.H && ix >= 0 && ix < g.W;
+                        const float* px = xi + (in ? static_cast<int64_t>(iy) * g.W + ix : 0);
+#pragma unroll
+                        for (int e = 0; e < 8; ++e) v[h][e] = (in && e < g.C) ? __ldg(px + static_cast<int64_t>(e) * hw) : 0.f;
+                    }
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const int i = i0 + h * kWStage;
+                        if (i >= g.xpix) continue;
+                        const uint4 q = make_uint4(pack_bf2(v[h][0], v[h][1]), pack_bf2(v[h][2], v[h][3]),
+                                                   pack_bf2(v[h][4], v[h][5]), pack_bf2(v[h][6], v[h][7]));
+#pragma unroll
+                        for (int tx = 0; tx < 3; ++tx)
+                            if (i - tx >= 0)
+                                *reinterpret_cast<uint4*>(Xs + (static_cast<uint32_t>(tx) * g.xpix + i - tx) * 16u) = q;
+                    }
+                }
+            } else
             for (int i0 = st; i0 < g.xpix; i0 += 2 * kWStage) {
                 // two pixels a pass, each with two channel groups: 32 loads in flight
                 const float* px[2];
@@ -557,11 +592,19 @@ __global__ void __launch_bounds__(kWThreads, 1)
                 // descriptor addresses are in 16-byte units: one unit per staged pixel of x
                 const uint64_t dbk = db0 + static_cast<uint64_t>(16 * ks);
                 const uint32_t acc = (j > 0 || ks > 0) ? 1u : 0u;
+                if (g.fold) {
+                    // one MMA per row tap: N = the three column taps x 8 channels (+ the zero group)
 #pragma unroll
-                for (int tap = 0; tap < 9; ++tap) {
-                    const int ty = tap / 3, tx = tap - 3 * ty;
-                    mma_f16_id(tmem + static_cast<uint32_t>(tap * g.N), da,
-                               dbk + static_cast<uint64_t>(ty * g.Wp + tx), idesc, acc);
+                    for (int ty = 0; ty < 3; ++ty)
+                        mma_f16_id(tmem + static_cast<uint32_t>(32 * ty), da, dbk + static_cast<uint64_t>(ty * g.Wp),
+                                   idesc, acc);
+                } else {
+#pragma unroll
+                    for (int tap = 0; tap < 9; ++tap) {
+                        const int ty = tap / 3, tx = tap - 3 * ty;
+                        mma_f16_id(tmem + static_cast<uint32_t>(tap * g.N), da,
+                                   dbk + static_cast<uint64_t>(ty * g.Wp + tx), idesc, acc);
+                    }
                 }
             }
             mma_commit(&S.x[b]);
@@ -581,7 +624,7 @@ __global__ void __launch_bounds__(kWThreads, 1)
         // chunks w / 4, w / 4 + 4, ...; column t * N + c is tap t of channel c
         const int quarter = warp & 3;
         const int k = 32 * quarter + lane;
-        const int cols = 9 * g.N;
+        const int cols = g.acc_cols;
         const int64_t kc9 = static_cast<int64_t>(g.K) * g.C * 9;
         if (32 * quarter < g.K) {
             for (int ch = warp >> 2; 32 * ch < cols; ch += kWThreads / 128) {
@@ -592,8 +635,16 @@ __global__ void __launch_bounds__(kWThreads, 1)
 #pragma unroll
                     for (int i = 0; i < 32; ++i) {
                         const int col = 32 * ch + i;
-                        const int t = col / g.N, c = col - t * g.N;
-                        if (col < cols && c < g.C) pk[c * 9 + t] = v[i];
+                        int t, c;
+                        if (g.fold) {              // column 32 ty + 8 tx + c
+                            const int tx = (col & 31) >> 3;
+                            t = tx < 3 ? 3 * (col >> 5) + tx : -1;
+                            c = col & 7;
+                        } else {
+                            t = col / g.N;
+                            c = col - t * g.N;
+                        }
+                        if (col < cols && t >= 0 && c < g.C) pk[c * 9 + t] = v[i];
                     }
                 }
             }
@@ -632,6 +683,8 @@ bool wgrad_geom(int n, int cin, int cout, int H, int W, WgradGeom& g) {
     g.kg = (cout + 7) / 8;
     g.Wp = (W + 2 + 3) / 4 * 4;
     g.vec4 = W % 4 == 0 ? 1 : 0;
+    g.fold = cin <= 8 ? 1 : 0;
+    const int xgroups = g.fold ? 4 : g.cg;          // staged channel groups of x
     const uint32_t budget = 227u * 1024u;
     g.R = 0;
     for (int nbuf = 2; nbuf >= 1 && g.R == 0; --nbuf) {
@@ -639,7 +692,7 @@ bool wgrad_geom(int n, int cin, int cout, int H, int W, WgradGeom& g) {
             if (H % R != 0) continue;
             const int Q = (R * g.Wp + 31) / 32 * 32;
             const int xpix = (Q + 2 * g.Wp + 2 + 7) / 8 * 8;
-            const uint32_t xbytes = static_cast<uint32_t>(g.cg) * xpix * 16u;
+            const uint32_t xbytes = static_cast<uint32_t>(xgroups) * xpix * 16u;
             const uint32_t dbytes = static_cast<uint32_t>(Q / 8) * 8u * g.kg * 16u;
             const uint32_t stage = (xbytes + dbytes + 127u) & ~127u;
             // the stages, 2 KB past the last one for the unused A rows, 1 KB alignment
@@ -658,13 +711,13 @@ bool wgrad_geom(int n, int cin, int cout, int H, int W, WgradGeom& g) {
     if (g.R == 0) return false;
     g.tiles_img = H / g.R;
     g.n_units = static_cast<int64_t>(n) * g.tiles_img;
-    const int cols = 9 * g.N;
-    g.tmem_cols = cols <= 256 ? 256 : 512;
-    return cols <= 512;
+    g.acc_cols = g.fold ? 3 * 32 : 9 * g.N;
+    g.tmem_cols = g.acc_cols <= 128 ? 128 : (g.acc_cols <= 256 ? 256 : 512);
+    return g.acc_cols <= 512;
 }
 
 int wgrad_grid(const WgradGeom& g, int num_sms) {
-    const int per_sm = g.tmem_cols == 512 || g.smem > 113u * 1024u ? 1 : 2;
+    const int per_sm = g.tmem_cols == 512 || g.smem > 113u * 1024u ? 1 : 2;   // TMEM and shared memory allow
     const int64_t slots = static_cast<int64_t>(per_sm) * num_sms;
     return static_cast<int>(g.n_units < slots ? g.n_units : slots);
 }
