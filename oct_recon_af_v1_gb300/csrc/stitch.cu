@@ -310,39 +310,47 @@ __global__ void __launch_bounds__(kStThreads) k_stitch_frames(const StitchDev* _
         const float4 cp = colp[k * kBlk + tx];
         const int x0 = __float_as_int(cp.x);
         if (x0 < 0) continue;
-        const StitchSlot s = slot[k];
-        const float* pa = sm + s.off;
-        const float* pf = pa + (s.xs + 1) * s.rst;
-        const bool opc = s.opc != 0;
+        const int rst = slot[k].rst;
+        // this thread's first A-scan of the patch, rows indexed by zr directly
+        const float* pa = sm + slot[k].off + x0 * rst - slot[k].r_lo;
         const float wx0 = cp.y, wx1 = cp.z;
+        const float4* rpk = rowp + k * kFZ + ty;
+        const float2* rfk = rowf + k * kFZ + ty;
+        if (slot[k].opc == 0) {
+            // F depends on the row only: its two taps and the den term per row
 #pragma unroll
-        for (int q = 0; q < kFRows; ++q) {
-            const int z = ty + 8 * q;
-            const float4 rp = rowp[k * kFZ + z];
-            const int zr = __float_as_int(rp.x);
-            if (zr < 0) continue;
-            const int o = x0 * s.rst + zr - s.r_lo;
-            const float w0 = rp.y, w1 = rp.z;
-            float f00, f01, f10, f11, d0, d1;
-            if (opc) {
-                f00 = pf[o];
-                f01 = pf[o + 1];
-                f10 = pf[o + s.rst];
-                f11 = pf[o + s.rst + 1];
-                d0 = fmaf(f01, w1, f00 * w0);
-                d1 = fmaf(f11, w1, f10 * w0);
-            } else {
-                const float2 ff = rowf[k * kFZ + z];
-                f00 = f10 = ff.x;
-                f01 = f11 = ff.y;
-                d0 = d1 = rp.w;
+            for (int q = 0; q < kFRows; ++q) {
+                const float4 rp = rpk[8 * q];
+                const int zr = __float_as_int(rp.x);
+                if (zr < 0) continue;
+                const float* p0 = pa + zr;
+                const float* p1 = p0 + rst;
+                const float w0 = rp.y, w1 = rp.z, d = rp.w;
+                const float2 ff = rfk[8 * q];
+                // a = magnitude * F (TileStitcher.contribute, stitching.py:136)
+                const float a00 = p0[0] * ff.x, a01 = p0[1] * ff.y;
+                const float a10 = p1[0] * ff.x, a11 = p1[1] * ff.y;
+                const float u0 = fmaf(a01, w1, a00 * w0), u1 = fmaf(a11, w1, a10 * w0);
+                an[q] += fmaf(u1, wx1, u0 * wx0);
+                ad[q] += fmaf(d, wx1, d * wx0);
             }
-            // a = magnitude * F (TileStitcher.contribute, stitching.py:136)
-            const float a00 = pa[o] * f00, a01 = pa[o + 1] * f01;
-            const float a10 = pa[o + s.rst] * f10, a11 = pa[o + s.rst + 1] * f11;
-            const float u0 = fmaf(a01, w1, a00 * w0), u1 = fmaf(a11, w1, a10 * w0);
-            an[q] += fmaf(u1, wx1, u0 * wx0);
-            ad[q] += fmaf(d1, wx1, d0 * wx0);
+        } else {
+            // optical-path correction: F per A-scan and row, its patch after the magnitudes
+            const float* pf = pa + (slot[k].xs + 1) * rst;
+#pragma unroll
+            for (int q = 0; q < kFRows; ++q) {
+                const float4 rp = rpk[8 * q];
+                const int zr = __float_as_int(rp.x);
+                if (zr < 0) continue;
+                const float w0 = rp.y, w1 = rp.z;
+                const float f00 = pf[zr], f01 = pf[zr + 1], f10 = pf[zr + rst], f11 = pf[zr + rst + 1];
+                const float d0 = fmaf(f01, w1, f00 * w0), d1 = fmaf(f11, w1, f10 * w0);
+                const float a00 = pa[zr] * f00, a01 = pa[zr + 1] * f01;
+                const float a10 = pa[zr + rst] * f10, a11 = pa[zr + rst + 1] * f11;
+                const float u0 = fmaf(a01, w1, a00 * w0), u1 = fmaf(a11, w1, a10 * w0);
+                an[q] += fmaf(u1, wx1, u0 * wx0);
+                ad[q] += fmaf(d1, wx1, d0 * wx0);
+            }
         }
     }
 
