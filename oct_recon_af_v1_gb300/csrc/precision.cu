@@ -465,8 +465,31 @@ __global__ void __launch_bounds__(256) k_prec_rowsum(const SpectralArgs a, const
         const int64_t b = as / a.nx, x = as - b * a.nx;
         const RawT* row = static_cast<const RawT*>(a.raw) + (b * a.interf + a.apod + x) * kN;
         const int* Sb = apod_sum + b * kN;
+        // eight samples a 16-byte load when the row is aligned (kN * 2 bytes a
+        // row: rows are aligned when the buffer is); with apod < 256 a lane's
+        // 64 terms, |apod raw - S| < 2^24 each, sum exactly in 32 bits
         long long s = 0;
-        for (int j = lane; j < kN; j += 32) s += a.apod * static_cast<int>(row[j]) - Sb[j];
+        if ((reinterpret_cast<uintptr_t>(row) & 15u) == 0 && a.apod < 256) {
+            int sl = 0;
+            const uint4* r4 = reinterpret_cast<const uint4*>(row);
+            const int4* s4 = reinterpret_cast<const int4*>(Sb);
+            for (int c = lane; c < kN / 8; c += 32) {
+                const uint4 rv = __ldg(r4 + c);
+                const int4 sa = __ldg(s4 + 2 * c), sb = __ldg(s4 + 2 * c + 1);
+                const uint32_t w[4] = {rv.x, rv.y, rv.z, rv.w};
+                const int sv[8] = {sa.x, sa.y, sa.z, sa.w, sb.x, sb.y, sb.z, sb.w};
+#pragma unroll
+                for (int e = 0; e < 8; ++e) {
+                    const uint32_t u = (w[e >> 1] >> (16 * (e & 1))) & 0xffffu;
+                    const int rawv = static_cast<RawT>(-1) < 0 ? static_cast<int>(static_cast<int16_t>(u))
+                                                               : static_cast<int>(u);
+                    sl += a.apod * rawv - sv[e];
+                }
+            }
+            s = sl;
+        } else {
+            for (int j = lane; j < kN; j += 32) s += a.apod * static_cast<int>(row[j]) - Sb[j];
+        }
         for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
         if (lane == 0) {
             sum_n[as] = s;
