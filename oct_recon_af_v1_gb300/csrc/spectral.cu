@@ -370,9 +370,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
                 // modular window order: step u reads the window sample congruent
                 // to u (mod U); the weights are stored in the same order
                 const float* dk = S.d[k] + wbase;
+                const float* dkh = dk + U;                // samples before s0 wrap to the next period
                 float win[U];
 #pragma unroll
-                for (int u = 0; u < U; ++u) win[u] = dk[u < wrot ? u + U : u];
+                for (int u = 0; u < U; ++u) win[u] = (u < wrot ? dkh : dk)[u];
                 float lh[4], lx[4];
                 bool lsafe[4];
 #pragma unroll
