@@ -188,7 +188,7 @@ class Volume:
         return sum(int(t.numel()) * 2 for t in self.raw.values())
 
 
-def run_step(ctx, vol, src, db_vol, bits, batch=9):
+def run_step(ctx, vol, src, db_vol, bits, batch=54):
     """One whole-volume reconstruction through the frame-batch API: for each
     y-row and each batch of `batch` frames, every tile's spectral stage and
     the stitched, finalised planes (num/den never leave the chip; the
@@ -1319,7 +1319,8 @@ def main():
     ap.add_argument("--test4", type=int, default=500, help="held-out B-scans of the learned estimator (config 4)")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--ref-frames", type=int, default=4)
-    ap.add_argument("--batch", type=int, default=9, help="frames per frame batch")
+    ap.add_argument("--batch", type=int, default=54,
+                    help="frames per frame-API call (config 1: 54 of the 270 B-scans; 9, 27, 54, 90 measured)")
     ap.add_argument("--bscans", type=int, default=270, help="B-scans per tile (270 = the full workload)")
     ap.add_argument("--no-graph", action="store_true")
     args = ap.parse_args()
