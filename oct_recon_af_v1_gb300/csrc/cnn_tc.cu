@@ -37,7 +37,7 @@ namespace {
 
 constexpr int kCM = 128;                    // output pixels per tile (MMA M)
 constexpr int kCThreads = 128;              // four warps = the 128 TMEM lanes
-constexpr int kCSlots = 4;                  // staged pixels per thread (a staged block holds <= 512)
+constexpr int kCSlots = 5;                  // staged pixels per thread (a staged block holds <= 640)
 
 struct ConvGeom {
     int n, cin, cout, H, W;
@@ -47,7 +47,8 @@ struct ConvGeom {
     int halo;          // 1: one staged copy with halo columns (W >= 128); 0: three shifted copies
     int cols_s;        // staged pixels per row
     int pix_c;         // staged pixels per chunk (one copy)
-    int nbuf;          // staged buffers (2: the next tile stages while the MMAs read the other)
+    int nbuf;          // staged buffers (2: the next block stages while the MMAs read the other)
+    int sh;            // tiles per staged block: 2 = a pooled pair's rows and halo read once, else 1
     int pool;          // 1: ReLU + 2x2 mean fused into the epilogue (units = vertical tile pairs)
     int tiles_img;     // tiles per image
     int64_t n_units;   // tiles, or tile pairs with pool
@@ -230,7 +231,7 @@ __global__ void __launch_bounds__(kCThreads, 4)
         tc_fence_before();
     };
 
-    uint32_t j = 0;            // tiles staged by this CTA so far
+    uint32_t j = 0;            // blocks staged by this CTA so far
     uint32_t ju = 0;           // units so far (accumulator set ju & 1)
     bool have_prev = false;
     int prev_img = 0, prev_y0 = 0, prev_x0 = 0;  // origin of the previous unit
@@ -239,16 +240,18 @@ __global__ void __launch_bounds__(kCThreads, 4)
         const int ab = static_cast<int>(ju & 1);
         int img, y0u, x0;
         unit_tile(g, u, 0, img, y0u, x0);
-        for (int h = 0; h < U && ok; ++h, ++j) {
-            // nbuf is 1 or 2: the buffer and the parity of its previous use
+        for (int h0 = 0; h0 < U && ok; h0 += g.sh, ++j) {
+            // one staged block per sh tiles (sh = 2: a pooled pair's rows and
+            // their halo read once); nbuf is 1 or 2: the buffer and the parity
+            // of its previous use
             const int b = g.nbuf == 2 ? static_cast<int>(j & 1u) : 0;
             if (j >= static_cast<uint32_t>(g.nbuf)) {
-                // the MMAs of the tile staged nbuf tiles ago have read X[b]
+                // the MMAs of the block staged nbuf blocks ago have read X[b]
                 const uint32_t use = g.nbuf == 2 ? (j - 2) >> 1 : j - 1;
                 ok = conv_wait(&S.x[b], use & 1u, S, status);
                 if (!ok) break;
             }
-            const int y0 = y0u + h;
+            const int y0 = y0u + h0;
             uint4* X = reinterpret_cast<uint4*>(base + b * g.xbytes);
             const float* xi = x + static_cast<int64_t>(img) * g.cin * hw;
             int off[kCSlots];
@@ -299,20 +302,24 @@ __global__ void __launch_bounds__(kCThreads, 4)
                 tc_fence_after();
                 const uint8_t* Xb = base + b * g.xbytes;
                 const uint32_t lbo = static_cast<uint32_t>(g.pix_c) * 16;
-                const uint32_t d_tmem = tmem + static_cast<uint32_t>((ab * U + h) * g.cout);
-                for (int tap = 0; tap < 9; ++tap) {
-                    const int dy = tap / 3, dx = tap - 3 * dy;
-                    const uint8_t* a0 = g.halo ? Xb + (dy * g.cols_s + dx) * 16
-                                               : Xb + static_cast<uint32_t>(dx * g.cin8) * lbo + dy * g.W * 16;
-                    for (int ks = 0; ks < g.cin8 / 2; ++ks) {
-                        const uint64_t da = smem_desc(a0 + 2 * ks * lbo, lbo, 128);
-                        const uint64_t db = smem_desc(B + static_cast<uint32_t>(tap * g.cin8 + 2 * ks) * b_chunk,
-                                                      b_chunk, 128);
-                        mma_f16_id(d_tmem, da, db, idesc, (tap > 0 || ks > 0) ? 1u : 0u);
+                for (int h = h0; h < h0 + g.sh; ++h) {
+                    // tile h of the unit: its rows start (h - h0) tile heights down the staged block
+                    const uint32_t d_tmem = tmem + static_cast<uint32_t>((ab * U + h) * g.cout);
+                    const uint8_t* Xh = Xb + static_cast<uint32_t>((h - h0) * g.rows * g.cols_s) * 16u;
+                    for (int tap = 0; tap < 9; ++tap) {
+                        const int dy = tap / 3, dx = tap - 3 * dy;
+                        const uint8_t* a0 = g.halo ? Xh + (dy * g.cols_s + dx) * 16
+                                                   : Xh + static_cast<uint32_t>(dx * g.cin8) * lbo + dy * g.W * 16;
+                        for (int ks = 0; ks < g.cin8 / 2; ++ks) {
+                            const uint64_t da = smem_desc(a0 + 2 * ks * lbo, lbo, 128);
+                            const uint64_t db = smem_desc(B + static_cast<uint32_t>(tap * g.cin8 + 2 * ks) * b_chunk,
+                                                          b_chunk, 128);
+                            mma_f16_id(d_tmem, da, db, idesc, (tap > 0 || ks > 0) ? 1u : 0u);
+                        }
                     }
                 }
                 mma_commit(&S.x[b]);
-                if (h == U - 1) mma_commit(&S.d[ab]);
+                if (h0 + g.sh == U) mma_commit(&S.d[ab]);
             }
         }
         if (!ok) break;
@@ -749,37 +756,49 @@ cudaError_t launch_conv3x3_tc(const float* x, const float* w, const float* b, fl
     g.wseg = W >= kCM ? kCM : W;
     g.rows = kCM / g.wseg;
     g.cols_s = g.halo ? g.wseg + 2 : g.wseg;
-    g.pix_c = (g.rows + 2) * g.cols_s;
     g.nbuf = g.halo ? 2 : 1;
     g.pool = pool ? 1 : 0;
     g.tiles_img = static_cast<int>(static_cast<int64_t>(H) * W / kCM);
     g.n_units = static_cast<int64_t>(n) * g.tiles_img / (pool ? 2 : 1);
-    g.xbytes = static_cast<uint32_t>((g.halo ? 1 : 3) * g.cin8 * g.pix_c) * 16u;
-    g.xbytes = (g.xbytes + 127u) & ~127u;
-    g.off_b = static_cast<uint32_t>(g.nbuf) * g.xbytes;
-    g.smem = g.off_b + 9u * static_cast<uint32_t>(g.cin8) * static_cast<uint32_t>(cout) * 16u + 1024u;
     const int cols = 2 * (pool ? 2 : 1) * cout;                   // two units of accumulators
     g.tmem_cols = cols <= 32 ? 32 : (cols <= 64 ? 64 : (cols <= 128 ? 128 : (cols <= 256 ? 256 : 512)));
     if (g.n_units == 0) return cudaSuccess;
-    if (g.smem > 227u * 1024u || g.pix_c > kCSlots * kCThreads) return cudaErrorInvalidValue;
     auto kern = bf16 ? k_conv3x3_tc<true> : k_conv3x3_tc<false>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(g.smem));
-    if (e != cudaSuccess) return e;
-    // CTAs per SM: shared memory, registers and TMEM columns
     int dev = 0, sms = 0, smem_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
     cudaFuncAttributes fa{};
-    e = cudaFuncGetAttributes(&fa, kern);
+    cudaError_t e = cudaFuncGetAttributes(&fa, kern);
     if (e != cudaSuccess) return e;
-    const int by_smem = smem_sm / static_cast<int>(g.smem + fa.sharedSizeBytes + 1024);
-    const int regs = (fa.numRegs + 7) / 8 * 8;
-    const int by_regs = 65536 / (regs * kCThreads);
-    const int by_tmem = 512 / g.tmem_cols;
-    int per_sm = by_smem < by_regs ? by_smem : by_regs;
-    per_sm = per_sm < by_tmem ? per_sm : by_tmem;
-    per_sm = per_sm < 1 ? 1 : per_sm;
+    // staged layout for sh tiles per block, and the CTAs per SM it allows
+    // (shared memory, registers, TMEM columns)
+    auto layout = [&](int sh) -> int {
+        g.sh = sh;
+        g.pix_c = (sh * g.rows + 2) * g.cols_s;
+        g.xbytes = static_cast<uint32_t>((g.halo ? 1 : 3) * g.cin8 * g.pix_c) * 16u;
+        g.xbytes = (g.xbytes + 127u) & ~127u;
+        g.off_b = static_cast<uint32_t>(g.nbuf) * g.xbytes;
+        g.smem = g.off_b + 9u * static_cast<uint32_t>(g.cin8) * static_cast<uint32_t>(cout) * 16u + 1024u;
+        if (g.smem > 227u * 1024u || g.pix_c > kCSlots * kCThreads) return 0;
+        const int by_smem = smem_sm / static_cast<int>(g.smem + fa.sharedSizeBytes + 1024);
+        const int regs = (fa.numRegs + 7) / 8 * 8;
+        const int by_regs = 65536 / (regs * kCThreads);
+        const int by_tmem = 512 / g.tmem_cols;
+        int ps = by_smem < by_regs ? by_smem : by_regs;
+        ps = ps < by_tmem ? ps : by_tmem;
+        return ps;
+    };
+    // a pooled pair staged once (its halo rows read once) unless that costs CTAs per SM
+    int per_sm = layout(1);
+    if (g.pool && g.halo) {
+        const int ps2 = layout(2);
+        if (ps2 < per_sm || ps2 == 0) per_sm = layout(1);
+        else per_sm = ps2;
+    }
+    if (per_sm == 0) return cudaErrorInvalidValue;
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(g.smem));
+    if (e != cudaSuccess) return e;
     const int64_t slots = static_cast<int64_t>(per_sm) * sms;
     const int64_t grid = g.n_units < slots ? g.n_units : slots;
     kern<<<static_cast<unsigned int>(grid), kCThreads, g.smem, st>>>(x, w, b, y, g, status);
