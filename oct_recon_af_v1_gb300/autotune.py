@@ -30,9 +30,25 @@ def ordered(tiles, order: str):
     return list(tiles)
 
 
-def tune_batch(ctx, tiles, threshold: float, stream, reps: int = 2, grabs=GRABS, orders=ORDERS):
-    """Return (grab, order, table of timings in ms) for this batch."""
-    import torch
+def cuda_timer(stream):
+    """time(fn, reps) -> ms per call of fn, CUDA events on `stream` after a synchronize."""
+    def time(fn, reps):
+        import torch
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+    return time
+
+
+def tune_batch(ctx, tiles, threshold: float, stream, reps: int = 2, grabs=GRABS, orders=ORDERS, timer=None):
+    """Return (grab, order, table of timings in ms) for this batch.  `timer`
+    (default: CUDA events on `stream`) is time(fn, reps) -> ms per call."""
+    time = timer or cuda_timer(stream)
     sig = signature(tiles)
     if sig in _CACHE:
         return _CACHE[sig]
@@ -41,14 +57,7 @@ def tune_batch(ctx, tiles, threshold: float, stream, reps: int = 2, grabs=GRABS,
         work = ordered(tiles, order)
         for grab in grabs:
             ctx.batch_process(work, threshold, grab=grab)          # warm (tile table upload, caches)
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            torch.cuda.synchronize()
-            e0.record(stream)
-            for _ in range(reps):
-                ctx.batch_process(work, threshold, grab=grab)
-            e1.record(stream)
-            torch.cuda.synchronize()
-            timings[(grab, order)] = e0.elapsed_time(e1) / reps
+            timings[(grab, order)] = time(lambda: ctx.batch_process(work, threshold, grab=grab), reps)
     best = min(timings, key=timings.get)
     _CACHE[sig] = (best[0], best[1], {f"{g}/{o}": round(t, 3) for (g, o), t in timings.items()})
     return _CACHE[sig]
@@ -57,15 +66,16 @@ def tune_batch(ctx, tiles, threshold: float, stream, reps: int = 2, grabs=GRABS,
 STITCH_ROWS = (32, 64, 128)
 
 
-def tune_stitch_rows(ctx, step, stream, key, reps: int = 3, rows=STITCH_ROWS):
+def tune_stitch_rows(ctx, step, stream, key, reps: int = 3, rows=STITCH_ROWS, timer=None):
     """Output rows per stitch block of octgb_frames_process (its tile shape:
     32, 64 or 128 rows x 32 columns).  `step` runs one whole workload through
     the frame API (not under graph capture); each candidate is run once to
     build its slot tables, then timed over `reps` runs with CUDA events on the
     launching stream.  Every voxel sums its tiles in the same order for every
     shape, so the choice changes the time only.  Leaves the fastest set on the
-    context and returns (rows, {rows: ms}); cached per `key`."""
-    import torch
+    context and returns (rows, {rows: ms}); cached per `key`.  `timer`
+    (default: CUDA events on `stream`) is time(fn, reps) -> ms per call."""
+    time = timer or cuda_timer(stream)
     if key in _CACHE:
         best, table = _CACHE[key]
         ctx.set_stitch_rows(best)
@@ -77,14 +87,9 @@ def tune_stitch_rows(ctx, step, stream, key, reps: int = 3, rows=STITCH_ROWS):
             step()
         except Exception:                                   # a shape whose patches exceed shared memory
             continue
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        torch.cuda.synchronize()
-        e0.record(stream)
-        for _ in range(reps):
-            step()
-        e1.record(stream)
-        torch.cuda.synchronize()
-        table[r] = round(e0.elapsed_time(e1) / reps, 3)
+        table[r] = round(time(step, reps), 3)
+    if not table:
+        raise RuntimeError("no stitch tile shape runs on this workload")
     best = min(table, key=table.get)
     ctx.set_stitch_rows(best)
     _CACHE[key] = (best, table)
