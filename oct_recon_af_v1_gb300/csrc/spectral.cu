@@ -68,7 +68,11 @@ constexpr int kDLine = kN + kTail;                        // d line incl. zero t
 // 2^-40 |o| from a float32 rounding boundary (r = (p + q) - o exactly, by
 // Fast2Sum), both the product and its float64 rounding round to o.  Otherwise
 // (about one sample in 65 000), and for powers of two (asymmetric boundaries)
-// and tiny values, the float64 product is formed as the reference does.
+// and tiny values, the float64 product is formed as the reference does.  A
+// window value of exactly zero (the Hann window's end points) gives the exact
+// product x * 0 (signed zero, or NaN) in both forms and needs no float64 step:
+// without this case the two warps holding the end points took the float64 path
+// for every A-scan.
 // The caller forms the float64 product for the lanes whose `safe` is false,
 // behind a warp vote, so the FP64 pipe only runs in the rare warps that need it.
 __device__ __forceinline__ float mul_window(float x, float2 h2, bool& safe) {
@@ -80,8 +84,10 @@ __device__ __forceinline__ float mul_window(float x, float2 h2, bool& safe) {
     const float ao = fabsf(o);
     const int bits = __float_as_int(ao);
     const float half_ulp = __int_as_float((bits & 0x7f800000) - (24 << 23));
-    safe = ao > 1e-30f && (bits & 0x007fffff) != 0 && fabsf(fabsf(r) - half_ulp) > ao * 9.094947e-13f;
-    return o;
+    const bool zero_h = h2.x == 0.f && h2.y == 0.f;
+    safe = zero_h || (ao > 1e-30f && (bits & 0x007fffff) != 0 && fabsf(fabsf(r) - half_ulp) > ao * 9.094947e-13f);
+    // x * 0 keeps x's sign, as the float64 product does (p + q would give +0)
+    return zero_h ? p : o;
 }
 
 // Where slot s of quad q reads its raw row and apodisation row and writes
