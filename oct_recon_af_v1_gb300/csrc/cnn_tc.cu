@@ -1,7 +1,12 @@
-// Tensor-core 3x3 convolution of the learned estimator (the inference form of
-// cnn.cu's k_conv3x3): stride 1, zero padding 1, + bias, NCHW float32 in and
-// out, FP16 operands and float32 accumulation on the 5th-generation tensor
-// cores (tcgen05.mma kind::f16, accumulator in TMEM).
+// Tensor-core kernels of the learned estimator.
+//
+// k_conv3x3_tc: the 3x3 convolution (cnn.cu's k_conv3x3 on the tensor cores):
+// stride 1, zero padding 1, + bias, NCHW float32 in and out, FP16 operands
+// (BF16 for the data gradient) and float32 accumulation on the 5th-generation
+// tensor cores (tcgen05.mma kind::f16, accumulator in TMEM).  Forward pass of
+// training and inference, and the data gradient (the convolution of dy with
+// the flipped kernel).  k_conv3x3_wgrad_tc (further down): the weight
+// gradient.
 //
 // Implicit GEMM without an im2col copy: M = 128 output pixels of one image (a
 // row segment when the width W >= 128, else 128 / W whole rows), N = the
@@ -21,7 +26,10 @@
 // and the accumulator (2 x N TMEM columns) are double-buffered, so tile j's
 // MMAs run while the CTA writes tile j - 1's pre-activations (every warp its
 // 32 TMEM lanes = pixels, + bias, coalesced along x) and stages tile j + 1.
-// Persistent over tiles.  Every mbarrier wait is bounded; on expiry the CTA
+// With ReLU + 2x2 mean fused (W >= 128) a unit is a vertical pair of tiles;
+// where the CTAs per SM allow, the pair's four input rows are staged as one
+// block (its halo rows read once) and the second tile's MMAs read it one row
+// down.  Persistent over units.  Every mbarrier wait is bounded; on expiry the CTA
 // records the status, waits (bounded) for its MMAs, frees its TMEM and
 // returns.
 #include <cuda_bf16.h>
