@@ -4,7 +4,9 @@
 // loop.  Per A-scan (2048 samples):
 //   (a) the raw row (4 KiB of uint16) is staged into shared memory by a bulk
 //       TMA copy (cp.async.bulk, mbarrier completion), double-buffered so the
-//       next quad's rows stream in while the current quad is computed;
+//       next quad's rows stream in while the current quad is computed; lanes
+//       0-3 of warp 0 resolve the quad's four rows (32-bit index arithmetic),
+//       issue their copies and leave the slots in shared memory for the CTA;
 //   (b) d[j] = float(raw[j]) - apod[j] (float32 apodisation mean of the
 //       B-scan, rounded from an exact sum as core/cpu_kernels.py:20-25 does),
 //       line mean m removed before d reaches shared memory (cpu_kernels.py:
