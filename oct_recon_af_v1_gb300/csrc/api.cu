@@ -61,7 +61,7 @@ struct Plan {
     std::vector<int2> zblk_h, cblk_h;   // host copies of the block tables
     bool lateral_identity = false;      // WxT is the identity (single-tile output grid)
     bool lateral_quad_local = false;    // every non-zero lateral weight stays inside the column's B-scan quad
-    DevBuf zr, wz0, wz1, xr, wx0, wx1, fz, shift, lo, hi, zblk, cblk, zrow, zf;
+    DevBuf zr, wz0, wz1, xr, wx0, wx1, fz, shift, lo, hi, zblk, cblk, zrow, zf, xcol;
     bool opc = false;
     StitchDev dev() const {
         StitchDev d;
@@ -79,6 +79,7 @@ struct Plan {
         d.cblk = cblk.as<int2>();
         d.zrow = zrow.as<float4>();
         d.zf = zf.as<float2>();
+        d.xcol = xcol.as<float4>();
         d.cblk_first = cblk_first;
         d.n_cblk = n_cblk;
         d.r0 = r0;
@@ -91,7 +92,7 @@ struct Plan {
         return d;
     }
     void release() {
-        for (DevBuf* b : {&zr, &wz0, &wz1, &xr, &wx0, &wx1, &fz, &shift, &lo, &hi, &zblk, &cblk, &zrow, &zf})
+        for (DevBuf* b : {&zr, &wz0, &wz1, &xr, &wx0, &wx1, &fz, &shift, &lo, &hi, &zblk, &cblk, &zrow, &zf, &xcol})
             b->release();
     }
 };
@@ -930,6 +931,14 @@ int octgb_stitch_plan(octgb_ctx* c, int n_rows, int r0, int r1, int c0, int c1, 
             }
             up(p->zrow, zrow.data(), zrow.size() * sizeof(float4));
             up(p->zf, zfv.data(), zfv.size() * sizeof(float2));
+            // per output column: {xr (int bits), wx0, wx1, 0}
+            std::vector<float4> xcol(C);
+            for (int cc = 0; cc < C; ++cc) {
+                float xrf;
+                memcpy(&xrf, &xr[cc], sizeof(float));
+                xcol[cc] = make_float4(xrf, wx0[cc], wx1[cc], 0.f);
+            }
+            up(p->xcol, xcol.data(), xcol.size() * sizeof(float4));
             if (shift != nullptr) {
                 require(n_y >= 1, "n_y must be >= 1 with optical-path correction");
                 const size_t m = static_cast<size_t>(n_y) * n_tile_x;

@@ -122,6 +122,8 @@ struct StitchDev {
     // {F0 = fz[zr], F1 = fz[zr + 1] or 0 past the window} (batched form)
     const float4* zrow;
     const float2* zf;
+    // per output column c0 + cc: {xr (int bits), wx0, wx1, 0} (frame-batch form)
+    const float4* xcol;
     int cblk_first, n_cblk;
     int r0, R, c0, C, n_out_z, n_tile_x, n_rows;
 };

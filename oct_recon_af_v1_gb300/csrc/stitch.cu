@@ -179,12 +179,39 @@ __device__ __forceinline__ void warp_minmax(float& mn, float& mx) {
     }
 }
 
-// Frame-batch kernel: one CTA = one frame x 64 output rows x 32 output
+// The fields of a tile's stitch plan that the frame-batch kernel reads,
+// copied to shared memory once per CTA (one load round for all slots).
+struct SlotPlan {
+    const float4* zrow;       // per output row {zr, wz0, wz1, d}
+    const float2* zf;         // per output row {F[zr], F[zr + 1]}
+    const float4* xcol;       // per output column {xr, wx0, wx1, 0}
+    const float* fz;
+    const int* shift;         // null without the optical-path correction
+    const int* lo;
+    const int* hi;
+    int r0, c0, C, n_out_z, n_tile_x, n_rows;
+};
+
+static_assert(sizeof(SlotPlan) % 16 == 0, "the row parameters after the slot plans need 16-byte alignment");
+
+// asynchronous global -> shared copy of one 8- or 16-byte element (both addresses aligned to its size)
+template <int kBytes>
+__device__ __forceinline__ void cp_async(void* dst, const void* src) {
+    static_assert(kBytes == 8 || kBytes == 16, "cp.async element size");
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(
+                     static_cast<uint32_t>(__cvta_generic_to_shared(dst))),
+                 "l"(src), "n"(kBytes)
+                 : "memory");
+}
+
+// Frame-batch kernel: one CTA = one frame x kFZ output rows x 32 output
 // columns.  The tiles touching each block and their patch extents come from a
-// table built once per tile list on the host (StitchSlot), so a CTA starts
-// with a few parallel loads.  All contributing patches and the tiles' row /
-// column interpolation parameters are staged in shared memory first (one
-// barrier, many loads in flight), then every voxel sums the tiles in order.
+// table built once per tile list on the host (StitchSlot); the CTA reads the
+// table and each tile's plan fields in one round of loads, then stages every
+// contributing patch and the tiles' per-row / per-column interpolation
+// parameters (precomputed per plan) in shared memory by asynchronous copies:
+// no load waits on another before the one barrier.  Then every voxel sums
+// the tiles in order.
 // kFZ output rows per CTA (the tile shape the autotuner picks: 32, 64 or 128)
 template <int kFZ>
 __global__ void __launch_bounds__(kStThreads) k_stitch_frames(const StitchDev* __restrict__ plans, const TileList tl,
@@ -196,12 +223,13 @@ __global__ void __launch_bounds__(kStThreads) k_stitch_frames(const StitchDev* _
                                                               unsigned int* __restrict__ plane_mm,
                                                               unsigned int* __restrict__ run_mm, int ns_max) {
     constexpr int kFRows = kFZ / 8;          // rows per thread
-    // dynamic shared memory: per-slot row / column parameters, then the patches
+    // dynamic shared memory: per-slot plan fields, row / column parameters, then the patches
     extern __shared__ __align__(16) float smem_all[];
     __shared__ StitchSlot slot[kMaxSeg];
-    float4* rowp = reinterpret_cast<float4*>(smem_all);           // [ns_max][kFZ] {zr, w0, w1, F interpolated}
-    float2* rowf = reinterpret_cast<float2*>(rowp + ns_max * kFZ); // [ns_max][kFZ] {F of the row's two taps}
-    float4* colp = reinterpret_cast<float4*>(rowf + ns_max * kFZ); // [ns_max][kBlk] {x0, wx0, wx1 (0 past the patch)}
+    SlotPlan* spl = reinterpret_cast<SlotPlan*>(smem_all);              // [ns_max]
+    float4* rowp = reinterpret_cast<float4*>(spl + ns_max);             // [ns_max][kFZ] {zr, w0, w1, F interpolated}
+    float2* rowf = reinterpret_cast<float2*>(rowp + ns_max * kFZ);      // [ns_max][kFZ] {F of the row's two taps}
+    float4* colp = reinterpret_cast<float4*>(rowf + ns_max * kFZ);      // [ns_max][kBlk] {xr, wx0, wx1, 0}
     float* sm = reinterpret_cast<float*>(colp + ns_max * kBlk);
     const int f = blockIdx.z;
     const int zb = blockIdx.y * kFZ;
@@ -209,7 +237,26 @@ __global__ void __launch_bounds__(kStThreads) k_stitch_frames(const StitchDev* _
     const int tid = threadIdx.x;
     const int blk = blockIdx.y * gridDim.x + blockIdx.x;
     const int ns = slot_count[blk];
-    if (tid < ns) slot[tid] = slots[static_cast<int64_t>(blk) * tl.n + tid];
+    if (tid < ns) {
+        const StitchSlot s = slots[static_cast<int64_t>(blk) * tl.n + tid];
+        const StitchDev& p = plans[tl.id[s.t]];
+        SlotPlan q;
+        q.zrow = p.zrow;
+        q.zf = p.zf;
+        q.xcol = p.xcol;
+        q.fz = p.fz;
+        q.shift = p.shift;
+        q.lo = p.lo;
+        q.hi = p.hi;
+        q.r0 = p.r0;
+        q.c0 = p.c0;
+        q.C = p.C;
+        q.n_out_z = p.n_out_z;
+        q.n_tile_x = p.n_tile_x;
+        q.n_rows = p.n_rows;
+        slot[tid] = s;
+        spl[tid] = q;
+    }
     __syncthreads();
 
     // 1. stage each contributing tile's interpolation parameters and its
@@ -219,26 +266,27 @@ __global__ void __launch_bounds__(kStThreads) k_stitch_frames(const StitchDev* _
     //    s.rst), so every 2 x 2 read below is in the patch
     for (int k = 0; k < ns; ++k) {
         const StitchSlot s = slot[k];
-        const StitchDev& p = plans[tl.id[s.t]];
+        const SlotPlan& p = spl[k];
         if (tid < kFZ) {
             // without the optical-path correction F depends on the row only:
-            // its two taps and the depth-interpolated F (the den term) per row
+            // its two taps and the depth-interpolated F (the den term) per row.
+            // The slot's rows reach zr + 1 of every row, so the per-plan F[zr + 1]
+            // (0 past the window) is the one the patch holds.
             const int zo = zb + tid;
-            const int zr = zo < p.n_out_z ? p.zr[zo] : -1;
-            const float w0 = zr >= 0 ? p.wz0[zo] : 0.f, w1 = zr >= 0 ? p.wz1[zo] : 0.f;
-            const bool has_r1 = zr >= 0 && zr - s.r_lo + 1 < s.rs;
-            const float fa = zr >= 0 ? p.fz[zr] : 0.f, fb = has_r1 ? p.fz[zr + 1] : 0.f;
-            rowp[k * kFZ + tid] = make_float4(__int_as_float(zr), w0, w1, fmaf(fb, w1, fa * w0));
-            rowf[k * kFZ + tid] = make_float2(fa, fb);
+            if (zo < p.n_out_z) {
+                cp_async<16>(rowp + k * kFZ + tid, p.zrow + zo);
+                cp_async<8>(rowf + k * kFZ + tid, p.zf + zo);
+            } else {
+                rowp[k * kFZ + tid] = make_float4(__int_as_float(-1), 0.f, 0.f, 0.f);
+                rowf[k * kFZ + tid] = make_float2(0.f, 0.f);
+            }
         } else if (tid < kFZ + kBlk) {
+            // the slot's A-scans reach xr + 1 of every column of the block
             const int cc = cb + tid - kFZ - p.c0;
-            const int xr = (cc >= 0 && cc < p.C) ? p.xr[cc] : -1;
-            const int x0 = xr - s.x_lo;
-            // the second lateral tap outside the patch contributes nothing
-            // (its column is the zero A-scan): its weight is 0 for the den term too
-            const bool has_x1 = x0 + 1 < s.xs;
-            colp[k * kBlk + tid - kFZ] = make_float4(__int_as_float(xr >= 0 ? x0 : -1), xr >= 0 ? p.wx0[cc] : 0.f,
-                                                     xr >= 0 && has_x1 ? p.wx1[cc] : 0.f, 0.f);
+            if (cc >= 0 && cc < p.C)
+                cp_async<16>(colp + k * kBlk + tid - kFZ, p.xcol + cc);
+            else
+                colp[k * kBlk + tid - kFZ] = make_float4(__int_as_float(-1), 0.f, 0.f, 0.f);
         }
         const float* mag_f = mag + s.t * mag_tile_stride + static_cast<int64_t>(f) * n_tile_x * kHalf;
         float* pa = sm + s.off;
@@ -308,11 +356,11 @@ __global__ void __launch_bounds__(kStThreads) k_stitch_frames(const StitchDev* _
     for (int q = 0; q < kFRows; ++q) an[q] = ad[q] = 0.f;
     for (int k = 0; k < ns; ++k) {
         const float4 cp = colp[k * kBlk + tx];
-        const int x0 = __float_as_int(cp.x);
-        if (x0 < 0) continue;
+        const int xr = __float_as_int(cp.x);
+        if (xr < 0) continue;
         const int rst = slot[k].rst;
         // this thread's first A-scan of the patch, rows indexed by zr directly
-        const float* pa = sm + slot[k].off + x0 * rst - slot[k].r_lo;
+        const float* pa = sm + slot[k].off + (xr - slot[k].x_lo) * rst - slot[k].r_lo;
         const float wx0 = cp.y, wx1 = cp.z;
         const float4* rpk = rowp + k * kFZ + ty;
         const float2* rfk = rowf + k * kFZ + ty;
@@ -609,7 +657,8 @@ cudaError_t launch_stitch_frames(const StitchDev* plans_dev, const TileList& til
                                  cudaStream_t st) {
     if (B == 0) return cudaSuccess;
     if (rows != 32 && rows != 64 && rows != 128) return cudaErrorInvalidValue;
-    const size_t smem = patch_smem_bytes + sizeof(float) * static_cast<size_t>(ns_max) * (6 * rows + 4 * kBlk) + 16;
+    const size_t smem = patch_smem_bytes +
+                        static_cast<size_t>(ns_max) * (sizeof(SlotPlan) + sizeof(float) * (6 * rows + 4 * kBlk)) + 16;
     if (smem > 160 * 1024) return cudaErrorInvalidValue;
     auto kern = rows == 32 ? k_stitch_frames<32> : (rows == 64 ? k_stitch_frames<64> : k_stitch_frames<128>);
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
