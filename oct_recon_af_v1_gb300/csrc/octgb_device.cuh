@@ -15,20 +15,52 @@ constexpr int kSpecStride = kN + (kN >> kPadShift);       // padded complex line
 
 __device__ __forceinline__ int pad(int e) { return e + (e >> kPadShift); }
 
-__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+// Packed float32 pairs (sm_100 family f32x2 instructions): one instruction
+// for both lanes, each lane rounded to nearest exactly as the scalar operation,
+// so results are bit-identical to two scalar ops.  The explicit rounding mode
+// also keeps ptxas from contracting them (as it would not contract the
+// scalar forms here either).
+__device__ __forceinline__ float2 add2(float2 a, float2 b) {
+    float2 r;
+    asm("{\n\t.reg .b64 x, y, z;\n\tmov.b64 x, {%2, %3};\n\tmov.b64 y, {%4, %5};\n\t"
+        "add.rn.f32x2 z, x, y;\n\tmov.b64 {%0, %1}, z;\n\t}"
+        : "=f"(r.x), "=f"(r.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return r;
+}
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
+    float2 r;
+    asm("{\n\t.reg .b64 x, y, z;\n\tmov.b64 x, {%2, %3};\n\tmov.b64 y, {%4, %5};\n\t"
+        "sub.rn.f32x2 z, x, y;\n\tmov.b64 {%0, %1}, z;\n\t}"
+        : "=f"(r.x), "=f"(r.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return r;
+}
+// (a.x b.x + c.x, a.y b.y + c.y), each a single-rounding fma
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
+    float2 r;
+    asm("{\n\t.reg .b64 x, y, z, w;\n\tmov.b64 x, {%2, %3};\n\tmov.b64 y, {%4, %5};\n\t"
+        "mov.b64 z, {%6, %7};\n\tfma.rn.f32x2 w, x, y, z;\n\tmov.b64 {%0, %1}, w;\n\t}"
+        : "=f"(r.x), "=f"(r.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+    return r;
+}
+
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return add2(a, b); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return sub2(a, b); }
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
     return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
 }
 __device__ __forceinline__ float2 muli(float2 a) { return make_float2(-a.y, a.x); }
 
-// inverse DFT-4 (omega = +i), natural order in and out
+// inverse DFT-4 (omega = +i), natural order in and out; b +- i e lane-crossed
+// in scalar form (a packed form would need the swapped pair of e first)
 __device__ __forceinline__ void dft4(float2& x0, float2& x1, float2& x2, float2& x3) {
-    const float2 a = cadd(x0, x2), b = csub(x0, x2), c = cadd(x1, x3), d = muli(csub(x1, x3));
+    const float2 a = cadd(x0, x2), b = csub(x0, x2), c = cadd(x1, x3), e = csub(x1, x3);
     x0 = cadd(a, c);
     x2 = csub(a, c);
-    x1 = cadd(b, d);
-    x3 = csub(b, d);
+    x1 = make_float2(b.x - e.y, b.y + e.x);
+    x3 = make_float2(b.x + e.y, b.y - e.x);
 }
 
 // cos/sin of multiples of pi/8 (float64 literals rounded to float32)

@@ -210,30 +210,37 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
     const int warp = tid / 32, lane = tid % 32;
     const int64_t nquads = kQueue ? static_cast<int64_t>(a.total_quads) : (a.n_ascans + kPerCta - 1) / kPerCta;
 
-    // this thread's shifted sinc weights and source window base
-    float wr[4][U];
-    if (U % 4 == 0) {
-        const float4* wp = reinterpret_cast<const float4*>(a.g.wsh + static_cast<int64_t>(tid) * 4 * U);
+    // this thread's shifted sinc weights and source window base; the weights
+    // of outputs 4t, 4t+1 (and 4t+2, 4t+3) at window step u form one packed
+    // pair wp[0][u] (wp[1][u]): two outputs per f32x2 fma
+    float2 wp[2][U];
+    {
+        auto set_w = [&](int r, int u, float w) {
+            if (r & 1) wp[r >> 1][u].y = w; else wp[r >> 1][u].x = w;
+        };
+        if (U % 4 == 0) {
+            const float4* src = reinterpret_cast<const float4*>(a.g.wsh + static_cast<int64_t>(tid) * 4 * U);
 #pragma unroll
-        for (int r = 0; r < 4; ++r)
+            for (int r = 0; r < 4; ++r)
 #pragma unroll
-            for (int q = 0; q < U / 4; ++q) {
-                const float4 v = __ldg(wp + r * (U / 4) + q);
-                wr[r][4 * q] = v.x;
-                wr[r][4 * q + 1] = v.y;
-                wr[r][4 * q + 2] = v.z;
-                wr[r][4 * q + 3] = v.w;
-            }
-    } else {                                          // U = 14: rows of 56 bytes, 8-byte aligned
-        const float2* wp = reinterpret_cast<const float2*>(a.g.wsh + static_cast<int64_t>(tid) * 4 * U);
+                for (int q = 0; q < U / 4; ++q) {
+                    const float4 v = __ldg(src + r * (U / 4) + q);
+                    set_w(r, 4 * q, v.x);
+                    set_w(r, 4 * q + 1, v.y);
+                    set_w(r, 4 * q + 2, v.z);
+                    set_w(r, 4 * q + 3, v.w);
+                }
+        } else {                                      // U = 14: rows of 56 bytes, 8-byte aligned
+            const float2* src = reinterpret_cast<const float2*>(a.g.wsh + static_cast<int64_t>(tid) * 4 * U);
 #pragma unroll
-        for (int r = 0; r < 4; ++r)
+            for (int r = 0; r < 4; ++r)
 #pragma unroll
-            for (int q = 0; q < U / 2; ++q) {
-                const float2 v = __ldg(wp + r * (U / 2) + q);
-                wr[r][2 * q] = v.x;
-                wr[r][2 * q + 1] = v.y;
-            }
+                for (int q = 0; q < U / 2; ++q) {
+                    const float2 v = __ldg(src + r * (U / 2) + q);
+                    set_w(r, 2 * q, v.x);
+                    set_w(r, 2 * q + 1, v.y);
+                }
+        }
     }
     const int s0 = __ldg(a.g.s0 + tid);
     const int wrot = s0 % U;                          // window samples before s0 wrap to the next period
@@ -344,10 +351,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
             float rv[4];
             RawLoad<RawT>::load4(&S.stage[buf][g][j], rv);
             const float4 ap = apv[q];
-            dv[4 * q] = rv[0] - ap.x;
-            dv[4 * q + 1] = rv[1] - ap.y;
-            dv[4 * q + 2] = rv[2] - ap.z;
-            dv[4 * q + 3] = rv[3] - ap.w;
+            const float2 d01 = sub2(make_float2(rv[0], rv[1]), make_float2(ap.x, ap.y));
+            const float2 d23 = sub2(make_float2(rv[2], rv[3]), make_float2(ap.z, ap.w));
+            dv[4 * q] = d01.x;
+            dv[4 * q + 1] = d01.y;
+            dv[4 * q + 2] = d23.x;
+            dv[4 * q + 3] = d23.y;
             sum += (dv[4 * q] + dv[4 * q + 1]) + (dv[4 * q + 2] + dv[4 * q + 3]);
         }
 #pragma unroll
@@ -357,10 +366,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
         {
             const float m = ((S.red[g][0] + S.red[g][1]) + (S.red[g][2] + S.red[g][3])) * (1.0f / kN);
             if (lt == 0) S.mval[g] = m;
+            const float2 m2 = make_float2(m, m);
 #pragma unroll
-            for (int q = 0; q < 4; ++q)
-                *reinterpret_cast<float4*>(&S.d[g][4 * lt + 512 * q]) =
-                    make_float4(dv[4 * q] - m, dv[4 * q + 1] - m, dv[4 * q + 2] - m, dv[4 * q + 3] - m);
+            for (int q = 0; q < 4; ++q) {
+                const float2 e01 = sub2(make_float2(dv[4 * q], dv[4 * q + 1]), m2);
+                const float2 e23 = sub2(make_float2(dv[4 * q + 2], dv[4 * q + 3]), m2);
+                *reinterpret_cast<float4*>(&S.d[g][4 * lt + 512 * q]) = make_float4(e01.x, e01.y, e23.x, e23.y);
+            }
         }
         // the window of this thread's four outputs: in flight across the barrier
         const float4 wa = __ldg(reinterpret_cast<const float4*>(a.g.win + 4 * tid));
@@ -382,14 +394,23 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
                 float win[U];
 #pragma unroll
                 for (int u = 0; u < U; ++u) win[u] = (u < wrot ? dkh : dk)[u];
+                // acc_r = sum_u w[r][u] win[u], the fmas in window order, two
+                // outputs per packed fma
+                float2 acc01 = make_float2(0.f, 0.f), acc23 = make_float2(0.f, 0.f);
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const float2 wu = make_float2(win[u], win[u]);
+                    acc01 = fma2(wp[0][u], wu, acc01);
+                    acc23 = fma2(wp[1][u], wu, acc23);
+                }
+                const float2 mk2 = make_float2(mk, mk);
+                const float2 v01 = add2(acc01, mk2), v23 = add2(acc23, mk2);
+                const float vr[4] = {v01.x, v01.y, v23.x, v23.y};
                 float lh[4], lx[4];
                 bool lsafe[4];
 #pragma unroll
                 for (int r = 0; r < 4; ++r) {
-                    float acc = 0.f;
-#pragma unroll
-                    for (int u = 0; u < U; ++u) acc = fmaf(wr[r][u], win[u], acc);
-                    const float v = acc + mk;
+                    const float v = vr[r];
                     const float2 sp = make_float2(v * wre[r], v * wim[r]);
                     if (Mode == kModeLinHann) {
                         // the real part of the spec output (1/N undone) times the
