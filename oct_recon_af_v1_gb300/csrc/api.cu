@@ -1862,7 +1862,7 @@ int octgb_selftest_wait_expiry(octgb_ctx* c, int which, int wait_limit_us) {
             throw;
         }
         ck(set(kDefaultLimit, 0, c->stream), "restore wait limit");
-        throw Error(OCTGB_ERR_STATE, "self-test: the starved bulk-copy wait did not expire");
+        throw Error(OCTGB_ERR_STATE, "self-test: the starved row-copy wait did not expire");
     });
 }
 

@@ -1,12 +1,15 @@
 // Fused spectral stage for sm_103a: raw camera counts -> |ifft| / dB.
 //
 // One CTA of 512 threads processes four A-scans per iteration of a persistent
-// loop.  Per A-scan (2048 samples):
-//   (a) the raw row (4 KiB of uint16) is staged into shared memory by a bulk
-//       TMA copy (cp.async.bulk, mbarrier completion), double-buffered so the
-//       next quad's rows stream in while the current quad is computed; lanes
-//       0-3 of warp 0 resolve the quad's four rows (32-bit index arithmetic),
-//       issue their copies and leave the slots in shared memory for the CTA;
+// loop, one A-scan per group of 128 threads in the per-A-scan stages.
+// Per A-scan (2048 samples):
+//   (a) the raw row (4 KiB of uint16) and the B-scan's apodisation-mean row
+//       reach shared memory by per-thread asynchronous copies one quad ahead:
+//       each thread copies exactly the samples it reads, and one arrival per
+//       thread on its group's mbarrier marks them landed (the bounded wait of
+//       the next iteration); the raw copies start once the background has
+//       read the current row, the apodisation copies once the sinc has read
+//       the current lines, so both hide behind the sinc and the transform;
 //   (b) d[j] = float(raw[j]) - apod[j] (float32 apodisation mean of the
 //       B-scan, rounded from an exact sum as core/cpu_kernels.py:20-25 does),
 //       line mean m removed before d reaches shared memory (cpu_kernels.py:
@@ -18,7 +21,8 @@
 //   (e) inverse FFT of length 2048 in shared memory: Stockham radix 16,16,8,
 //       each radix butterfly in registers (128 threads, 16 points each);
 //   (f) |X[k]| for k < N/2 (spectral.py:153), optionally 20*log10 with a
-//       depth crop and a running min/max for the global clim.
+//       depth crop and a running min/max for the global clim; magnitudes of
+//       16-bit raws leave by one 4 KiB bulk copy per A-scan from shared memory.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -106,25 +110,26 @@ struct SlotRef {
 
 template <typename RawT>
 struct Smem {
-    uint64_t bar[2];
-    SlotRef slot[2][kPerCta];                       // the quad of each stage buffer (thread 0 fills it)
+    uint64_t bar[kPerCta];                          // slot k: its group's copies of the rows have landed
+    SlotRef slot[kPerCta];                          // queue mode: the next quad's slots (warp 0 fills them)
     float red[kPerCta][4];
     float mval[kPerCta];
     unsigned int mm[2];
-    alignas(128) RawT stage[2][kPerCta][kN];        // bulk-copy destinations (16-byte aligned)
-    alignas(16) float d[kPerCta][kDLine];           // background-free line
+    alignas(16) RawT stage[kPerCta][kN];            // raw rows (each thread copies the samples it reads)
+    alignas(16) float d[kPerCta][kDLine];           // apodisation-mean row, then the background-free line
     alignas(16) float2 spec[kPerCta][kSpecStride];  // windowed spectrum / FFT work line
     // second FFT line of each A-scan (16-bit raws; float32 raws need the
     // shared memory for their larger staging rows and transform in place)
     alignas(16) float2 fft_y[sizeof(RawT) == 2 ? kPerCta : 1][kSpecStride];
     alignas(16) float2 tw2[16][16];                 // stage-2 twiddles [r][j mod 16]
     alignas(16) float2 tw3[8][256];                 // stage-3 twiddles [r][j]
+    alignas(16) float4 win[2][kThreads];            // window of outputs 4t, 4t+1 ([0][t]) and 4t+2, 4t+3 ([1][t])
 };
 
 // dynamic + static shared memory of the kernel within the 227 KB a CTA may use
-static_assert(sizeof(Smem<uint16_t>) + 2 * sizeof(int64_t) + kMaxQueueTiles * sizeof(unsigned) <= 232448,
+static_assert(sizeof(Smem<uint16_t>) + sizeof(int64_t) + kMaxQueueTiles * sizeof(unsigned) <= 232448,
               "spectral kernel shared memory (16-bit raws) exceeds 227 KB");
-static_assert(sizeof(Smem<float>) + 2 * sizeof(int64_t) + kMaxQueueTiles * sizeof(unsigned) <= 232448,
+static_assert(sizeof(Smem<float>) + sizeof(int64_t) + kMaxQueueTiles * sizeof(unsigned) <= 232448,
               "spectral kernel shared memory (float32 raws) exceeds 227 KB");
 
 // A launch holds fewer than 2^31 A-scans (the host checks), so the index
@@ -201,7 +206,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
     constexpr bool kQueue = Mode == kModeResample;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     Smem<RawT>& S = *reinterpret_cast<Smem<RawT>*>(smem_raw);
-    __shared__ int64_t qbuf[2];                        // quad held by each stage buffer (-1: none)
+    __shared__ int64_t qbuf[1];                        // queue mode: the next quad (-1: none)
     __shared__ unsigned int quad0_s[kQueue ? kMaxQueueTiles : 1];
 
     const int tid = threadIdx.x;
@@ -209,6 +214,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
     const int lt = tid % kGroup;       // thread within the A-scan group
     const int warp = tid / 32, lane = tid % 32;
     const int64_t nquads = kQueue ? static_cast<int64_t>(a.total_quads) : (a.n_ascans + kPerCta - 1) / kPerCta;
+    // magnitude mode with 16-bit raws: each A-scan's |X| leaves by one bulk
+    // copy from the free second FFT line (thread 0 of its group issues it)
+    const bool bulk_out = Mode == kModeMag && sizeof(RawT) == 2 && (reinterpret_cast<uintptr_t>(a.out) & 15u) == 0;
 
     // this thread's shifted sinc weights and source window base; the weights
     // of outputs 4t, 4t+1 (and 4t+2, 4t+3) at window step u form one packed
@@ -247,8 +255,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
     const int wbase = s0 - wrot;
 
     if (tid == 0) {
-        mbar_init(&S.bar[0], 1);
-        mbar_init(&S.bar[1], 1);
+        for (int k = 0; k < kPerCta; ++k) mbar_init(&S.bar[k], kGroup);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         S.mm[0] = 0xffffffffu;
         S.mm[1] = 0u;
@@ -264,10 +271,17 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
         const int r = k / 256, j = k % 256;
         S.tw3[r][j] = __ldg(a.g.tw + (r * j) % kN);
     }
+    S.win[0][tid] = __ldg(reinterpret_cast<const float4*>(a.g.win + 4 * tid));
+    S.win[1][tid] = __ldg(reinterpret_cast<const float4*>(a.g.win + 4 * tid + 2));
     float run_min = __int_as_float(0x7f800000), run_max = -__int_as_float(0x7f800000);
     __syncthreads();
 
-    // the next quad after `cur` (lane 0 of warp 0)
+    // Rows reach shared memory by per-thread asynchronous copies: thread lt of
+    // group g copies exactly the raw samples and apodisation-mean values it
+    // reads (4 x 4 at 4 lt + 512 q) of its group's slot, one quad ahead, and
+    // one arrival per thread on the group's barrier (kGroup a phase) marks
+    // them landed.  No thread waits on another to issue, and the CTA-wide
+    // barrier of the background doubles as the check of the bounded waits.
     int64_t item_next = 0, item_end = 0;               // queue mode: current grab [next, end)
     auto next_quad = [&](int64_t cur) -> int64_t {
         if (!kQueue) {
@@ -281,63 +295,113 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
         item_end = base + a.grab < nquads ? base + a.grab : nquads;
         return base;
     };
-    // warp 0 issues a quad: lane k < 4 resolves slot k (in parallel) and copies
-    // its row; lane 0 arms the buffer's barrier first
-    int tile_hint = 0;                                 // lanes 0-3: tile of the last quad issued
-    auto issue = [&](int64_t quad, int buf, bool first) {
-        SlotRef r{};
-        bool v = false;
-        if (lane < kPerCta) {
-            r = slot_ref<RawT, kQueue>(a, quad0_s, quad, lane, tile_hint);
-            v = r.valid;
-            S.slot[buf][lane] = r;                     // read by every thread once the buffer is current
-        }
-        const uint32_t nvalid = static_cast<uint32_t>(__popc(__ballot_sync(0xffffffffu, v)));
-        if (lane == 0) mbar_expect_tx(&S.bar[buf], nvalid * kN * sizeof(RawT) + starved_bytes(first));
-        __syncwarp();
-        if (v) tma_bulk_g2s(&S.stage[buf][lane][0], r.row, kN * sizeof(RawT), &S.bar[buf]);
-    };
-    // lane 0 of warp 0 owns the schedule; the quad is shared with the warp
+    // queue mode: lane 0 of warp 0 owns the schedule; lanes 0-3 resolve the
+    // quad's slots into S.slot (read by the groups after the next CTA barrier)
+    int tile_hint = 0;                                 // queue mode, lanes 0-3: tile of the last quad resolved
     auto warp_next = [&](int64_t cur) -> int64_t {
         int64_t n = 0;
         if (lane == 0) n = next_quad(cur);
-        return static_cast<int64_t>(__shfl_sync(0xffffffffu, static_cast<long long>(n), 0));
+        n = static_cast<int64_t>(__shfl_sync(0xffffffffu, static_cast<long long>(n), 0));
+        if (lane < kPerCta && n >= 0) S.slot[lane] = slot_ref<RawT, true>(a, quad0_s, n, lane, tile_hint);
+        return n;
+    };
+    // static mode: this group's A-scan (position within the batch) steps by
+    // gridDim.x quads a time without division: step = dbt B-scans + dx A-scans
+    const unsigned int nx_u = static_cast<unsigned int>(a.nx), B_u = static_cast<unsigned int>(a.B);
+    const unsigned int step = static_cast<unsigned int>(gridDim.x) * kPerCta;
+    const unsigned int dbt = step / nx_u, dx = step - dbt * nx_u;
+    unsigned int pas = 0, px = 0, pb = 0, psg = 0;     // A-scan, column, B-scan in segment, segment
+    auto static_slot = [&]() -> SlotRef {
+        SlotRef r;
+        r.valid = static_cast<int64_t>(pas) < a.n_ascans;
+        const unsigned int sg = r.valid ? psg : 0u;
+        r.row = static_cast<const RawT*>(a.seg[sg]) +
+                ((static_cast<int64_t>(r.valid ? pb : 0u) * a.interf + a.apod + (r.valid ? px : 0u)) * kN);
+        r.apod_row = static_cast<int64_t>(sg) * B_u + (r.valid ? pb : 0u);
+        r.as = pas;
+        r.tile = 0;
+        return r;
+    };
+    auto static_advance = [&]() {
+        pas += step;
+        px += dx;
+        unsigned int inc = dbt;
+        if (px >= nx_u) {
+            px -= nx_u;
+            ++inc;
+        }
+        pb += inc;
+        if (pb >= B_u) {
+            const unsigned int c = pb / B_u;
+            psg += c;
+            pb -= c * B_u;
+        }
+    };
+    // this thread's raw samples / apodisation values of slot r, then its
+    // arrival on the group's barrier (after the apodisation copies)
+    auto copy_raw = [&](const SlotRef& r) {
+        if (!r.valid) return;
+        const RawT* src = static_cast<const RawT*>(r.row);
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            cp_async_ca<4 * sizeof(RawT)>(&S.stage[g][4 * lt + 512 * q], src + 4 * lt + 512 * q);
+    };
+    auto copy_apod = [&](const SlotRef& r, bool first) {
+        if (r.valid) {
+            const float* src = a.apod_mean + r.apod_row * kN;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) cp_async_ca<16>(&S.d[g][4 * lt + 512 * q], src + 4 * lt + 512 * q);
+        }
+        // self-test: the first phase of slot 0's barrier waits for bytes that never come
+        if (first && tid == 0) {
+            const uint32_t sb = starved_bytes(true);
+            if (sb) mbar_expect_tx_only(&S.bar[0], sb);
+        }
+        cp_async_arrive(&S.bar[g]);
     };
 
-    if (warp == 0) {
-        const int64_t q0 = warp_next(-1);
-        if (lane == 0) qbuf[0] = q0;
-        if (q0 >= 0) issue(q0, 0, true);
-    }
-    __syncthreads();
-
-    for (int it = 0;; ++it) {
-        const int buf = it & 1;
-        const int64_t quad = qbuf[buf];
-        if (quad < 0) break;
+    int64_t quad;
+    SlotRef cur{};                                     // this group's slot of the current quad
+    if (!kQueue) {
+        quad = next_quad(-1);
+        if (quad >= 0) {
+            const unsigned int as0 = static_cast<unsigned int>(quad) * kPerCta + static_cast<unsigned int>(g);
+            const unsigned int bt = as0 / nx_u;
+            pas = as0;
+            px = as0 - bt * nx_u;
+            psg = bt / B_u;
+            pb = bt - psg * B_u;
+            cur = static_slot();
+        }
+    } else {
         if (warp == 0) {
-            const int64_t nq = warp_next(quad);
-            if (lane == 0) qbuf[buf ^ 1] = nq;
-            if (nq >= 0) issue(nq, buf ^ 1, false);
+            const int64_t q0 = warp_next(-1);
+            if (lane == 0) qbuf[0] = q0;
         }
+        __syncthreads();
+        quad = qbuf[0];
+        if (quad >= 0) cur = S.slot[g];
+        __syncthreads();                               // read before warp 0 resolves the next quad
+    }
+    if (quad >= 0) {
+        copy_raw(cur);
+        copy_apod(cur, true);
+    }
 
-        // this group's apodisation row does not depend on the raw copy: its
-        // loads are in flight while the copy is awaited
-        const SlotRef me = S.slot[buf][g];
+    for (int it = 0; quad >= 0; ++it) {
+        const SlotRef me = cur;
         const bool valid = me.valid;
-        const float* apod = a.apod_mean + me.apod_row * kN;
-        float4 apv[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) apv[q] = __ldg(reinterpret_cast<const float4*>(apod + 4 * lt + 512 * q));
-
-        const bool ok = mbar_wait_bounded(&S.bar[buf], (it >> 1) & 1, a.status);
-        if (__syncthreads_or(!ok)) {
-            // the next quad's rows may still be arriving: let them land before
-            // the CTA's shared memory is released
-            if (tid == 0 && qbuf[buf ^ 1] >= 0) mbar_wait_bounded(&S.bar[buf ^ 1], ((it + 1) >> 1) & 1, a.status);
-            __syncthreads();
-            return;
+        int64_t nq = -1;
+        if (!kQueue) {
+            nq = next_quad(quad);
+        } else {
+            // the groups read S.slot / qbuf of this quad before the last CTA barrier
+            if (warp == 0) {
+                const int64_t n = warp_next(quad);
+                if (lane == 0) qbuf[0] = n;
+            }
         }
+        const bool ok = mbar_wait_bounded(&S.bar[g], it & 1, a.status);
 
         // ---- (b) background: d = raw - apod, line mean (group g, A-scan g) ----
         // d = raw - apod stays in registers until the line mean m is known;
@@ -349,8 +413,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
         for (int q = 0; q < 4; ++q) {
             const int j = 4 * lt + 512 * q;
             float rv[4];
-            RawLoad<RawT>::load4(&S.stage[buf][g][j], rv);
-            const float4 ap = apv[q];
+            RawLoad<RawT>::load4(&S.stage[g][j], rv);
+            const float4 ap = *reinterpret_cast<const float4*>(&S.d[g][j]);
             const float2 d01 = sub2(make_float2(rv[0], rv[1]), make_float2(ap.x, ap.y));
             const float2 d23 = sub2(make_float2(rv[2], rv[3]), make_float2(ap.z, ap.w));
             dv[4 * q] = d01.x;
@@ -374,10 +438,27 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
                 *reinterpret_cast<float4*>(&S.d[g][4 * lt + 512 * q]) = make_float4(e01.x, e01.y, e23.x, e23.y);
             }
         }
-        // the window of this thread's four outputs: in flight across the barrier
-        const float4 wa = __ldg(reinterpret_cast<const float4*>(a.g.win + 4 * tid));
-        const float4 wb = __ldg(reinterpret_cast<const float4*>(a.g.win + 4 * tid + 2));
-        __syncthreads();
+        if (__syncthreads_or(!ok)) {
+            // a wait ran out: let this thread's copies land before the CTA's
+            // shared memory is released
+            cp_async_wait_all();
+            if (bulk_out && lt == 0) bulk_wait_all();
+            __syncthreads();
+            return;
+        }
+        // the next quad's raw samples (this thread's own have been read above)
+        SlotRef nxt{};
+        if (!kQueue) {
+            if (nq >= 0) {
+                static_advance();
+                nxt = static_slot();
+            }
+        } else {
+            nq = qbuf[0];
+            if (nq >= 0) nxt = S.slot[g];
+        }
+        if (nq >= 0) copy_raw(nxt);
+        const float4 wa = S.win[0][tid], wb = S.win[1][tid];
 
         // ---- (c)+(d) sinc k-linearisation and window, four A-scans ----
         {
@@ -439,7 +520,14 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
                 }
             }
         }
+        // the previous quad's magnitudes have left the second FFT line before
+        // the transform below overwrites it
+        if (bulk_out && lt == 0) bulk_wait_read();
         __syncthreads();
+        // every line has been read: the next quad's apodisation row into d
+        if (nq >= 0) copy_apod(nxt, false);
+        quad = nq;
+        cur = nxt;
         if (Mode == kModeSpec || Mode == kModeLinHann) continue;
 
         // ---- (e)+(f) inverse FFT, group g on its own line; |X[k]|, k < N/2 ----
@@ -449,7 +537,18 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
             ifft2048_low_mag_pp(X, S.fft_y[g], S.tw2, S.tw3, g, lt, magv);
         else
             ifft2048_low_mag(X, S.tw2, S.tw3, g, lt, magv);
-        if (Mode == kModeMag || Mode == kModeDb) {
+        if (Mode == kModeMag && bulk_out) {
+            // the last stage read only X: the second line Y is free for |X[k]|
+            // (k < N/2, contiguous float32), which leaves by one 4 KiB bulk copy
+            float* M = reinterpret_cast<float*>(S.fft_y[sizeof(RawT) == 2 ? g : 0]);
+#pragma unroll
+            for (int h = 0; h < 2; ++h)
+#pragma unroll
+                for (int r = 0; r < 4; ++r) M[lt + 128 * h + 256 * r] = magv[h][r];
+            fence_proxy_async();
+            group_sync(g);
+            if (lt == 0 && valid) tma_bulk_s2g(a.out + me.as * kHalf, M, kHalf * sizeof(float));
+        } else if (Mode == kModeMag || Mode == kModeDb) {
             if (valid) {
 #pragma unroll
                 for (int h = 0; h < 2; ++h)
@@ -539,6 +638,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
         }
     }
 
+    if (bulk_out && lt == 0) bulk_wait_all();
     if ((Mode == kModeDb || Mode == kModeResample) && a.minmax != nullptr) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {

@@ -1,10 +1,11 @@
 """A bounded device wait that runs out: the kernels' error path.
 
-octgb_selftest_wait_expiry makes each CTA's first bulk-copy barrier expect 16
+octgb_selftest_wait_expiry makes each CTA's first row-copy barrier expect 16
 bytes more than its copies deliver (every copy lands; only that barrier never
 completes) with the wait limit cut to a few milliseconds.  The wait must run
-out, the kernel must drain what it issued (the spectral kernel its next rows;
-the tensor-core kernel its copies and MMAs, and free its tensor memory) and
+out, the kernel must drain what it issued (the spectral kernel its threads'
+row copies; the tensor-core kernel its copies and MMAs, and free its tensor
+memory) and
 report through the status word; the call returns OCTGB_ERR_TIMEOUT and the
 same context then reconstructs normally.  No GPU faults, traps or hangs: every
 wait is bounded and every copy issued is a valid one.
