@@ -128,15 +128,13 @@ __device__ __forceinline__ void tma_bulk_g2s(void* dst, const void* src, uint32_
         : "memory");
 }
 
-// asynchronous global -> shared copy of kBytes (4, 8 or 16; both addresses
-// aligned to it), tracked per thread
-template <int kBytes>
-__device__ __forceinline__ void cp_async_ca(void* dst, const void* src) {
-    static_assert(kBytes == 4 || kBytes == 8 || kBytes == 16, "cp.async element size");
-    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(smem_u32(dst)), "l"(src), "n"(kBytes) : "memory");
-}
 // one arrival on the mbarrier once every cp.async this thread issued so far
 // has landed (counted against the barrier's expected arrivals)
+// asynchronous global -> shared copy of 16 bytes (both addresses 16-byte
+// aligned) through L2 only, no L1 line allocated; tracked per thread
+__device__ __forceinline__ void cp_async_cg16(void* dst, const void* src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
 __device__ __forceinline__ void cp_async_arrive(uint64_t* bar) {
     asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
 }

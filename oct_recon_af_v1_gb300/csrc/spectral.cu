@@ -4,9 +4,9 @@
 // loop, one A-scan per group of 128 threads in the per-A-scan stages.
 // Per A-scan (2048 samples):
 //   (a) the raw row (4 KiB of uint16) and the B-scan's apodisation-mean row
-//       reach shared memory by per-thread asynchronous copies one quad ahead:
-//       each thread copies exactly the samples it reads, and one arrival per
-//       thread on its group's mbarrier marks them landed (the bounded wait of
+//       reach shared memory by asynchronous 16-byte copies (through L2 only)
+//       that the A-scan's 128 threads issue one quad ahead; one arrival per
+//       thread on the group's mbarrier marks them landed (the bounded wait of
 //       the next iteration); the raw copies start once the background has
 //       read the current row, the apodisation copies once the sinc has read
 //       the current lines, so both hide behind the sinc and the transform;
@@ -276,12 +276,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
     float run_min = __int_as_float(0x7f800000), run_max = -__int_as_float(0x7f800000);
     __syncthreads();
 
-    // Rows reach shared memory by per-thread asynchronous copies: thread lt of
-    // group g copies exactly the raw samples and apodisation-mean values it
-    // reads (4 x 4 at 4 lt + 512 q) of its group's slot, one quad ahead, and
-    // one arrival per thread on the group's barrier (kGroup a phase) marks
-    // them landed.  No thread waits on another to issue, and the CTA-wide
-    // barrier of the background doubles as the check of the bounded waits.
+    // Rows reach shared memory by asynchronous copies issued by every thread:
+    // group g copies its slot's raw row and apodisation-mean row one quad
+    // ahead, and one arrival per thread on the group's barrier (kGroup a
+    // phase) marks them landed.  No warp issues for the others, and the
+    // CTA-wide barrier of the background doubles as the check of the bounded
+    // waits.
     int64_t item_next = 0, item_end = 0;               // queue mode: current grab [next, end)
     auto next_quad = [&](int64_t cur) -> int64_t {
         if (!kQueue) {
@@ -337,20 +337,24 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
             pb -= c * B_u;
         }
     };
-    // this thread's raw samples / apodisation values of slot r, then its
-    // arrival on the group's barrier (after the apodisation copies)
+    // slot r's raw row and apodisation-mean row, copied by the group in
+    // 16-byte pieces through L2 only (no L1 lines: the shared memory leaves L1
+    // ~28 KB), then each thread's arrival on the group's barrier (after the
+    // apodisation copies); the completed phase makes both rows visible to the
+    // whole group
     auto copy_raw = [&](const SlotRef& r) {
         if (!r.valid) return;
-        const RawT* src = static_cast<const RawT*>(r.row);
+        constexpr int kPieces = kN * static_cast<int>(sizeof(RawT)) / 16;   // 256 (16-bit raws) or 512
+        const char* src = static_cast<const char*>(r.row);
+        char* dst = reinterpret_cast<char*>(&S.stage[g][0]);
 #pragma unroll
-        for (int q = 0; q < 4; ++q)
-            cp_async_ca<4 * sizeof(RawT)>(&S.stage[g][4 * lt + 512 * q], src + 4 * lt + 512 * q);
+        for (int c = lt; c < kPieces; c += kGroup) cp_async_cg16(dst + 16 * c, src + 16 * c);
     };
     auto copy_apod = [&](const SlotRef& r, bool first) {
         if (r.valid) {
             const float* src = a.apod_mean + r.apod_row * kN;
 #pragma unroll
-            for (int q = 0; q < 4; ++q) cp_async_ca<16>(&S.d[g][4 * lt + 512 * q], src + 4 * lt + 512 * q);
+            for (int q = 0; q < 4; ++q) cp_async_cg16(&S.d[g][4 * lt + 512 * q], src + 4 * lt + 512 * q);
         }
         // self-test: the first phase of slot 0's barrier waits for bytes that never come
         if (first && tid == 0) {
