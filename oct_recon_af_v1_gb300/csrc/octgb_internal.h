@@ -89,6 +89,9 @@ struct SpectralArgs {
     unsigned int total_quads;
     int grab;                 // quads taken per atomic grab
     float thr;                // weight threshold (pipeline.py:296-297)
+    // static mode, set by the launcher: a CTA's grid stride (gridDim.x quads)
+    // as whole B-scans plus A-scans, step_x < nx
+    unsigned int step_bt, step_x;
 };
 
 // spectral.cu

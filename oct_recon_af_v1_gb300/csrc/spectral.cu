@@ -102,8 +102,8 @@ __device__ __forceinline__ float mul_window(float x, float2 h2, bool& safe) {
 // memory, binary search).
 struct SlotRef {
     const void* row;     // raw row (kN samples)
-    int64_t apod_row;    // row of the apodisation-mean buffer
-    int64_t as;          // static: global A-scan index; queue: A-scan index within the tile
+    unsigned int apod_row;   // row of the apodisation-mean buffer
+    unsigned int as;     // static: global A-scan index; queue: A-scan index within the tile
     int tile;            // queue: tile index
     bool valid;
 };
@@ -180,8 +180,8 @@ __device__ __forceinline__ SlotRef slot_ref(const SpectralArgs& a, const unsigne
         const int64_t xc = r.valid ? x : 0;
         const int64_t bc = r.valid ? b : 0;
         r.row = static_cast<const RawT*>(t.raw) + ((bc * t.interf + t.apod + xc) * kN);
-        r.apod_row = t.apod_row0 + bc;
-        r.as = bc * t.nx + xc;                         // A-scan index within the tile
+        r.apod_row = static_cast<unsigned int>(t.apod_row0 + bc);
+        r.as = static_cast<unsigned int>(bc * t.nx + xc);   // A-scan index within the tile
         r.tile = lo;
     }
     return r;
@@ -306,10 +306,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
         return n;
     };
     // static mode: this group's A-scan (position within the batch) steps by
-    // gridDim.x quads a time without division: step = dbt B-scans + dx A-scans
-    const unsigned int nx_u = static_cast<unsigned int>(a.nx), B_u = static_cast<unsigned int>(a.B);
-    const unsigned int step = static_cast<unsigned int>(gridDim.x) * kPerCta;
-    const unsigned int dbt = step / nx_u, dx = step - dbt * nx_u;
+    // gridDim.x quads a time without division (the launcher splits the
+    // stride into a.step_bt B-scans + a.step_x A-scans)
     unsigned int pas = 0, px = 0, pb = 0, psg = 0;     // A-scan, column, B-scan in segment, segment
     auto static_slot = [&]() -> SlotRef {
         SlotRef r;
@@ -317,24 +315,25 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
         const unsigned int sg = r.valid ? psg : 0u;
         r.row = static_cast<const RawT*>(a.seg[sg]) +
                 ((static_cast<int64_t>(r.valid ? pb : 0u) * a.interf + a.apod + (r.valid ? px : 0u)) * kN);
-        r.apod_row = static_cast<int64_t>(sg) * B_u + (r.valid ? pb : 0u);
+        r.apod_row = sg * static_cast<unsigned int>(a.B) + (r.valid ? pb : 0u);
         r.as = pas;
         r.tile = 0;
         return r;
     };
     auto static_advance = [&]() {
-        pas += step;
-        px += dx;
-        unsigned int inc = dbt;
-        if (px >= nx_u) {
-            px -= nx_u;
+        const unsigned int nx = static_cast<unsigned int>(a.nx), B = static_cast<unsigned int>(a.B);
+        pas += static_cast<unsigned int>(gridDim.x) * kPerCta;
+        px += a.step_x;
+        unsigned int inc = a.step_bt;
+        if (px >= nx) {
+            px -= nx;
             ++inc;
         }
         pb += inc;
-        if (pb >= B_u) {
-            const unsigned int c = pb / B_u;
+        if (pb >= B) {
+            const unsigned int c = pb / B;
             psg += c;
-            pb -= c * B_u;
+            pb -= c * B;
         }
     };
     // slot r's raw row and apodisation-mean row, copied by the group in
@@ -352,7 +351,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
     };
     auto copy_apod = [&](const SlotRef& r, bool first) {
         if (r.valid) {
-            const float* src = a.apod_mean + r.apod_row * kN;
+            const float* src = a.apod_mean + static_cast<int64_t>(r.apod_row) * kN;
 #pragma unroll
             for (int q = 0; q < 4; ++q) cp_async_cg16(&S.d[g][4 * lt + 512 * q], src + 4 * lt + 512 * q);
         }
@@ -370,11 +369,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
         quad = next_quad(-1);
         if (quad >= 0) {
             const unsigned int as0 = static_cast<unsigned int>(quad) * kPerCta + static_cast<unsigned int>(g);
-            const unsigned int bt = as0 / nx_u;
+            const unsigned int nx = static_cast<unsigned int>(a.nx), B = static_cast<unsigned int>(a.B);
+            const unsigned int bt = as0 / nx;
             pas = as0;
-            px = as0 - bt * nx_u;
-            psg = bt / B_u;
-            pb = bt - psg * B_u;
+            px = as0 - bt * nx;
+            psg = bt / B;
+            pb = bt - psg * B;
             cur = static_slot();
         }
     } else {
@@ -551,7 +551,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
                 for (int r = 0; r < 4; ++r) M[lt + 128 * h + 256 * r] = magv[h][r];
             fence_proxy_async();
             group_sync(g);
-            if (lt == 0 && valid) tma_bulk_s2g(a.out + me.as * kHalf, M, kHalf * sizeof(float));
+            if (lt == 0 && valid) tma_bulk_s2g(a.out + static_cast<int64_t>(me.as) * kHalf, M, kHalf * sizeof(float));
         } else if (Mode == kModeMag || Mode == kModeDb) {
             if (valid) {
 #pragma unroll
@@ -561,12 +561,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
                         const int k = lt + 128 * h + 256 * r;
                         const float mag = magv[h][r];
                         if (Mode == kModeMag) {
-                            a.out[me.as * kHalf + k] = mag;
+                            a.out[static_cast<int64_t>(me.as) * kHalf + k] = mag;
                         } else {
                             const int z = k - a.z0;
                             if (z >= 0 && z < a.nz) {
                                 const float db = 20.0f * log10f(mag);
-                                a.out[me.as * a.nz + z] = db;
+                                a.out[static_cast<int64_t>(me.as) * a.nz + z] = db;
                                 if (isfinite(db)) {
                                     run_min = fminf(run_min, db);
                                     run_max = fmaxf(run_max, db);
@@ -619,7 +619,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
                 const bool in0 = xr >= 0 && s0i >= 0 && s0i < kPerCta, in1 = xr >= 0 && s1i >= 0 && s1i < kPerCta;
                 const float* U0 = reinterpret_cast<const float*>(S.spec[in0 ? s0i : 0]) + kHalf;
                 const float* U1 = reinterpret_cast<const float*>(S.spec[in1 ? s1i : 0]) + kHalf;
-                float* out = tile.out + me.as * tile.nz;
+                float* out = tile.out + static_cast<int64_t>(me.as) * tile.nz;
                 for (int zo = lt; zo < tile.nz; zo += kGroup) {
                     const float4 rw = __ldg(p.zrow + zo);
                     const int zr = __float_as_int(rw.x);
@@ -715,7 +715,12 @@ cudaError_t launch_t(const SpectralArgs& a, int grid, cudaStream_t st) {
     cudaError_t e = cudaFuncSetAttribute(k_spectral<RawT, Mode, U>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(smem));
     if (e != cudaSuccess) return e;
-    k_spectral<RawT, Mode, U><<<grid, kThreads, smem, st>>>(a);
+    // the grid stride of the static schedule in B-scans + A-scans
+    SpectralArgs b = a;
+    const unsigned int step = static_cast<unsigned int>(grid) * kPerCta;
+    b.step_bt = a.nx > 0 ? step / static_cast<unsigned int>(a.nx) : 0u;
+    b.step_x = a.nx > 0 ? step - b.step_bt * static_cast<unsigned int>(a.nx) : 0u;
+    k_spectral<RawT, Mode, U><<<grid, kThreads, smem, st>>>(b);
     return cudaGetLastError();
 }
 
