@@ -21,8 +21,9 @@
 //   (e) inverse FFT of length 2048 in shared memory: Stockham radix 16,16,8,
 //       each radix butterfly in registers (128 threads, 16 points each);
 //   (f) |X[k]| for k < N/2 (spectral.py:153), optionally 20*log10 with a
-//       depth crop and a running min/max for the global clim; magnitudes of
-//       16-bit raws leave by one 4 KiB bulk copy per A-scan from shared memory.
+//       depth crop and a running min/max for the global clim; with 16-bit
+//       raws each A-scan's row (magnitudes, or a dB crop of a multiple of 4
+//       rows) leaves by one bulk copy from shared memory.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -214,9 +215,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
     const int lt = tid % kGroup;       // thread within the A-scan group
     const int warp = tid / 32, lane = tid % 32;
     const int64_t nquads = kQueue ? static_cast<int64_t>(a.total_quads) : (a.n_ascans + kPerCta - 1) / kPerCta;
-    // magnitude mode with 16-bit raws: each A-scan's |X| leaves by one bulk
-    // copy from the free second FFT line (thread 0 of its group issues it)
-    const bool bulk_out = Mode == kModeMag && sizeof(RawT) == 2 && (reinterpret_cast<uintptr_t>(a.out) & 15u) == 0;
+    // magnitude mode, and dB mode with a crop of a multiple of 4 rows, with
+    // 16-bit raws: each A-scan's output row leaves by one bulk copy from the
+    // free second FFT line (thread 0 of its group issues it)
+    const bool bulk_out = (Mode == kModeMag || (Mode == kModeDb && (a.nz & 3) == 0)) && sizeof(RawT) == 2 &&
+                          (reinterpret_cast<uintptr_t>(a.out) & 15u) == 0;
 
     // this thread's shifted sinc weights and source window base; the weights
     // of outputs 4t, 4t+1 (and 4t+2, 4t+3) at window step u form one packed
@@ -541,17 +544,35 @@ __global__ void __launch_bounds__(kThreads, 1) k_spectral(const SpectralArgs a) 
             ifft2048_low_mag_pp(X, S.fft_y[g], S.tw2, S.tw3, g, lt, magv);
         else
             ifft2048_low_mag(X, S.tw2, S.tw3, g, lt, magv);
-        if (Mode == kModeMag && bulk_out) {
-            // the last stage read only X: the second line Y is free for |X[k]|
-            // (k < N/2, contiguous float32), which leaves by one 4 KiB bulk copy
+        if ((Mode == kModeMag || Mode == kModeDb) && bulk_out) {
+            // the last stage read only X: the second line Y is free for the
+            // output row (|X[k]|, k < N/2, or dB of the crop, contiguous
+            // float32), which leaves by one bulk copy
             float* M = reinterpret_cast<float*>(S.fft_y[sizeof(RawT) == 2 ? g : 0]);
 #pragma unroll
             for (int h = 0; h < 2; ++h)
 #pragma unroll
-                for (int r = 0; r < 4; ++r) M[lt + 128 * h + 256 * r] = magv[h][r];
+                for (int r = 0; r < 4; ++r) {
+                    const int k = lt + 128 * h + 256 * r;
+                    if (Mode == kModeMag) {
+                        M[k] = magv[h][r];
+                    } else {
+                        const int z = k - a.z0;
+                        if (z >= 0 && z < a.nz) {
+                            const float db = 20.0f * log10f(magv[h][r]);
+                            M[z] = db;
+                            if (valid && isfinite(db)) {
+                                run_min = fminf(run_min, db);
+                                run_max = fmaxf(run_max, db);
+                            }
+                        }
+                    }
+                }
             fence_proxy_async();
             group_sync(g);
-            if (lt == 0 && valid) tma_bulk_s2g(a.out + static_cast<int64_t>(me.as) * kHalf, M, kHalf * sizeof(float));
+            const int n_row = Mode == kModeMag ? kHalf : a.nz;
+            if (lt == 0 && valid)
+                tma_bulk_s2g(a.out + static_cast<int64_t>(me.as) * n_row, M, static_cast<uint32_t>(n_row) * 4u);
         } else if (Mode == kModeMag || Mode == kModeDb) {
             if (valid) {
 #pragma unroll
