@@ -809,7 +809,7 @@ cudaError_t set_wait_test_spectral(unsigned long long limit_ns, int starve, cuda
 int spectral_max_ctas_per_sm(int dtype, int mode) {
     (void)dtype;
     (void)mode;
-    return 1;   // 512 threads, ~155 KB shared memory, 128 registers: one CTA per SM
+    return 1;   // 512 threads, ~219 KB shared memory, 128 registers: one CTA per SM
 }
 
 size_t spectral_smem_bytes(int dtype) {
