@@ -287,7 +287,7 @@ int octgb_graph_launch(octgb_ctx *ctx, int graph_id);
  * runs the spectral kernel (which = 0) or the precision form's tensor-core
  * sinc (which = 1, integer raws; needs a geometry with precision tiles) on a
  * small internal batch of zero raws, with the waits' limit cut to
- * wait_limit_us (100 .. 2 000 000) and each CTA's first bulk-copy barrier
+ * wait_limit_us (100 .. 2 000 000) and each CTA's first row-copy barrier
  * expecting 16 bytes more than its copies deliver.  Every copy still lands;
  * only that barrier never completes, so the wait runs out, the kernel drains
  * what it issued (and frees its tensor memory) and reports through the status
