@@ -53,9 +53,9 @@ sys.path.insert(0, str(ROOT))
 METRIC = "A-scans/s on 1 GB300 (fused vs plain FP32; learned vs search β) at ≤1 LSB"
 APOD = 25
 # DRAM bytes per A-scan of the spectral kernel from one ncu capture
-# (profiles/k_spectral_config1_small.md: (49.44 + 7.00) MB over 12 000 A-scans;
+# (profiles/k_spectral_config1_small.md: (49.43 + 7.16) MB over 12 000 A-scans;
 # caches flushed before the kernel, magnitudes partly still in L2 at its end)
-SPECTRAL_DRAM_BYTES_PER_ASCAN = (49.435136e6 + 7.001344e6) / 12000
+SPECTRAL_DRAM_BYTES_PER_ASCAN = (49.433856e6 + 7.155456e6) / 12000
 
 
 # ------------------------------------------------------------------------ workload description
